@@ -1,0 +1,155 @@
+"""Generate golden vectors by running the unmodified OOPAO reference.
+
+Run in a container that holds the reference source tree:
+
+    python tests/golden/make_golden.py [/path/to/OOPAO/project]
+
+It imports the reference through ``refimport.import_reference`` (display and
+I/O dependencies stubbed), builds Telescope / Source / DeformableMirror /
+Pyramid objects exactly as a user script does, propagates seeded inputs with
+``ngs**tel*dm*wfs`` (or ``wfs.wfs_measure``), and stores inputs and outputs
+in ``tests/golden/<case>.npz``.  The reference always computes in float64.
+
+Inputs are stored in the fixtures (rather than regenerated from seeds) so the
+tests never depend on a random-number stream.
+"""
+import contextlib
+import io
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+
+def _quiet():
+    return contextlib.redirect_stdout(io.StringIO())
+
+
+def screen(res, seed, rms_rad):
+    """Seeded smooth random phase map (power-law spectrum), rms in radians."""
+    rng = np.random.default_rng(seed)
+    f = np.fft.fftfreq(res)
+    fx, fy = np.meshgrid(f, f)
+    fr = np.sqrt(fx ** 2 + fy ** 2)
+    fr[0, 0] = 1.0
+    spec = fr ** (-11 / 6)
+    spec[0, 0] = 0
+    ph = np.real(np.fft.ifft2(spec * (rng.standard_normal((res, res)) + 1j * rng.standard_normal((res, res)))))
+    ph -= ph.mean()
+    return ph / ph.std() * rms_rad
+
+
+def build(OOPAO, res, n_subap, modulation, light_ratio, co=0.0, diameter=8.0, **wfs_kw):
+    from OOPAO.Telescope import Telescope
+    from OOPAO.Source import Source
+    from OOPAO.DeformableMirror import DeformableMirror
+    from OOPAO.Pyramid import Pyramid
+    with _quiet():
+        tel = Telescope(resolution=res, diameter=diameter, samplingTime=1e-3, centralObstruction=co)
+        ngs = Source(optBand='V0', magnitude=8)
+        ngs * tel
+        dm = DeformableMirror(tel, nSubap=n_subap, mechCoupling=0.35)
+        wfs = Pyramid(nSubap=n_subap, telescope=tel, modulation=modulation, lightRatio=light_ratio,
+                      **wfs_kw)
+    return tel, ngs, dm, wfs
+
+
+def measure_dm(tel, ngs, dm, wfs, coefs):
+    with _quiet():
+        dm.coefs = coefs
+        ngs ** tel * dm * wfs
+    return dict(raw=np.array(wfs.raw_data), frame=np.array(wfs.cam.frame),
+                signal=np.array(wfs.signal), signal_2D=np.array(wfs.signal_2D),
+                phase=np.array(ngs.phase))
+
+
+def measure_phase(tel, ngs, dm, wfs, phase):
+    with _quiet():
+        dm.coefs = 0
+        ngs ** tel
+        wfs.wfs_measure(phase_in=phase)
+    return dict(raw=np.array(wfs.raw_data), frame=np.array(wfs.cam.frame),
+                signal=np.array(wfs.signal), signal_2D=np.array(wfs.signal_2D))
+
+
+def geometry_record(tel, ngs, dm, wfs):
+    return dict(
+        pupil=np.array(tel.pupil), intensity=np.array(ngs.intensity), wavelength=ngs.wavelength,
+        N=wfs.resolution, cam=wfs.cam.resolution, n_theta=wfs.nTheta, n_signal=wfs.nSignal,
+        valid_i4q=np.array(wfs.validI4Q), reference_2d=np.array(wfs.referenceSignal_2D),
+        n_act=dm.nValidAct, modulation_path=np.array(wfs.modulation_path if wfs.modulation != 0 or wfs.user_modulation_path is not None else np.zeros((1, 2))),
+    )
+
+
+def case_small(OOPAO, name, res, n_subap, modulation, light_ratio, co=0.0, full=True, n_im=6,
+               seeds=(1, 2), **kw):
+    tel, ngs, dm, wfs = build(OOPAO, res, n_subap, modulation, light_ratio, co=co, **kw)
+    rec = geometry_record(tel, ngs, dm, wfs)
+    import json
+    rec['params'] = json.dumps(dict(res=res, n_subap=n_subap, modulation=modulation,
+                                    light_ratio=light_ratio, co=co, **kw))
+    if full and res <= 32:
+        rec['mask'] = np.array(wfs.mask)
+        rec['tt'] = np.array(wfs.phaseBuffModulationLowres) if wfs.modulation != 0 else np.zeros((1, res, res), np.float32)
+        rec['phasor'] = np.array(wfs.phasor)
+        rec['modes'] = np.array(dm.modes)
+    rng = np.random.default_rng(seeds[0])
+    coefs = rng.standard_normal(dm.nValidAct) * 60e-9
+    out = measure_dm(tel, ngs, dm, wfs, coefs)
+    rec['dm_coefs'] = coefs
+    for k, v in out.items():
+        if k == 'raw' and not full:
+            continue
+        rec['dm_' + k] = v
+    ph = screen(res, seeds[1], 2.0) * tel.pupil
+    out = measure_phase(tel, ngs, dm, wfs, ph)
+    rec['screen_phase'] = ph
+    for k, v in out.items():
+        if k == 'raw' and not full:
+            continue
+        rec['screen_' + k] = v
+    if n_im:
+        from OOPAO.calibration.InteractionMatrix import InteractionMatrix
+        m2c = np.eye(dm.nValidAct)[:, :n_im]
+        with _quiet():
+            calib = InteractionMatrix(ngs, tel, dm, wfs, M2C=m2c, stroke=1e-8, nMeasurements=4,
+                                      single_pass=True)
+            calib_pp = InteractionMatrix(ngs, tel, dm, wfs, M2C=m2c, stroke=1e-8, nMeasurements=1,
+                                         single_pass=False)
+        rec['im_m2c'] = m2c
+        rec['im_D'] = np.array(calib.D)
+        rec['im_M'] = np.array(calib.M)
+        rec['im_pp_D'] = np.array(calib_pp.D)
+    if not full or res > 32:
+        # influence-function summaries (the full matrix is too large to store)
+        rec['modes_colsum'] = dm.modes.sum(axis=0)
+        rec['modes_col0'] = dm.modes[:, 0]
+        rec['modes_sq'] = float((dm.modes ** 2).sum())
+        rec['mask_real_sum'] = float(np.real(wfs.mask).astype(np.float64).sum())
+        rec['mask_imag_sum'] = float(np.imag(wfs.mask).astype(np.float64).sum())
+        rec['mask_row0'] = np.array(wfs.mask[0])
+        rec['mask_col_mid'] = np.array(wfs.mask[:, wfs.resolution // 2 - 3])
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **rec)
+    print(name, 'N', rec['N'], 'cam', rec['cam'], 'K', rec['n_theta'], 'nSignal', rec['n_signal'],
+          'nAct', rec['n_act'])
+
+
+def main():
+    from refimport import import_reference
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+    OOPAO = import_reference(ref_root)
+    case_small(OOPAO, 'tiny', 24, 4, 3, 0.5)
+    case_small(OOPAO, 'tiny_nocenter', 24, 4, 2, 0.5, psfCentering=False, n_im=0)
+    case_small(OOPAO, 'tiny_rooftop', 24, 4, 2, 0.3, rooftop=0.5, theta_rotation=0.1,
+               nTheta_user_defined=8, n_im=0)
+    case_small(OOPAO, 'tiny_nomod', 32, 4, 0, 0.2, co=0.25, n_im=0, n_pix_separation=4)
+    case_small(OOPAO, 'small_sep', 40, 10, 2, 0.5, n_pix_separation=4, n_pix_edge=2,
+               nTheta_user_defined=12, n_im=4)
+    case_small(OOPAO, 'c1', 120, 20, 3, 0.5, full=False, n_im=3, nTheta_user_defined=48)
+
+
+if __name__ == '__main__':
+    main()
