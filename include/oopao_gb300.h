@@ -1,0 +1,127 @@
+/*
+ * oopao_gb300 — C ABI of the GB300 (sm_103a) modulated pyramid wavefront
+ * sensor and deformable-mirror influence-function projection.
+ *
+ * All array arguments are plain pointers.  "host" pointers are read during
+ * the call only; "device" pointers must be CUDA device memory on the current
+ * device.  `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ * stream).  Every function returns OOPAO_OK (0) or an OOPAO_ERR_* code; the
+ * message of the last failure on the calling thread is in oopao_last_error().
+ * Compute calls are asynchronous with respect to the host.
+ *
+ * Layouts: 2-D maps are row-major [row][col]; complex values are interleaved
+ * (re, im) float pairs; batched maps are [batch][row][col].
+ *
+ * Each entry point names the reference (cheritier/OOPAO) interface whose
+ * computation it replaces; paths are relative to the OOPAO project root.
+ */
+#ifndef OOPAO_GB300_H
+#define OOPAO_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  OOPAO_OK = 0,
+  OOPAO_ERR_INVALID = 1,      /* bad argument (size, pointer, mode) */
+  OOPAO_ERR_UNSUPPORTED = 2,  /* e.g. FFT size with a prime factor > 13 */
+  OOPAO_ERR_CUDA = 3,         /* a CUDA runtime call failed */
+  OOPAO_ERR_WORKSPACE = 4     /* workspace smaller than one batch item needs */
+};
+
+/* Library ABI version (incremented on any signature change). */
+int oopao_abi_version(void);
+/* Message of the last error on this thread ("" if none). */
+const char* oopao_last_error(void);
+
+/* ------------------------------------------------------------------------
+ * Pyramid wavefront sensor plan.
+ * Replaces the geometry built by Pyramid.__init__ (OOPAO/Pyramid.py:26-366):
+ * FFT grid n_fft (:276-279), camera size cam (:285), centring phasor
+ * (:342-344), complex64 mask (:368-391) and the modulation path (:1112-1139).
+ * ------------------------------------------------------------------------ */
+typedef struct oopao_pwfs_plan oopao_pwfs_plan;
+
+/* mask_host: [n_fft*n_fft] complex64 (interleaved floats), the pyramid mask
+ *   (already multiplied by any spatial filter).
+ * tt_path_host: [2*n_theta] modulation points (x_k, y_k) in lambda/D, or NULL
+ *   with n_theta == 1 for the non-modulated sensor.
+ * tt_scale: telescope.resolution / telescope.initial_resolution (:336-339).
+ * psf_centering: 1 = mask centred on 4 pixels (phasor), 0 = on 1 pixel
+ *   (fftshift of the focal field, :632-639). */
+int oopao_pwfs_plan_create(oopao_pwfs_plan** plan, int res, int n_fft, int cam, int n_theta,
+                           const float* mask_host, const double* tt_path_host, double tt_scale,
+                           int psf_centering);
+int oopao_pwfs_plan_destroy(oopao_pwfs_plan* plan);
+
+/* Pupil amplitude sqrt(src.intensity / nTheta) [res*res] (OOPAO/Pyramid.py:674). */
+int oopao_pwfs_set_amplitude(oopao_pwfs_plan* plan, const float* amp_host);
+/* Optional per-point weights [n_theta] (Pyramid.weight_vector, :750-755);
+ * NULL restores the plain sum. */
+int oopao_pwfs_set_weights(oopao_pwfs_plan* plan, const float* weights_host);
+/* Launch shape (autotuner hook): lines per CTA of the three FFT passes and
+ * the number of partial sums over modulation points.  0 keeps a value. */
+int oopao_pwfs_set_launch(oopao_pwfs_plan* plan, int rows_per_cta, int cols_per_cta,
+                          int inv_rows_per_cta, int ksplit);
+
+/* Bytes of device workspace oopao_pwfs_measure needs for `batch` items
+ * processed in one chunk (a smaller workspace makes it loop over chunks;
+ * it must hold at least one item). */
+size_t oopao_pwfs_workspace_bytes(const oopao_pwfs_plan* plan, int batch);
+
+/* Modulated propagation + detector binning.
+ * Replaces Pyramid.wfs_measure / pyramid_transform (OOPAO/Pyramid.py:612-833)
+ * and the noise-free camera sum-binning (Pyramid.__mul__ :1178-1203,
+ * tools.set_binning OOPAO/tools/tools.py:464-483).
+ * opd: device [batch][res][res] float32; the phase is opd*phase_scale
+ *   (phase_scale = 2*pi/lambda for an OPD in metres, 1 for a phase in rad).
+ * frame: device [batch][cam][cam] float32 (required).
+ * raw: device [batch][n_fft][n_fft] float32 raw_data, or NULL. */
+int oopao_pwfs_measure(const oopao_pwfs_plan* plan, const float* opd, double phase_scale,
+                       int batch, float* frame, float* raw, void* workspace,
+                       size_t workspace_bytes, void* stream);
+
+/* Signal-processing setup (Pyramid.initialization / signalProcessing,
+ * OOPAO/Pyramid.py:541-589, :835-926, grabQuadrant :946-961).
+ * mode: 0 slopesMaps, 1 slopesMaps_incidence_flux, 2 slopesMaps_camera_flux,
+ *       3 fullFrame, 4 fullFrame_incidence_flux, 5 fullFrame_camera_flux,
+ *       6 fullFrame_sum_flux.
+ * n_quad: quadrant size (slopes modes); quad_origin_host: [8] (row, col) of
+ *   the top-left pixel of quadrants 1..4 in the camera frame.
+ * valid_host: [n_quad*n_quad] validI4Q (slopes) or [cam*cam] validSignal
+ *   (full frame), 0/1 bytes.
+ * ref2d_host: referenceSignal_2D [2*n_quad*n_quad] or [cam*cam], or NULL (0).
+ * norma_const: the flux normalisation of the *_incidence_flux modes. */
+int oopao_pwfs_set_signal_processing(oopao_pwfs_plan* plan, int mode, int n_quad,
+                                     const int* quad_origin_host, const unsigned char* valid_host,
+                                     const float* ref2d_host, double slopes_units,
+                                     double norma_const);
+/* Number of entries of wfs.signal for the current valid map. */
+int oopao_pwfs_n_signal(const oopao_pwfs_plan* plan);
+
+/* wfs.signal_2D / wfs.signal from camera frames (signalProcessing).
+ * frame: device [batch][cam][cam]; signal_2d: device [batch][2*n_quad][n_quad]
+ * (slopes) or [batch][cam][cam] (full frame); signal: device
+ * [batch][n_signal]; norma: device [batch] or NULL. */
+int oopao_pwfs_signal(const oopao_pwfs_plan* plan, const float* frame, int batch,
+                      float* signal_2d, float* signal, float* norma, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Deformable mirror influence-function projection.
+ * Replaces the dm.coefs setter OPD = modes @ coefs
+ * (OOPAO/DeformableMirror.py:651-686).
+ * modes_t: device [n_act][n_pix] float32 (the transpose of dm.modes).
+ * coefs: device [n_act][batch] float32 (the layout of a 2-D dm.coefs).
+ * opd: device [batch][n_pix] float32 = (modes @ coefs)^T * scale.
+ * ------------------------------------------------------------------------ */
+int oopao_dm_opd_f32(const float* modes_t, const float* coefs, int n_act, int n_pix, int batch,
+                     float scale, float* opd, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OOPAO_GB300_H */

@@ -1,0 +1,85 @@
+"""ctypes binding of the in-tree C-ABI library (``include/oopao_gb300.h``).
+
+The library is the only compute path: there is no CPU fallback.  Loading
+fails with an exception when the library has not been built, and every
+status code other than OOPAO_OK raises ``OopaoError``.
+"""
+import ctypes
+import os
+
+from .tools import OopaoError
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, '_lib', 'liboopao_gb300.so')
+
+c_int, c_float, c_double, c_size_t, c_void_p = (ctypes.c_int, ctypes.c_float, ctypes.c_double,
+                                                 ctypes.c_size_t, ctypes.c_void_p)
+P = ctypes.POINTER
+
+# name -> (restype, argtypes); mirrors include/oopao_gb300.h
+SIGNATURES = {
+    'oopao_abi_version': (c_int, []),
+    'oopao_last_error': (ctypes.c_char_p, []),
+    'oopao_pwfs_plan_create': (c_int, [P(c_void_p), c_int, c_int, c_int, c_int, c_void_p, c_void_p,
+                                       c_double, c_int]),
+    'oopao_pwfs_plan_destroy': (c_int, [c_void_p]),
+    'oopao_pwfs_set_amplitude': (c_int, [c_void_p, c_void_p]),
+    'oopao_pwfs_set_weights': (c_int, [c_void_p, c_void_p]),
+    'oopao_pwfs_set_launch': (c_int, [c_void_p, c_int, c_int, c_int, c_int]),
+    'oopao_pwfs_workspace_bytes': (c_size_t, [c_void_p, c_int]),
+    'oopao_pwfs_measure': (c_int, [c_void_p, c_void_p, c_double, c_int, c_void_p, c_void_p, c_void_p,
+                                   c_size_t, c_void_p]),
+    'oopao_pwfs_set_signal_processing': (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                                 c_double, c_double]),
+    'oopao_pwfs_n_signal': (c_int, [c_void_p]),
+    'oopao_pwfs_signal': (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    'oopao_dm_opd_f32': (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_float, c_void_p, c_void_p]),
+}
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load the library once (``OopaoError`` if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OopaoError('oopao_gb300 CUDA library not built (%s); run '
+                         '`python -m oopao_gb300.build`' % path)
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status, what=''):
+    if status != 0:
+        msg = load().oopao_last_error().decode(errors='replace')
+        raise OopaoError('%s failed (status %d): %s' % (what, status, msg))
+
+
+def call(name, *args):
+    lib = load()
+    st = getattr(lib, name)(*args)
+    if SIGNATURES[name][0] is c_int and name not in ('oopao_abi_version', 'oopao_pwfs_n_signal'):
+        check(st, name)
+    return st
+
+
+def ptr(t):
+    """Device/host address of a torch tensor or numpy array (None -> NULL)."""
+    if t is None:
+        return None
+    if hasattr(t, 'data_ptr'):
+        return t.data_ptr()
+    return t.ctypes.data
+
+
+def stream_handle(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream

@@ -1,0 +1,144 @@
+"""Interaction matrix and reconstructor: drop-ins for the reference
+``InteractionMatrix`` (``OOPAO/calibration/InteractionMatrix.py:13-169``) and
+``CalibrationVault`` (``OOPAO/calibration/CalibrationVault.py:14-122``).
+
+``InteractionMatrix`` keeps the reference signature and column rule
+(column = factor * 0.5 * (s+ - s-) / stroke, factor 2 and s- = 0 for
+``single_pass``).  Three GPU schedules compute the same matrix:
+
+* ``method='batched'`` (default): the DM projection of a chunk of modes
+  (one GEMM) feeds one batched pyramid launch over all (mode, modulation
+  point) pairs of the chunk; nothing returns to the host until the end.
+* ``method='per_mode'``: the plain schedule, one mode at a time through the
+  public operator path ``dm.coefs = c; ngs**tel*dm*wfs`` (push, then pull).
+* ``method='jvp'``: columns from the hand-written tangent of the sensor
+  (``oopao_gb300.autodiff``), exact in the limit stroke -> 0.
+
+The SVD of ``CalibrationVault`` runs in float64 on the GPU.
+"""
+import time
+
+import numpy as np
+import torch
+
+from .tools import OopaoError
+
+
+class CalibrationVault:
+    def __init__(self, D, nTrunc: int = 0, display: bool = False, print_details: bool = False,
+                 invert: bool = True):
+        if invert:
+            dev = torch.device('cuda', torch.cuda.current_device()) if torch.cuda.is_available() else None
+            if dev is None:
+                raise OopaoError('CalibrationVault needs a CUDA device')
+            Dt = torch.as_tensor(np.asarray(D, dtype=np.float64), device=dev)
+            U, s, Vh = torch.linalg.svd(Dt, full_matrices=False)
+            U, s, V = U.cpu().numpy(), s.cpu().numpy(), Vh.cpu().numpy()
+            self.s = s
+            self.S = np.diag(s)
+            self.eigenValues = s
+            self.D = U @ self.S @ V
+            self.U = np.transpose(U)
+            self.V = V
+            self._nTrunc = nTrunc
+            n_ev = len(s) - nTrunc
+            self.iS = np.diag(1 / self.eigenValues)
+            self.M = np.transpose(self.V) @ self.iS @ self.U
+            self._truncate(n_ev)
+        else:
+            self.D = D
+
+    def _truncate(self, n_ev):
+        self.iStrunc = np.diag(1 / self.eigenValues[:n_ev])
+        self.Vtrunc = self.V[:n_ev, :]
+        self.Utrunc = self.U[:n_ev, :]
+        self.VtruncT = np.transpose(self.Vtrunc)
+        self.UtruncT = np.transpose(self.Utrunc)
+        self.Mtrunc = self.VtruncT @ self.iStrunc @ self.Utrunc
+        self.Dtrunc = self.UtruncT @ np.diag(self.eigenValues[:n_ev]) @ self.Vtrunc
+        self.cond = self.eigenValues[0] / self.eigenValues[(-self._nTrunc - 1)]
+
+    @property
+    def nTrunc(self):
+        return self._nTrunc
+
+    @nTrunc.setter
+    def nTrunc(self, val):
+        self._nTrunc = val
+        self._truncate(len(self.s) - val)
+
+
+def _signals_batched(ngs, tel, dm, wfs, commands, phase_offset=None):
+    """Device signals [B, nSignal] for DM command columns [nAct, B]."""
+    dev = wfs._dev
+    c = torch.as_tensor(np.ascontiguousarray(commands, dtype=np.float32), device=dev)
+    scale = 2 * np.pi / ngs.wavelength
+    out = []
+    B = c.shape[1]
+    step = max(1, wfs.max_batch)
+    for b0 in range(0, B, step):
+        cb = c[:, b0:b0 + step].contiguous()
+        opd = dm.opd_device(cb)
+        if phase_offset is not None:
+            opd = opd + torch.as_tensor(np.asarray(phase_offset) / scale, dtype=torch.float32, device=dev)
+        frame, _ = wfs._measure_frames(opd, scale)
+        frame = wfs.cam._integrate_device(frame)
+        _, sig = wfs._signals(frame)
+        out.append(sig)
+    return torch.cat(out, dim=0)
+
+
+def InteractionMatrix(ngs, tel, dm, wfs, M2C, stroke, atm=None, phaseOffset=0, nMeasurements=50,
+                      noise='off', invert=True, nTrunc=0, print_time=False, display=False,
+                      single_pass=True, method='batched'):
+    if noise == 'off':
+        wfs.cam.photonNoise = 0
+        wfs.cam.readoutNoise = 0
+        wfs.cam.backgroundNoise = 0
+    tel.isPaired = False
+    ngs ** tel
+    M2C = np.asarray(M2C)
+    if M2C.ndim == 1:
+        M2C = M2C[:, None]
+    n_modes = M2C.shape[1]
+    t0 = time.time()
+    if method == 'batched':
+        if not np.isscalar(phaseOffset) or phaseOffset != 0:
+            off = np.asarray(phaseOffset)
+        else:
+            off = None
+        sp = _signals_batched(ngs, tel, dm, wfs, M2C * stroke, off)
+        if single_pass:
+            intmat = (0.5 * sp / stroke).T
+            factor = 2
+        else:
+            sm = _signals_batched(ngs, tel, dm, wfs, -M2C * stroke, off)
+            intmat = (0.5 * (sp - sm) / stroke).T
+            factor = 1
+        intmat = intmat.double().cpu().numpy()
+    elif method == 'per_mode':
+        intmat = np.zeros([wfs.nSignal, n_modes])
+        for i in range(n_modes):
+            dm.coefs = M2C[:, i] * stroke
+            ngs ** tel * dm * wfs
+            s_plus = wfs.device_signal
+            if single_pass:
+                col = 0.5 * s_plus / stroke
+                factor = 2
+            else:
+                dm.coefs = -M2C[:, i] * stroke
+                ngs ** tel * dm * wfs
+                col = 0.5 * (s_plus - wfs.device_signal) / stroke
+                factor = 1
+            intmat[:, i] = col.double().cpu().numpy()
+    elif method == 'jvp':
+        from .autodiff import jvp_interaction_matrix
+        intmat = jvp_interaction_matrix(ngs, tel, dm, wfs, M2C).double().cpu().numpy()
+        factor = 1
+    else:
+        raise OopaoError('unknown InteractionMatrix method %r' % method)
+    if print_time:
+        print('Interaction matrix: %d modes in %.3f s' % (n_modes, time.time() - t0))
+    dm.coefs = 0
+    ngs ** tel
+    return CalibrationVault(factor * intmat, invert=invert, nTrunc=nTrunc)

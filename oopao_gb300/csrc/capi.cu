@@ -1,0 +1,18 @@
+// Error reporting and version entry points of the C ABI.
+#include <stdio.h>
+#include <string.h>
+
+#include "common.cuh"
+
+namespace {
+thread_local char g_last_error[512] = "";
+}
+
+void oopao_set_last_error(const char* msg, const char* file, int line) {
+  const char* base = strrchr(file, '/');
+  snprintf(g_last_error, sizeof(g_last_error), "%s (%s:%d)", msg ? msg : "", base ? base + 1 : file, line);
+}
+
+extern "C" int oopao_abi_version(void) { return 1; }
+
+extern "C" const char* oopao_last_error(void) { return g_last_error; }

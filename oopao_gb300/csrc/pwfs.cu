@@ -1,0 +1,619 @@
+// Modulated pyramid WFS propagation on GB300 (sm_103a).
+//
+// Per modulation point k the reference computes (OOPAO/Pyramid.py:612-646)
+//     E_k = A * exp(i (phi + TT_k))          placed at rows/cols [off, off+res)
+//     F_k = fft2(E_k * phasor)               N x N
+//     G_k = ifft2(F_k * mask)
+//     raw = sum_k |G_k|^2                    (:741-751)
+// and the camera sums raw over N/cam x N/cam blocks (:1178-1203).
+//
+// The phasor exp(-i pi (N+1)/N (x+y)) and the modulation tilt
+// x_k*Tip + y_k*Tilt are both separable in (row, col), so E_k*phasor =
+// A e^{i phi} * rowfac_k[col] * colfac_k[row].  The 2-D transforms are split
+// into three fused passes over shared-memory line FFTs (fft.cuh):
+//   pass 1 (rows_fwd):  build the field for `res` non-zero rows, forward
+//                       row FFT, store Y[b,k] (res x N).
+//   pass 2 (cols):      per column: gather the res non-zero entries, forward
+//                       FFT, multiply the mask column, inverse FFT, store
+//                       Z[b,k] (N x N).
+//   pass 3 (rows_inv):  per row: inverse FFT of Z rows for a range of points,
+//                       accumulate |.|^2 over them, store a partial sum.
+//   pass 4 (bin):       sum the partials, bin N/cam x N/cam -> camera frame,
+//                       optionally write raw_data.
+// The 1/N^2 of numpy's ifft2 is folded into rowfac.
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+#include "fft.cuh"
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr size_t kSmemLimit = 227 * 1024;
+
+}  // namespace
+
+struct oopao_pwfs_plan {
+  int device;
+  int res, n, cam, k, bin, off;
+  int psf_centering;
+  FftPlan fft;
+  float2* d_tw;      // [n]      exp(-2 pi i t / n)
+  float2* d_mask;    // [n*n]
+  float2* d_rowfac;  // [k*res]  exp(i x_k t_j s) rho(j+off) / n^2
+  float2* d_colfac;  // [k*res]  exp(i y_k t_i s) rho(i+off)
+  float* d_amp;      // [res*res]
+  float* d_weights;  // [k] or null
+  // launch shape
+  int rows_per_cta, cols_per_cta, inv_rows_per_cta, ksplit;
+  // signal processing
+  int sp_mode, nq, n2d, n_signal, cam2;
+  int q_r0[4], q_c0[4];
+  float slopes_units, norma_const;
+  unsigned char* d_valid;
+  float* d_ref2d;
+  int* d_sig_index;
+};
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
+
+struct RowsFwdArgs {
+  FftPlan fft;
+  const float2* tw;
+  const float* opd;     // [B][res][res]
+  float phase_scale;
+  const float* amp;     // [res][res]
+  const float2* rowfac; // [K][res]
+  const float2* colfac; // [K][res]
+  float2* y;            // [B][K][res][n]
+  int res, n, k, off, lines;
+};
+
+__global__ void __launch_bounds__(kThreads) pwfs_rows_fwd(RowsFwdArgs a) {
+  extern __shared__ float2 smem[];
+  const int n = a.n;
+  float2* tw = smem;
+  float2* buf0 = smem + n;
+  float2* buf1 = buf0 + a.lines * n;
+  const int tid = threadIdx.x;
+  const int b = blockIdx.z, kk = blockIdx.y, i0 = blockIdx.x * a.lines;
+  const int nl = min(a.lines, a.res - i0);
+  for (int t = tid; t < n; t += blockDim.x) tw[t] = a.tw[t];
+  const float* opd = a.opd + (size_t)b * a.res * a.res;
+  const float2* rf = a.rowfac + (size_t)kk * a.res;
+  const float2* cf = a.colfac + (size_t)kk * a.res;
+  for (int idx = tid; idx < a.lines * n; idx += blockDim.x) {
+    const int line = idx / n;
+    const int x = idx - line * n;
+    const int j = x - a.off;
+    float2 v = make_float2(0.f, 0.f);
+    if (line < nl && j >= 0 && j < a.res) {
+      const int i = i0 + line;
+      const float am = a.amp[i * a.res + j];
+      if (am != 0.f) {
+        float s, c;
+        sincosf(opd[i * a.res + j] * a.phase_scale, &s, &c);
+        v = cmul(cmul(make_float2(am * c, am * s), rf[j]), cf[i]);
+      }
+    }
+    buf0[idx] = v;
+  }
+  __syncthreads();
+  float2* out = fft_lines<false>(buf0, buf1, a.fft, tw, nl, n, tid, blockDim.x);
+  float2* y = a.y + (((size_t)b * a.k + kk) * a.res + i0) * n;
+  for (int idx = tid; idx < nl * n; idx += blockDim.x) y[idx] = out[idx];
+}
+
+struct ColsArgs {
+  FftPlan fft;
+  const float2* tw;
+  const float2* mask;  // [n][n]
+  const float2* y;     // [B][K][res][n]
+  float2* z;           // [B][K][n][n]
+  int res, n, k, off, cols;
+};
+
+__global__ void __launch_bounds__(kThreads) pwfs_cols(ColsArgs a) {
+  extern __shared__ float2 smem[];
+  const int n = a.n, C = a.cols;
+  float2* tw = smem;
+  float2* buf0 = smem + n;
+  float2* buf1 = buf0 + C * n;
+  const int tid = threadIdx.x;
+  const int b = blockIdx.z, kk = blockIdx.y, c0 = blockIdx.x * C;
+  for (int t = tid; t < n; t += blockDim.x) tw[t] = a.tw[t];
+  const float2* y = a.y + ((size_t)b * a.k + kk) * a.res * n;
+  // gather: column c of the tile becomes line c; rows outside [off, off+res) are zero
+  for (int idx = tid; idx < C * n; idx += blockDim.x) {
+    const int c = idx % C;
+    const int r = idx / C;
+    const int i = r - a.off;
+    float2 v = make_float2(0.f, 0.f);
+    if (c0 + c < n && i >= 0 && i < a.res) v = y[(size_t)i * n + c0 + c];
+    buf0[c * n + r] = v;
+  }
+  __syncthreads();
+  float2* f = fft_lines<false>(buf0, buf1, a.fft, tw, C, n, tid, blockDim.x);
+  float2* other = (f == buf0) ? buf1 : buf0;
+  for (int idx = tid; idx < C * n; idx += blockDim.x) {
+    const int c = idx % C;
+    const int r = idx / C;
+    if (c0 + c < n) f[c * n + r] = cmul(f[c * n + r], a.mask[(size_t)r * n + c0 + c]);
+  }
+  __syncthreads();
+  float2* g = fft_lines<true>(f, other, a.fft, tw, C, n, tid, blockDim.x);
+  float2* z = a.z + ((size_t)b * a.k + kk) * n * n;
+  for (int idx = tid; idx < C * n; idx += blockDim.x) {
+    const int c = idx % C;
+    const int r = idx / C;
+    if (c0 + c < n) z[(size_t)r * n + c0 + c] = g[c * n + r];
+  }
+}
+
+struct RowsInvArgs {
+  FftPlan fft;
+  const float2* tw;
+  const float2* z;       // [B][K][n][n]
+  const float* weights;  // [K] or null
+  float* partial;        // [B][ksplit][n][n]
+  int n, k, lines, ksplit;
+};
+
+__global__ void __launch_bounds__(kThreads) pwfs_rows_inv(RowsInvArgs a) {
+  extern __shared__ float2 smem[];
+  const int n = a.n;
+  float2* tw = smem;
+  float2* buf0 = smem + n;
+  float2* buf1 = buf0 + a.lines * n;
+  float* acc = reinterpret_cast<float*>(buf1 + a.lines * n);
+  const int tid = threadIdx.x;
+  const int b = blockIdx.z, slot = blockIdx.y, r0 = blockIdx.x * a.lines;
+  const int nl = min(a.lines, n - r0);
+  const int kbeg = (int)(((long long)slot * a.k) / a.ksplit);
+  const int kend = (int)(((long long)(slot + 1) * a.k) / a.ksplit);
+  for (int t = tid; t < n; t += blockDim.x) tw[t] = a.tw[t];
+  for (int idx = tid; idx < a.lines * n; idx += blockDim.x) acc[idx] = 0.f;
+  for (int kk = kbeg; kk < kend; kk++) {
+    const float2* z = a.z + (((size_t)b * a.k + kk) * n + r0) * n;
+    for (int idx = tid; idx < nl * n; idx += blockDim.x) buf0[idx] = z[idx];
+    __syncthreads();
+    float2* g = fft_lines<true>(buf0, buf1, a.fft, tw, nl, n, tid, blockDim.x);
+    const float w = a.weights ? a.weights[kk] : 1.f;
+    for (int idx = tid; idx < nl * n; idx += blockDim.x) acc[idx] = fmaf(w, cabs2(g[idx]), acc[idx]);
+    __syncthreads();
+  }
+  float* p = a.partial + (((size_t)b * a.ksplit + slot) * n + r0) * n;
+  for (int idx = tid; idx < nl * n; idx += blockDim.x) p[idx] = acc[idx];
+}
+
+// One CTA per (camera row, batch item); thread = camera column.  Also writes
+// raw_data rows (sum of partials) when requested.
+__global__ void pwfs_bin(const float* __restrict__ partial, float* __restrict__ frame,
+                         float* __restrict__ raw, int n, int cam, int bin, int ksplit) {
+  const int b = blockIdx.y, cy = blockIdx.x;
+  const float* p = partial + (size_t)b * ksplit * n * n;
+  if (raw) {
+    for (int idx = threadIdx.x; idx < bin * n; idx += blockDim.x) {
+      const int y = cy * bin + idx / n, x = idx % n;
+      float s = 0.f;
+      for (int q = 0; q < ksplit; q++) s += p[((size_t)q * n + y) * n + x];
+      raw[((size_t)b * n + y) * n + x] = s;
+    }
+  }
+  for (int cx = threadIdx.x; cx < cam; cx += blockDim.x) {
+    float s = 0.f;
+    for (int dy = 0; dy < bin; dy++) {
+      float row = 0.f;
+      for (int dx = 0; dx < bin; dx++) {
+        float v = 0.f;
+        for (int q = 0; q < ksplit; q++) v += p[((size_t)q * n + cy * bin + dy) * n + cx * bin + dx];
+        row += v;
+      }
+      s += row;
+    }
+    frame[((size_t)b * cam + cy) * cam + cx] = s;
+  }
+}
+
+// Deterministic block sum (fixed tree for a fixed blockDim).
+__device__ float block_sum(float v, float* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  float t = 0.f;
+  if (w == 0) {
+    t = (l < nw) ? red[l] : 0.f;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (l == 0) red[32] = t;
+  }
+  __syncthreads();
+  const float r = red[32];
+  __syncthreads();
+  return r;
+}
+
+struct SignalArgs {
+  const float* frame;        // [B][cam][cam]
+  const unsigned char* valid;
+  const float* ref2d;        // or null
+  const int* sig_index;      // [n_signal]
+  float* signal_2d;          // [B][n2d]
+  float* signal;             // [B][n_signal]
+  float* norma;              // [B] or null
+  int mode, cam, nq, n2d, n_signal, n_valid;
+  int q_r0[4], q_c0[4];
+  float units, norma_const;
+};
+
+__global__ void pwfs_signal(SignalArgs a) {
+  __shared__ float red[33];
+  const int b = blockIdx.x;
+  const float* fr = a.frame + (size_t)b * a.cam * a.cam;
+  float* s2 = a.signal_2d + (size_t)b * a.n2d;
+  const bool slopes = a.mode <= 2;
+  float part = 0.f;
+  if (slopes) {
+    const int nq2 = a.nq * a.nq;
+    if (a.mode == 0) {
+      for (int idx = threadIdx.x; idx < nq2; idx += blockDim.x) {
+        if (!a.valid[idx]) continue;
+        const int r = idx / a.nq, c = idx % a.nq;
+        const float i1 = fr[(a.q_r0[0] + r) * a.cam + a.q_c0[0] + c];
+        const float i2 = fr[(a.q_r0[1] + r) * a.cam + a.q_c0[1] + c];
+        const float i3 = fr[(a.q_r0[2] + r) * a.cam + a.q_c0[2] + c];
+        const float i4 = fr[(a.q_r0[3] + r) * a.cam + a.q_c0[3] + c];
+        part += ((i1 + i2) + i3) + i4;
+      }
+    } else if (a.mode == 2) {
+      for (int idx = threadIdx.x; idx < a.cam * a.cam; idx += blockDim.x) part += fr[idx];
+    }
+  } else if (a.mode == 3) {
+    for (int idx = threadIdx.x; idx < a.cam * a.cam; idx += blockDim.x)
+      if (a.valid[idx]) part += fr[idx];
+  } else if (a.mode == 5 || a.mode == 6) {
+    for (int idx = threadIdx.x; idx < a.cam * a.cam; idx += blockDim.x) part += fr[idx];
+  }
+  const float tot = block_sum(part, red);
+  float norma;
+  switch (a.mode) {
+    case 0: norma = tot / (float)a.n_valid; break;
+    case 2: case 5: norma = tot / (float)(a.cam * a.cam); break;
+    case 3: case 6: norma = tot; break;
+    default: norma = a.norma_const; break;
+  }
+  if (slopes) {
+    const int nq2 = a.nq * a.nq;
+    for (int idx = threadIdx.x; idx < nq2; idx += blockDim.x) {
+      const int r = idx / a.nq, c = idx % a.nq;
+      float sx = 0.f, sy = 0.f;
+      if (a.valid[idx]) {
+        const float i1 = fr[(a.q_r0[0] + r) * a.cam + a.q_c0[0] + c];
+        const float i2 = fr[(a.q_r0[1] + r) * a.cam + a.q_c0[1] + c];
+        const float i3 = fr[(a.q_r0[2] + r) * a.cam + a.q_c0[2] + c];
+        const float i4 = fr[(a.q_r0[3] + r) * a.cam + a.q_c0[3] + c];
+        sx = ((i1 - i2) + i4) - i3;
+        sy = ((i1 - i4) + i2) - i3;
+      }
+      const float rx = a.ref2d ? a.ref2d[idx] : 0.f;
+      const float ry = a.ref2d ? a.ref2d[nq2 + idx] : 0.f;
+      s2[idx] = (sx / norma - rx) * a.units;
+      s2[nq2 + idx] = (sy / norma - ry) * a.units;
+    }
+  } else {
+    for (int idx = threadIdx.x; idx < a.cam * a.cam; idx += blockDim.x) {
+      const float rr = a.ref2d ? a.ref2d[idx] : 0.f;
+      s2[idx] = fr[idx] / norma - rr;
+    }
+  }
+  __syncthreads();
+  float* sg = a.signal + (size_t)b * a.n_signal;
+  for (int t = threadIdx.x; t < a.n_signal; t += blockDim.x) sg[t] = s2[a.sig_index[t]];
+  if (a.norma && threadIdx.x == 0) a.norma[b] = norma;
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+
+namespace {
+
+size_t rows_smem(int n, int lines) { return (size_t)(n + 2 * lines * n) * sizeof(float2); }
+size_t inv_smem(int n, int lines) { return rows_smem(n, lines) + (size_t)lines * n * sizeof(float); }
+
+int max_lines(int n, bool with_acc) {
+  int l = 32;
+  while (l > 1 && (with_acc ? inv_smem(n, l) : rows_smem(n, l)) > kSmemLimit) l--;
+  return l;
+}
+
+void free_plan(oopao_pwfs_plan* p) {
+  if (!p) return;
+  cudaFree(p->d_tw);
+  cudaFree(p->d_mask);
+  cudaFree(p->d_rowfac);
+  cudaFree(p->d_colfac);
+  cudaFree(p->d_amp);
+  cudaFree(p->d_weights);
+  cudaFree(p->d_valid);
+  cudaFree(p->d_ref2d);
+  cudaFree(p->d_sig_index);
+  free(p);
+}
+
+// numpy.linspace(-pi, pi, res)[j]
+double tt_grid(int j, int res) {
+  if (res == 1) return -M_PI;
+  if (j == res - 1) return M_PI;
+  return -M_PI + j * (2.0 * M_PI / (res - 1));
+}
+
+}  // namespace
+
+extern "C" int oopao_pwfs_plan_create(oopao_pwfs_plan** out, int res, int n, int cam, int k,
+                                      const float* mask_host, const double* path_host,
+                                      double tt_scale, int psf_centering) {
+  OOPAO_CHECK_ARG(out != nullptr, "plan pointer is NULL");
+  *out = nullptr;
+  OOPAO_CHECK_ARG(res > 0 && n >= res && (n - res) % 2 == 0, "need n_fft >= res with n_fft-res even");
+  OOPAO_CHECK_ARG(cam > 0 && n % cam == 0, "n_fft must be a multiple of the camera size");
+  OOPAO_CHECK_ARG(k >= 1, "n_theta must be >= 1");
+  OOPAO_CHECK_ARG(mask_host != nullptr, "mask is NULL");
+  OOPAO_CHECK_ARG(path_host != nullptr || k == 1, "modulation path is NULL");
+  FftPlan fp;
+  if (!fft_make_plan(n, &fp)) {
+    oopao_set_last_error("FFT size has a prime factor > 13 or too many stages", __FILE__, __LINE__);
+    return OOPAO_ERR_UNSUPPORTED;
+  }
+  oopao_pwfs_plan* p = (oopao_pwfs_plan*)calloc(1, sizeof(oopao_pwfs_plan));
+  OOPAO_CHECK_ARG(p != nullptr, "out of host memory");
+  cudaGetDevice(&p->device);
+  p->res = res; p->n = n; p->cam = cam; p->k = k; p->bin = n / cam; p->off = (n - res) / 2;
+  p->psf_centering = psf_centering;
+  p->fft = fp;
+  p->rows_per_cta = std::min(8, max_lines(n, false));
+  p->cols_per_cta = std::min(16, max_lines(n, false));
+  p->inv_rows_per_cta = std::min(8, max_lines(n, true));
+  p->ksplit = std::min(k, 8);
+  p->slopes_units = 1.f;
+  p->sp_mode = -1;
+
+  std::vector<float2> tw(n), rowfac((size_t)k * res), colfac((size_t)k * res);
+  for (int t = 0; t < n; t++) {
+    const double a = -2.0 * M_PI * (double)t / n;
+    tw[t] = make_float2((float)cos(a), (float)sin(a));
+  }
+  // rho(t): centring phasor exp(-i pi (N+1) t / N), or (-1)^t for the
+  // fftshift of the 1-pixel-centred mask; 1/N^2 of ifft2 folded into rowfac.
+  auto rho = [&](int t, double* re, double* im) {
+    if (psf_centering) {
+      const long long m = ((long long)(n + 1) * t) % (2LL * n);
+      const double a = -M_PI * (double)m / n;
+      *re = cos(a); *im = sin(a);
+    } else {
+      *re = (t % 2) ? -1.0 : 1.0; *im = 0.0;
+    }
+  };
+  const double inv_n2 = 1.0 / ((double)n * (double)n);
+  for (int kk = 0; kk < k; kk++) {
+    const double xk = path_host ? path_host[2 * kk] : 0.0;
+    const double yk = path_host ? path_host[2 * kk + 1] : 0.0;
+    for (int j = 0; j < res; j++) {
+      const double t = tt_grid(j, res) * tt_scale;
+      double pr, pi;
+      rho(j + p->off, &pr, &pi);
+      const double ax = xk * t, ay = yk * t;
+      const double cr = cos(ax), ci = sin(ax);
+      rowfac[(size_t)kk * res + j] = make_float2((float)((cr * pr - ci * pi) * inv_n2),
+                                                 (float)((cr * pi + ci * pr) * inv_n2));
+      const double dr = cos(ay), di = sin(ay);
+      colfac[(size_t)kk * res + j] = make_float2((float)(dr * pr - di * pi), (float)(dr * pi + di * pr));
+    }
+  }
+  std::vector<float> ones((size_t)res * res, 0.f);
+#define ALLOC_COPY(dst, src, bytes)                                   \
+  do {                                                                \
+    cudaError_t e1 = cudaMalloc((void**)&(dst), (bytes));             \
+    if (e1 == cudaSuccess && (src) != nullptr)                        \
+      e1 = cudaMemcpy((dst), (src), (bytes), cudaMemcpyHostToDevice); \
+    if (e1 != cudaSuccess) {                                          \
+      oopao_set_last_error(cudaGetErrorString(e1), __FILE__, __LINE__); \
+      free_plan(p);                                                   \
+      return OOPAO_ERR_CUDA;                                          \
+    }                                                                 \
+  } while (0)
+  ALLOC_COPY(p->d_tw, tw.data(), sizeof(float2) * n);
+  ALLOC_COPY(p->d_mask, mask_host, sizeof(float2) * (size_t)n * n);
+  ALLOC_COPY(p->d_rowfac, rowfac.data(), sizeof(float2) * rowfac.size());
+  ALLOC_COPY(p->d_colfac, colfac.data(), sizeof(float2) * colfac.size());
+  ALLOC_COPY(p->d_amp, ones.data(), sizeof(float) * ones.size());
+#undef ALLOC_COPY
+  cudaError_t e = cudaFuncSetAttribute(pwfs_rows_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(pwfs_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(pwfs_rows_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+  if (e != cudaSuccess) {
+    oopao_set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+    free_plan(p);
+    return OOPAO_ERR_CUDA;
+  }
+  *out = p;
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_pwfs_plan_destroy(oopao_pwfs_plan* p) {
+  free_plan(p);
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_pwfs_set_amplitude(oopao_pwfs_plan* p, const float* amp_host) {
+  OOPAO_CHECK_ARG(p && amp_host, "NULL argument");
+  OOPAO_CUDA_TRY(cudaMemcpy(p->d_amp, amp_host, sizeof(float) * p->res * p->res, cudaMemcpyHostToDevice));
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_pwfs_set_weights(oopao_pwfs_plan* p, const float* w) {
+  OOPAO_CHECK_ARG(p, "NULL plan");
+  if (!w) {
+    cudaFree(p->d_weights);
+    p->d_weights = nullptr;
+    return OOPAO_OK;
+  }
+  if (!p->d_weights) OOPAO_CUDA_TRY(cudaMalloc((void**)&p->d_weights, sizeof(float) * p->k));
+  OOPAO_CUDA_TRY(cudaMemcpy(p->d_weights, w, sizeof(float) * p->k, cudaMemcpyHostToDevice));
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_pwfs_set_launch(oopao_pwfs_plan* p, int rows, int cols, int inv_rows, int ksplit) {
+  OOPAO_CHECK_ARG(p, "NULL plan");
+  if (rows > 0) {
+    OOPAO_CHECK_ARG(rows_smem(p->n, rows) <= kSmemLimit, "rows_per_cta exceeds shared memory");
+    p->rows_per_cta = rows;
+  }
+  if (cols > 0) {
+    OOPAO_CHECK_ARG(rows_smem(p->n, cols) <= kSmemLimit, "cols_per_cta exceeds shared memory");
+    p->cols_per_cta = cols;
+  }
+  if (inv_rows > 0) {
+    OOPAO_CHECK_ARG(inv_smem(p->n, inv_rows) <= kSmemLimit, "inv_rows_per_cta exceeds shared memory");
+    p->inv_rows_per_cta = inv_rows;
+  }
+  if (ksplit > 0) {
+    OOPAO_CHECK_ARG(ksplit <= p->k, "ksplit must not exceed n_theta");
+    p->ksplit = ksplit;
+  }
+  return OOPAO_OK;
+}
+
+namespace {
+size_t item_bytes(const oopao_pwfs_plan* p) {
+  return sizeof(float2) * (size_t)p->k * ((size_t)p->res * p->n + (size_t)p->n * p->n) +
+         sizeof(float) * (size_t)p->ksplit * p->n * p->n;
+}
+}  // namespace
+
+extern "C" size_t oopao_pwfs_workspace_bytes(const oopao_pwfs_plan* p, int batch) {
+  if (!p || batch < 1) return 0;
+  return item_bytes(p) * (size_t)batch + 256;
+}
+
+extern "C" int oopao_pwfs_measure(const oopao_pwfs_plan* p, const float* opd, double phase_scale,
+                                  int batch, float* frame, float* raw, void* ws, size_t ws_bytes,
+                                  void* stream) {
+  OOPAO_CHECK_ARG(p && opd && frame && ws, "NULL argument");
+  OOPAO_CHECK_ARG(batch >= 1, "batch must be >= 1");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t per = item_bytes(p);
+  uintptr_t base = ((uintptr_t)ws + 255) & ~(uintptr_t)255;
+  const size_t usable = ws_bytes > (base - (uintptr_t)ws) ? ws_bytes - (base - (uintptr_t)ws) : 0;
+  const int chunk = (int)std::min<size_t>((size_t)batch, usable / per);
+  if (chunk < 1) {
+    oopao_set_last_error("workspace smaller than one batch item", __FILE__, __LINE__);
+    return OOPAO_ERR_WORKSPACE;
+  }
+  const int n = p->n, res = p->res, k = p->k;
+  float2* y = (float2*)base;
+  float2* z = y + (size_t)chunk * k * res * n;
+  float* partial = (float*)(z + (size_t)chunk * k * n * n);
+  for (int b0 = 0; b0 < batch; b0 += chunk) {
+    const int bc = std::min(chunk, batch - b0);
+    RowsFwdArgs ra{p->fft, p->d_tw, opd + (size_t)b0 * res * res, (float)phase_scale, p->d_amp,
+                   p->d_rowfac, p->d_colfac, y, res, n, k, p->off, p->rows_per_cta};
+    dim3 g1(ceil_div(res, p->rows_per_cta), k, bc);
+    pwfs_rows_fwd<<<g1, kThreads, rows_smem(n, p->rows_per_cta), st>>>(ra);
+    ColsArgs ca{p->fft, p->d_tw, p->d_mask, y, z, res, n, k, p->off, p->cols_per_cta};
+    dim3 g2(ceil_div(n, p->cols_per_cta), k, bc);
+    pwfs_cols<<<g2, kThreads, rows_smem(n, p->cols_per_cta), st>>>(ca);
+    RowsInvArgs ia{p->fft, p->d_tw, z, p->d_weights, partial, n, k, p->inv_rows_per_cta, p->ksplit};
+    dim3 g3(ceil_div(n, p->inv_rows_per_cta), p->ksplit, bc);
+    pwfs_rows_inv<<<g3, kThreads, inv_smem(n, p->inv_rows_per_cta), st>>>(ia);
+    dim3 g4(p->cam, bc);
+    pwfs_bin<<<g4, 128, 0, st>>>(partial, frame + (size_t)b0 * p->cam * p->cam,
+                                 raw ? raw + (size_t)b0 * n * n : nullptr, n, p->cam, p->bin, p->ksplit);
+  }
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_pwfs_set_signal_processing(oopao_pwfs_plan* p, int mode, int nq,
+                                                const int* quad_origin, const unsigned char* valid,
+                                                const float* ref2d, double units, double norma_const) {
+  OOPAO_CHECK_ARG(p && valid, "NULL argument");
+  OOPAO_CHECK_ARG(mode >= 0 && mode <= 6, "unknown signal-processing mode");
+  const bool slopes = mode <= 2;
+  int n2d;
+  if (slopes) {
+    OOPAO_CHECK_ARG(quad_origin != nullptr && nq > 0, "slopes modes need quadrant geometry");
+    for (int q = 0; q < 4; q++) {
+      OOPAO_CHECK_ARG(quad_origin[2 * q] >= 0 && quad_origin[2 * q] + nq <= p->cam &&
+                          quad_origin[2 * q + 1] >= 0 && quad_origin[2 * q + 1] + nq <= p->cam,
+                      "quadrant outside the camera frame");
+      p->q_r0[q] = quad_origin[2 * q];
+      p->q_c0[q] = quad_origin[2 * q + 1];
+    }
+    n2d = 2 * nq * nq;
+  } else {
+    n2d = p->cam * p->cam;
+  }
+  const int nvalid_cells = slopes ? nq * nq : p->cam * p->cam;
+  std::vector<int> idx;
+  int nvalid = 0;
+  for (int i = 0; i < nvalid_cells; i++) nvalid += valid[i] ? 1 : 0;
+  if (slopes) {
+    // validSignal = concatenate((validI4Q, validI4Q)); row-major order
+    for (int h = 0; h < 2; h++)
+      for (int i = 0; i < nvalid_cells; i++)
+        if (valid[i]) idx.push_back(h * nvalid_cells + i);
+  } else {
+    for (int i = 0; i < nvalid_cells; i++)
+      if (valid[i]) idx.push_back(i);
+  }
+  OOPAO_CHECK_ARG(!idx.empty(), "no valid pixel");
+  cudaFree(p->d_valid);
+  cudaFree(p->d_ref2d);
+  cudaFree(p->d_sig_index);
+  p->d_valid = nullptr; p->d_ref2d = nullptr; p->d_sig_index = nullptr;
+  OOPAO_CUDA_TRY(cudaMalloc((void**)&p->d_valid, nvalid_cells));
+  OOPAO_CUDA_TRY(cudaMemcpy(p->d_valid, valid, nvalid_cells, cudaMemcpyHostToDevice));
+  if (ref2d) {
+    OOPAO_CUDA_TRY(cudaMalloc((void**)&p->d_ref2d, sizeof(float) * n2d));
+    OOPAO_CUDA_TRY(cudaMemcpy(p->d_ref2d, ref2d, sizeof(float) * n2d, cudaMemcpyHostToDevice));
+  }
+  OOPAO_CUDA_TRY(cudaMalloc((void**)&p->d_sig_index, sizeof(int) * idx.size()));
+  OOPAO_CUDA_TRY(cudaMemcpy(p->d_sig_index, idx.data(), sizeof(int) * idx.size(), cudaMemcpyHostToDevice));
+  p->sp_mode = mode;
+  p->nq = nq;
+  p->n2d = n2d;
+  p->n_signal = (int)idx.size();
+  p->slopes_units = (float)units;
+  p->norma_const = (float)norma_const;
+  p->cam2 = nvalid;  // number of valid cells
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_pwfs_n_signal(const oopao_pwfs_plan* p) { return p ? p->n_signal : -1; }
+
+extern "C" int oopao_pwfs_signal(const oopao_pwfs_plan* p, const float* frame, int batch,
+                                 float* signal_2d, float* signal, float* norma, void* stream) {
+  OOPAO_CHECK_ARG(p && frame && signal_2d && signal, "NULL argument");
+  OOPAO_CHECK_ARG(p->sp_mode >= 0, "signal processing not configured");
+  OOPAO_CHECK_ARG(batch >= 1, "batch must be >= 1");
+  SignalArgs a;
+  a.frame = frame; a.valid = p->d_valid; a.ref2d = p->d_ref2d; a.sig_index = p->d_sig_index;
+  a.signal_2d = signal_2d; a.signal = signal; a.norma = norma;
+  a.mode = p->sp_mode; a.cam = p->cam; a.nq = p->nq; a.n2d = p->n2d; a.n_signal = p->n_signal;
+  a.n_valid = p->cam2;
+  for (int q = 0; q < 4; q++) { a.q_r0[q] = p->q_r0[q]; a.q_c0[q] = p->q_c0[q]; }
+  a.units = p->slopes_units; a.norma_const = p->norma_const;
+  pwfs_signal<<<batch, 256, 0, (cudaStream_t)stream>>>(a);
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}

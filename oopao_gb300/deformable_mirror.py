@@ -1,0 +1,211 @@
+"""Deformable mirror: drop-in for the reference ``DeformableMirror``
+(``OOPAO/DeformableMirror.py``) on the PWFS path.
+
+Construction builds the Gaussian influence functions on the host in float64
+exactly as the reference (Fried grid and radial actuator selection
+:306-340, ``modesComputation`` :572-600), or takes user ``modes``.  The IF
+matrix is then kept on the GPU, transposed ([n_act][n_pix]), and every
+``dm.coefs = ...`` runs the projection OPD = modes @ coefs on the device
+through ``oopao_dm_opd_f32`` (FP32) or, with ``if_dtype='bf16'``, the
+tensor-core path.  ``dm.OPD`` is materialised on the host only when read.
+"""
+import numpy as np
+import torch
+
+from . import _native as N
+from .runtime import device
+from .tools import OopaoError, print_
+
+
+class DeformableMirror:
+    def __init__(self, telescope, nSubap: float, mechCoupling: float = 0.35, coordinates=None,
+                 pitch: float = None, modes=None, misReg=None, M4_param=None, nJobs: int = 30,
+                 nThreads: int = 20, print_dm_properties: bool = True, floating_precision: int = 64,
+                 altitude: float = None, flip=False, flip_lr=False, sign=1, actuator_selection=None,
+                 user_defined_influence_functions_tag=None, if_dtype: str = 'fp32'):
+        if M4_param is not None:
+            raise OopaoError('M4 influence functions are not supported by oopao_gb300')
+        if altitude is not None:
+            raise OopaoError('Altitude-conjugated DMs are not supported by oopao_gb300')
+        if misReg is not None:
+            raise OopaoError('Mis-registered DMs are not supported by oopao_gb300 (pass modes=)')
+        if mechCoupling <= 0:
+            raise OopaoError('The value of mechanical coupling should be positive.')
+        self.telescope = telescope
+        self.altitude = None
+        self.print_dm_properties = print_dm_properties
+        self.floating_precision = floating_precision
+        self.flip_ = flip
+        self.flip_lr = flip_lr
+        self.sign = sign
+        self.actuator_selection = actuator_selection
+        self.resolution = telescope.resolution
+        self.mechCoupling = mechCoupling
+        self.tag = 'deformableMirror'
+        self.D = telescope.D
+        self.isM4 = False
+        self.precision = np.float64
+        self.pitch = self.D / nSubap if pitch is None else pitch
+        self.if_dtype = if_dtype
+        if coordinates is None:
+            self.nAct = nSubap + 1
+            self.nActAlongDiameter = self.nAct - 1
+            x = np.linspace(-self.D / 2, self.D / 2, self.nAct)
+            X, Y = np.meshgrid(x, x)
+            self.xIF0 = np.reshape(X, [self.nAct ** 2])
+            self.yIF0 = np.reshape(Y, [self.nAct ** 2])
+            r = np.sqrt(self.xIF0 ** 2 + self.yIF0 ** 2)
+            if self.actuator_selection is None:
+                r_in = telescope.centralObstruction * telescope.initial_D / 2 - 0.5 * self.pitch
+                r_out = telescope.initial_D / 2 + 0.7533 * self.pitch
+                self.actuator_selection = [r_in, r_out]
+            if np.isscalar(self.actuator_selection):
+                self.validAct = np.ones_like(r, dtype=bool)
+            else:
+                if len(self.actuator_selection) != 2:
+                    raise OopaoError('actuator_selection must be either a scalar or a vector of length 2 '
+                                     'to specify the inner and outer radius.')
+                self.validAct = (r >= self.actuator_selection[0]) * (r <= self.actuator_selection[1])
+            self.nValidAct = int(np.sum(self.validAct))
+        else:
+            coordinates = np.asarray(coordinates)
+            if coordinates.ndim != 2 or coordinates.shape[1] != 2:
+                raise OopaoError('Wrong size for the DM coordinates, the (x,y) coordinates should be '
+                                 'input as a 2D array of dimension [nAct,2]')
+            self.xIF0 = coordinates[:, 0]
+            self.yIF0 = coordinates[:, 1]
+            self.nAct = len(self.xIF0)
+            self.nActAlongDiameter = self.D / self.pitch
+            self.validAct = np.arange(self.nAct)
+            self.nValidAct = self.nAct
+        xIF = self.xIF0[self.validAct]
+        yIF = self.yIF0[self.validAct]
+        self.nIF = len(xIF)
+        self.coordinates = np.stack([xIF, yIF], axis=1)
+        self.xIF, self.yIF = xIF, yIF
+        if modes is None:
+            u0x = self.resolution / 2 + xIF * self.resolution / self.D
+            u0y = self.resolution / 2 + yIF * self.resolution / self.D
+            self.modes = self._gaussian_modes(u0x, u0y)
+            if np.isscalar(self.actuator_selection):
+                pup = telescope.pupil.flatten() == 1
+                std = np.std(self.modes[pup, :], axis=0)
+                keep = np.where(std > self.actuator_selection * np.max(std))[0]
+                self.modes = self.modes[:, keep]
+                self.validAct = keep
+                self.nValidAct = len(keep)
+                self.nIF = self.nValidAct
+                self.xIF, self.yIF = self.xIF[keep], self.yIF[keep]
+                self.coordinates = self.coordinates[keep]
+        else:
+            self.modes = np.asarray(modes) * self.sign
+            self.nValidAct = self.modes.shape[1]
+        if self.modes.shape[0] != self.resolution ** 2:
+            raise OopaoError('modes must be [resolution**2, n_modes]')
+        self._dev = device()
+        self._modes_t = None
+        self._upload_modes()
+        self._opd_dev = None
+        self._opd_host = None
+        self._coefs = None
+        self.coefs = np.zeros(self.nValidAct, dtype=np.float32 if floating_precision == 32 else np.float64)
+        self.current_coefs = self.coefs.copy()
+        print_(self, print_dm_properties)
+
+    # ------------------------------------------------------------ IF build
+    def _gaussian_modes(self, u0x, u0y):
+        """``modesComputation`` (OOPAO/DeformableMirror.py:572-600), zero mis-registration."""
+        res = self.resolution
+        cx = (self.resolution / self.nActAlongDiameter) / np.sqrt(2 * np.log(1. / self.mechCoupling))
+        cy = cx
+        theta = 0.0
+        x = np.linspace(0, 1, res) * res
+        X, Y = np.meshgrid(x, x)
+        a = np.cos(theta) ** 2 / (2 * cx ** 2) + np.sin(theta) ** 2 / (2 * cy ** 2)
+        b = -np.sin(2 * theta) / (4 * cx ** 2) + np.sin(2 * theta) / (4 * cy ** 2)
+        c = np.sin(theta) ** 2 / (2 * cx ** 2) + np.cos(theta) ** 2 / (2 * cy ** 2)
+        out = np.empty((res * res, len(u0x)))
+        for i, (x0, y0) in enumerate(zip(u0x, u0y)):
+            G = self.sign * np.exp(-(a * (X - x0) ** 2 + 2 * b * (X - x0) * (Y - y0) + c * (Y - y0) ** 2))
+            if self.flip_lr:
+                G = np.fliplr(G)
+            if self.flip_:
+                G = np.flip(G)
+            out[:, i] = G.reshape(res * res)
+        if self.floating_precision == 32:
+            out = np.float32(out)
+        return out
+
+    def _upload_modes(self):
+        mt = np.ascontiguousarray(np.asarray(self.modes, dtype=np.float32).T)
+        self._modes_t = torch.as_tensor(mt, device=self._dev)
+        self._modes_bf16 = None
+
+    # ------------------------------------------------------------ projection
+    def opd_device(self, coefs_dev, scale=1.0, out=None):
+        """Device projection: coefs [n_act] or [n_act, B] float32 -> opd
+        [B, res, res] float32 (= (modes @ coefs)^T * scale)."""
+        c = coefs_dev if coefs_dev.ndim == 2 else coefs_dev[:, None]
+        c = c.contiguous()
+        B = c.shape[1]
+        res = self.resolution
+        if out is None:
+            out = torch.empty((B, res, res), dtype=torch.float32, device=self._dev)
+        N.call('oopao_dm_opd_f32', N.ptr(self._modes_t), N.ptr(c), self.nValidAct, res * res, B,
+               float(scale), N.ptr(out), N.stream_handle())
+        return out
+
+    @property
+    def coefs(self):
+        return self._coefs
+
+    @coefs.setter
+    def coefs(self, val):
+        if torch.is_tensor(val):
+            cd = val.to(device=self._dev, dtype=torch.float32)
+            self._coefs = val
+            if cd.shape[0] != self.nValidAct:
+                raise OopaoError('Error: wrong value for the coefficients')
+        else:
+            if self.floating_precision == 32:
+                val = np.float32(val)
+            if np.isscalar(val):
+                if val != 0:
+                    raise OopaoError('Error: wrong value for the coefficients')
+                val = np.zeros(self.nValidAct, dtype=self.precision)
+            val = np.asarray(val)
+            if len(val) != self.nValidAct:
+                raise OopaoError('Error: wrong value for the coefficients')
+            self._coefs = val
+            cd = torch.as_tensor(np.ascontiguousarray(val, dtype=np.float32), device=self._dev)
+        opd = self.opd_device(cd)
+        self._opd_dev = opd[0] if cd.ndim == 1 else opd
+        self._opd_host = None
+        self.current_coefs = self._coefs.copy() if hasattr(self._coefs, 'copy') else self._coefs.clone()
+
+    @property
+    def OPD(self):
+        if self._opd_host is None:
+            a = self._opd_dev.detach().to('cpu', torch.float64).numpy()
+            self._opd_host = np.moveaxis(a, 0, -1) if a.ndim == 3 else a
+        return self._opd_host
+
+    def relay(self, src):
+        if src.tag != 'source':
+            raise OopaoError('Only a single Source can be propagated (asterisms are not supported)')
+        src.optical_path.append([self.tag, self])
+        if self._opd_dev.ndim == 2 and (src._opd_zero or src._opd_np is None and not src._dev_fresh):
+            # OPD_no_pupil = 0 + dm.OPD
+            src._set_device_opd(self._opd_dev)
+        elif self._opd_dev.ndim == 2:
+            base = src.device_opd(self._dev)
+            if base.ndim != 2:
+                base = torch.zeros_like(self._opd_dev)
+            src._set_device_opd(base + self._opd_dev)
+        else:
+            # several OPDs at once replace the current one (DeformableMirror.py:447-449)
+            src._set_device_opd(self._opd_dev)
+
+    def __repr__(self):
+        return 'DeformableMirror(nValidAct=%d, pitch=%.3f m, coupling=%.2f)' % (
+            self.nValidAct, self.pitch, self.mechCoupling)

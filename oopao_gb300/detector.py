@@ -1,0 +1,88 @@
+"""WFS camera: drop-in for the reference ``Detector`` (``OOPAO/Detector.py``)
+as used by the pyramid.
+
+The pyramid kernels write the noise-free, sum-binned frame on the device
+(``integrate``/``readout`` with the default settings reduce to that frame,
+``OOPAO/Detector.py:273-354``).  ``frame`` is materialised on the host only
+when read.  QE and gain are applied on the device; photon and readout noise,
+when switched on, are drawn on the device after the binning (the reference
+seeds its noise from the wall clock, so noisy frames are statistical, not
+bit-level, matches).
+"""
+import numpy as np
+import torch
+
+from .tools import OopaoError
+
+
+class Detector:
+    def __init__(self, nRes: int = None, integrationTime: float = None, bits: int = None,
+                 output_precision: int = None, FWC: int = None, gain: int = 1, sensor: str = 'CCD',
+                 QE: float = 1., binning: int = 1, psf_sampling: float = 2., darkCurrent: float = 0.,
+                 readoutNoise: float = 0, photonNoise: bool = False, backgroundNoise: bool = False,
+                 backgroundFlux: float = None, backgroundMap: float = None, log_scale: bool = False):
+        if sensor not in ['EMCCD', 'CCD', 'CMOS']:
+            raise OopaoError("Sensor must be 'EMCCD', 'CCD', or 'CMOS'")
+        self.resolution = nRes
+        self.integrationTime = integrationTime
+        self.bits = bits
+        self.output_precision = output_precision
+        self.FWC = FWC
+        self.gain = gain
+        self.sensor = sensor
+        self.QE = QE
+        self.binning = binning
+        self.psf_sampling = psf_sampling
+        self.darkCurrent = darkCurrent
+        self.readoutNoise = readoutNoise
+        self.photonNoise = photonNoise
+        self.backgroundNoise = backgroundNoise
+        self.backgroundFlux = backgroundFlux
+        self.backgroundMap = backgroundMap
+        self.log_scale = log_scale
+        self.tag = 'detector'
+        self._integrated_time = 0
+        self.is_focal_plane_camera = False
+        self._frame_dev = None
+        self._frame_host = np.zeros([nRes, nRes]) if nRes is not None else None
+        self.generator = None
+
+    def _unsupported(self):
+        if self.integrationTime is not None or self.bits is not None or self.FWC is not None or \
+                self.darkCurrent != 0 or self.backgroundNoise or self.backgroundMap is not None or \
+                self.log_scale or self.sensor == 'EMCCD' or self.binning != 1:
+            raise OopaoError('oopao_gb300 Detector supports QE, gain, photon and readout noise only')
+
+    def _integrate_device(self, frame_dev):
+        """Apply QE, noise and gain to device frames [B,cam,cam] (in place when possible)."""
+        self._unsupported()
+        f = frame_dev
+        if self.photonNoise:
+            f = torch.poisson(f.clamp_min(0), generator=self.generator)
+        if self.QE != 1:
+            f = f * self.QE
+        if self.readoutNoise != 0:
+            f = f + torch.round(torch.randn(f.shape, device=f.device, generator=self.generator) *
+                                self.readoutNoise)
+        if self.gain != 1:
+            f = f * self.gain
+        return f
+
+    def _set_device_frame(self, t):
+        self._frame_dev = t
+        self._frame_host = None
+
+    @property
+    def frame(self):
+        if self._frame_host is None and self._frame_dev is not None:
+            a = self._frame_dev.detach().to('cpu', torch.float64).numpy()
+            self._frame_host = a[0] if a.ndim == 3 and a.shape[0] == 1 else a
+        return self._frame_host
+
+    @frame.setter
+    def frame(self, val):
+        self._frame_host = np.asarray(val)
+        self._frame_dev = None
+
+    def __repr__(self):
+        return 'Detector(%s px, QE=%.2f, gain=%s)' % (self.resolution, self.QE, self.gain)
