@@ -1,0 +1,391 @@
+"""Benchmark: PWFS frames/s of the batched interaction-matrix build.
+
+Workload (N=1): the "batched calibration" configuration — 8 m pupil, 120 px
+(6 px/subaperture), 20x20 pyramid (N=264 FFT grid, 44x44 camera),
+modulation 3 lambda/D with 48 points, 21x21 Gaussian-IF DM (357 valid
+actuators, coupling 0.35), 300 KL-like modes, push-pull +-1e-8 m RMS,
+float32 commands, FP64 SVD reconstructor keeping 280 modes.  One step = one
+push-pull interaction matrix = 600 PWFS frames (each frame = 48 modulation
+points).
+
+  value: frames/s with the mode basis and IFs resident on the GPU
+         (DM GEMM -> batched propagation -> signals, no host copies)
+  e2e:   frames/s through the public call
+         InteractionMatrix(ngs, tel, dm, wfs, M2C, stroke, single_pass=False,
+         nTrunc=20) with M2C in host memory and the CalibrationVault
+         returned to host memory
+
+``--impl reference`` times the float64 CPU oracle port of the reference
+algorithm on the host cores on a bounded sample of the same workload.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import contextlib
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+RES, NSUB, MOD, NTHETA, NMODES, STROKE, NTRUNC = 120, 20, 3, 48, 300, 1e-8, 20
+WORKLOAD = ('batched push-pull interaction matrix: 8 m, 120 px, 20x20 PWFS (N=264, cam 44), '
+            'modulation 3 l/D x 48 points, 21x21 Gaussian DM (357 act), 300 KL-like modes, '
+            '+-1e-8 m RMS, FP64 SVD 280 modes')
+
+
+def _quiet():
+    return contextlib.redirect_stdout(io.StringIO())
+
+
+def kl_like_basis(modes, pupil, n_modes, diameter=8.0, r0=0.15, L0=25.0):
+    """Synthetic KL-like basis [n_act, n_modes]: eigenvectors of the von
+    Karman phase covariance sampled at the actuator footprints, each column
+    scaled to 1 m RMS OPD over the pupil.  Stands in for the reference's KL
+    basis (its computation is not on the measured path)."""
+    from scipy.special import gamma, kv
+    res = pupil.shape[0]
+    n_act = modes.shape[1]
+    ipup = pupil.reshape(-1) > 0
+    w = modes[ipup]                                   # [npup, n_act]
+    x = (np.arange(res) - res / 2) * diameter / res
+    X, Y = np.meshgrid(x, x)
+    px, py = X.reshape(-1)[ipup], Y.reshape(-1)[ipup]
+    wsum = w.sum(axis=0)
+    cx, cy = (w * px[:, None]).sum(0) / wsum, (w * py[:, None]).sum(0) / wsum
+    r = np.hypot(cx[:, None] - cx[None], cy[:, None] - cy[None])
+    k0 = 2 * np.pi / L0
+    c = (L0 / r0) ** (5 / 3) * gamma(11 / 6) / (2 ** (5 / 6) * np.pi ** (8 / 3)) * \
+        (24 / 5 * gamma(6 / 5)) ** (5 / 6)
+    rr = np.maximum(r, 1e-9)
+    cov = c * (k0 * rr) ** (5 / 6) * kv(5 / 6, k0 * rr)
+    cov[r < 1e-9] = c * gamma(5 / 6) / 2 ** (1 / 6)
+    ev, vec = np.linalg.eigh(cov)
+    vec = vec[:, np.argsort(ev)[::-1][:n_modes]]
+    opd = w @ vec
+    vec = vec / opd.std(axis=0)[None]
+    return np.ascontiguousarray(vec)
+
+
+def build_system(dev_index):
+    import oopao_gb300 as og
+    with _quiet():
+        tel = og.Telescope(resolution=RES, diameter=8.0, samplingTime=1e-3)
+        ngs = og.Source(optBand='V0', magnitude=8)
+        ngs * tel
+        dm = og.DeformableMirror(tel, nSubap=NSUB, mechCoupling=0.35)
+        wfs = og.Pyramid(nSubap=NSUB, telescope=tel, modulation=MOD, lightRatio=0.5,
+                         nTheta_user_defined=NTHETA, max_batch=100)
+    return tel, ngs, dm, wfs
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+         'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix='.csv')
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.gpu), '--query-gpu=' + self.Q, '--format=csv,noheader,nounits',
+                 '-lms', '200'], stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(',')]
+                if len(f) >= 9:
+                    rows.append(f)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        if not rows:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['unavailable'], 'samples': 0}
+        sm = [float(r[1]) for r in rows if r[1].replace('.', '').isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace('.', '').isdigit()]
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == 'active'})
+        return {'sm_mhz': statistics.median(sm) if sm else None, 'sm_max_mhz': max(mx) if mx else None,
+                'reasons': reasons, 'samples': len(rows)}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    try:
+        d = json.load(open(p))
+        return float(d['hbm_gbs']), 'measured'
+    except Exception:
+        return 6800.0, 'fallback'
+
+
+def load_traffic(kernel):
+    """DRAM bytes per (mode, point) unit from a committed ncu summary, or None."""
+    p = os.path.join(ROOT, 'profiles', 'traffic.json')
+    try:
+        d = json.load(open(p))
+        return d[kernel]
+    except Exception:
+        return None
+
+
+def kernel_bytes(kernel, res, n, cam, k, bc, ksplit):
+    """Algorithmic (compulsory) DRAM bytes of one launch over bc batch items."""
+    units = bc * k
+    if kernel == 'pwfs_rows_fwd':
+        return units * 8 * res * n + bc * 4 * res * res + 4 * res * res
+    if kernel == 'pwfs_cols':
+        return units * (8 * res * n + 8 * n * n) + 8 * n * n
+    if kernel == 'pwfs_rows_inv':
+        return units * 8 * n * n + bc * ksplit * 4 * n * n
+    return bc * ksplit * 4 * n * n + bc * 4 * cam * cam
+
+
+KERNELS = ['pwfs_rows_fwd', 'pwfs_cols', 'pwfs_rows_inv', 'pwfs_bin']
+
+
+def cpu_oracle_rate(budget_s=12.0, min_frames=4, threads=None):
+    """Oracle (float64 numpy/scipy port of the reference) push-pull frames/s on
+    the host cores for a bounded sample of the workload."""
+    from oracle import pwfs_oracle as O
+    threads = threads or os.cpu_count() or 1
+    inten = O.source_intensity(O.telescope_pupil(RES), O.n_photon('V0', 8), 1e-3, 8.0)
+    wfs = O.build_pyramid(RES, NSUB, MOD, 0.5, inten, n_theta_user=NTHETA, workers=threads)
+    modes = O.dm_modes(RES, 8.0, NSUB)
+    pupil = O.telescope_pupil(RES)
+    m2c = kl_like_basis(modes, pupil, 8)
+    lam = O.PHOTOMETRY['V0'][0]
+    frames, t0 = 0, time.perf_counter()
+    m = 0
+    while True:
+        O.interaction_matrix(wfs, modes, m2c[:, m % 8:m % 8 + 1], STROKE, lam, pupil, single_pass=False,
+                             workers=threads)
+        frames += 2
+        m += 1
+        el = time.perf_counter() - t0
+        if frames >= min_frames and el >= budget_s:
+            break
+    return frames / el, frames, el, threads
+
+
+def run_reference(args):
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    rates = []
+    for i in range(args.warmup + args.steps):
+        r, frames, el, thr = cpu_oracle_rate(budget_s=1.0, min_frames=2, threads=threads)
+        if i >= args.warmup:
+            rates.append(r)
+    v = statistics.median(rates)
+    line = {
+        'metric': 'PWFS frames/s (batched IM build)', 'value': v, 'unit': 'frames/s',
+        'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': 1000.0 * 2 * NMODES / v, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'impl': 'reference',
+        'config': {'workload': WORKLOAD, 'sample': 'per step: 1 s of push-pull modes (2 frames each)'},
+        'cpu_baseline': {'value': v, 'unit': 'frames/s', 'cores': threads, 'kind': 'port',
+                         'sample': 'push-pull IM columns, >=1 s per step, float64 oracle, scipy.fft workers=%d'
+                                   % threads},
+        'e2e': {'value': v, 'unit': 'frames/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group('nccl')
+    from oopao_gb300 import _native as N
+    from oopao_gb300.calibration import InteractionMatrix, _signals_batched
+    tel, ngs, dm, wfs = build_system(local)
+    m2c = kl_like_basis(dm.modes, tel.pupil, NMODES)
+    dev = wfs._dev
+    m2c_dev = torch.as_tensor(m2c.astype(np.float32), device=dev)
+    n, cam, k = wfs.resolution, wfs._cam_eff, wfs.nTheta
+    plan = wfs.plan
+    ksplit = 8 if k >= 8 else k
+    scale = 2 * np.pi / ngs.wavelength
+    ngs ** tel
+    wfs.plan.set_amplitude(ngs.intensity, wfs._amplitude_key())
+
+    def device_step():
+        sp_all, sm_all = [], []
+        for b0 in range(0, NMODES, wfs.max_batch):
+            cb = m2c_dev[:, b0:b0 + wfs.max_batch] * STROKE
+            for sgn, acc in ((1.0, sp_all), (-1.0, sm_all)):
+                opd = dm.opd_device((cb * sgn).contiguous())
+                frame, _ = wfs._measure_frames(opd, scale)
+                _, sig = wfs._signals(frame)
+                acc.append(sig)
+        sp, sm = torch.cat(sp_all), torch.cat(sm_all)
+        return (0.5 * (sp - sm) / STROKE).T
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        device_step()
+    barrier()
+    stream = torch.cuda.current_stream()
+    N.call('oopao_pwfs_set_profiling', plan.h, 1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n0 = N.load().oopao_launch_count()
+    with ClockSampler(local) as clk:
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            D = device_step()
+        e1.record(stream)
+        barrier()
+    launches = N.load().oopao_launch_count() - n0
+    ms_step = e0.elapsed_time(e1) / args.steps
+    ms = (N.c_double * 4)()
+    cnt = (N.c_int * 4)()
+    N.call('oopao_pwfs_profile_read', plan.h, ms, cnt)
+    N.call('oopao_pwfs_set_profiling', plan.h, 0)
+    clocks = clk.summary()
+    if world > 1:
+        t = torch.tensor([ms_step], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    frames_step = 2 * NMODES
+    value = frames_step * world / (ms_step / 1000.0)
+
+    # ---- roofline of the dominant kernel
+    totals = {KERNELS[i]: ms[i] for i in range(4)}
+    top = max(totals, key=totals.get)
+    ti = KERNELS.index(top)
+    # per launch: chunks of max_batch items; bytes summed over the launches of the timed region
+    chunks = [min(wfs.max_batch, NMODES - b0) for b0 in range(0, NMODES, wfs.max_batch)] * 2 * args.steps
+    byts = sum(kernel_bytes(top, RES, n, cam, k, bc, ksplit) for bc in chunks)
+    achieved = byts / (totals[top] / 1000.0) / 1e9
+    peak, peak_kind = load_peaks()
+    tr = load_traffic(top)
+    traffic = None
+    if tr is not None:
+        units_per_launch = np.mean(chunks) * k
+        traffic = float(tr['dram_bytes_per_unit']) * units_per_launch
+    share = totals[top] / max(sum(totals.values()), 1e-12)
+
+    # ---- end to end through the public API (host M2C in, host vault out)
+    ngs ** tel
+    for _ in range(max(1, args.warmup // 2)):
+        InteractionMatrix(ngs, tel, dm, wfs, m2c, STROKE, single_pass=False, nTrunc=NTRUNC)
+    barrier()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, args.steps // 2)
+    for _ in range(e2e_steps):
+        calib = InteractionMatrix(ngs, tel, dm, wfs, m2c, STROKE, single_pass=False, nTrunc=NTRUNC)
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    ns = wfs.nSignal
+    h2d = m2c.size * 4 + ns * NMODES * 8      # commands (float32) + D for the FP64 SVD
+    d2h = ns * NMODES * 4 + (ns * NMODES + NMODES + NMODES * NMODES) * 8  # D + U, s, V
+    e2e = {'value': frames_step * world / e2e_s, 'unit': 'frames/s', 'h2d_bytes_per_step': int(h2d),
+           'd2h_bytes_per_step': int(d2h), 'im_build_ms': e2e_s * 1000.0,
+           'api': 'InteractionMatrix(..., single_pass=False, nTrunc=20)'}
+
+    # ---- reported CPU baseline (rank 0, N=1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        r, frames, el, thr = cpu_oracle_rate()
+        cpu = {'value': r, 'unit': 'frames/s', 'cores': thr, 'kind': 'port',
+               'sample': '%d push-pull frames (%d KL-like modes) in %.1f s, float64 oracle, '
+                         'scipy.fft workers=%d' % (frames, frames // 2, el, thr)}
+
+    # accuracy of this step's IM against the float64 oracle on 2 columns
+    err = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import pwfs_oracle as O
+        inten = O.source_intensity(O.telescope_pupil(RES), O.n_photon('V0', 8), 1e-3, 8.0)
+        ow = O.build_pyramid(RES, NSUB, MOD, 0.5, inten, n_theta_user=NTHETA, workers=os.cpu_count())
+        Dref = O.interaction_matrix(ow, O.dm_modes(RES, 8.0, NSUB), m2c[:, :2], STROKE,
+                                    ngs.wavelength, O.telescope_pupil(RES), single_pass=False,
+                                    workers=os.cpu_count())
+        err = O.rel_l2(D[:, :2].double().cpu().numpy(), Dref)
+
+    if rank == 0:
+        line = {
+            'metric': 'PWFS frames/s (batched IM build)', 'value': value, 'unit': 'frames/s',
+            'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms_step,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+            'data': 'synthetic (seeded KL-like basis, Gaussian IFs)',
+            'config': {'workload': WORKLOAD, 'frames_per_step': frames_step, 'modulation_points': k,
+                       'fft_grid': n, 'camera': cam, 'batch_per_launch': wfs.max_batch,
+                       'l2': 'intermediates (>=2.4 GB per launch) exceed L2; no flush needed',
+                       'im_rel_fro_err_vs_fp64_oracle_2cols': err},
+            'roofline': {'bound': 'hbm', 'kernel': top, 'achieved': achieved, 'peak': peak,
+                         'unit': 'GB/s', 'frac': achieved / peak, 'peak_kind': peak_kind,
+                         'traffic': traffic, 'kernel_share': share,
+                         'kernel_ms': {kk: totals[kk] for kk in KERNELS},
+                         'launches': {KERNELS[i]: cnt[i] for i in range(4)}},
+            'e2e': e2e,
+            'gpu_launches': int(launches),
+            'clocks': clocks,
+            'cpu_baseline': cpu,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline and accuracy legs')
+    args = ap.parse_args()
+    if args.impl == 'reference':
+        run_reference(args)
+    else:
+        import __graft_entry__
+        __graft_entry__.build()
+        run_ours(args)
+
+
+if __name__ == '__main__':
+    main()

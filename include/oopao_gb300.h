@@ -36,6 +36,9 @@ enum {
 int oopao_abi_version(void);
 /* Message of the last error on this thread ("" if none). */
 const char* oopao_last_error(void);
+/* Number of CUDA kernels this library has launched in the process
+ * (instrumentation, no reference counterpart). */
+unsigned long long oopao_launch_count(void);
 
 /* ------------------------------------------------------------------------
  * Pyramid wavefront sensor plan.
@@ -83,6 +86,14 @@ size_t oopao_pwfs_workspace_bytes(const oopao_pwfs_plan* plan, int batch);
 int oopao_pwfs_measure(const oopao_pwfs_plan* plan, const float* opd, double phase_scale,
                        int batch, float* frame, float* raw, void* workspace,
                        size_t workspace_bytes, void* stream);
+
+/* Per-kernel timing (instrumentation, no reference counterpart): when
+ * enabled, every oopao_pwfs_measure records CUDA events around its four
+ * kernels (row FFT, column FFT/mask/IFFT, row IFFT/|.|^2, binning) on its
+ * stream.  profile_read waits for the last event, returns the summed
+ * milliseconds and launch counts per kernel ([4] each) and clears them. */
+int oopao_pwfs_set_profiling(oopao_pwfs_plan* plan, int enable);
+int oopao_pwfs_profile_read(oopao_pwfs_plan* plan, double* ms, int* launches);
 
 /* Signal-processing setup (Pyramid.initialization / signalProcessing,
  * OOPAO/Pyramid.py:541-589, :835-926, grabQuadrant :946-961).

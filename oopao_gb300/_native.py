@@ -20,6 +20,7 @@ P = ctypes.POINTER
 SIGNATURES = {
     'oopao_abi_version': (c_int, []),
     'oopao_last_error': (ctypes.c_char_p, []),
+    'oopao_launch_count': (ctypes.c_ulonglong, []),
     'oopao_pwfs_plan_create': (c_int, [P(c_void_p), c_int, c_int, c_int, c_int, c_void_p, c_void_p,
                                        c_double, c_int]),
     'oopao_pwfs_plan_destroy': (c_int, [c_void_p]),
@@ -29,6 +30,8 @@ SIGNATURES = {
     'oopao_pwfs_workspace_bytes': (c_size_t, [c_void_p, c_int]),
     'oopao_pwfs_measure': (c_int, [c_void_p, c_void_p, c_double, c_int, c_void_p, c_void_p, c_void_p,
                                    c_size_t, c_void_p]),
+    'oopao_pwfs_set_profiling': (c_int, [c_void_p, c_int]),
+    'oopao_pwfs_profile_read': (c_int, [c_void_p, c_void_p, c_void_p]),
     'oopao_pwfs_set_signal_processing': (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p,
                                                  c_double, c_double]),
     'oopao_pwfs_n_signal': (c_int, [c_void_p]),

@@ -25,6 +25,8 @@
 
 // Records a message for oopao_last_error(); thread-local.
 void oopao_set_last_error(const char* msg, const char* file, int line);
+// Adds n to the process-wide kernel-launch counter (oopao_launch_count).
+void oopao_count_launches(int n);
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));

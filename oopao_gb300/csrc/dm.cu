@@ -116,6 +116,7 @@ extern "C" int oopao_dm_opd_f32(const float* modes_t, const float* coefs, int n_
     dim3 grid(ceil_div(n_pix, BN), ceil_div(batch, BM));
     dm_gemm<<<grid, 256, 0, st>>>(modes_t, coefs, n_act, n_pix, batch, scale, opd);
   }
+  oopao_count_launches(1);
   OOPAO_CUDA_TRY(cudaGetLastError());
   return OOPAO_OK;
 }

@@ -39,8 +39,25 @@ constexpr size_t kSmemLimit = 227 * 1024;
 
 }  // namespace
 
+// Per-kernel CUDA-event timing of oopao_pwfs_measure (bench instrumentation):
+// 5 events per chunk bracket the 4 kernels on the launching stream.
+struct PwfsProfile {
+  bool enabled = false;
+  std::vector<cudaEvent_t> pool;
+  size_t used = 0;
+  cudaEvent_t next() {
+    if (used == pool.size()) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+      pool.push_back(e);
+    }
+    return pool[used++];
+  }
+};
+
 struct oopao_pwfs_plan {
   int device;
+  PwfsProfile* prof;
   int res, n, cam, k, bin, off;
   int psf_centering;
   FftPlan fft;
@@ -338,6 +355,10 @@ int max_lines(int n, bool with_acc) {
 
 void free_plan(oopao_pwfs_plan* p) {
   if (!p) return;
+  if (p->prof) {
+    for (cudaEvent_t e : p->prof->pool) cudaEventDestroy(e);
+    delete p->prof;
+  }
   cudaFree(p->d_tw);
   cudaFree(p->d_mask);
   cudaFree(p->d_rowfac);
@@ -377,6 +398,7 @@ extern "C" int oopao_pwfs_plan_create(oopao_pwfs_plan** out, int res, int n, int
   oopao_pwfs_plan* p = (oopao_pwfs_plan*)calloc(1, sizeof(oopao_pwfs_plan));
   OOPAO_CHECK_ARG(p != nullptr, "out of host memory");
   cudaGetDevice(&p->device);
+  p->prof = new PwfsProfile();
   p->res = res; p->n = n; p->cam = cam; p->k = k; p->bin = n / cam; p->off = (n - res) / 2;
   p->psf_centering = psf_centering;
   p->fft = fp;
@@ -523,21 +545,34 @@ extern "C" int oopao_pwfs_measure(const oopao_pwfs_plan* p, const float* opd, do
   float2* y = (float2*)base;
   float2* z = y + (size_t)chunk * k * res * n;
   float* partial = (float*)(z + (size_t)chunk * k * n * n);
+  PwfsProfile* prof = p->prof->enabled ? p->prof : nullptr;
+  auto mark = [&]() {
+    if (prof) {
+      cudaEvent_t e = prof->next();
+      if (e) cudaEventRecord(e, st);
+    }
+  };
   for (int b0 = 0; b0 < batch; b0 += chunk) {
     const int bc = std::min(chunk, batch - b0);
+    mark();
     RowsFwdArgs ra{p->fft, p->d_tw, opd + (size_t)b0 * res * res, (float)phase_scale, p->d_amp,
                    p->d_rowfac, p->d_colfac, y, res, n, k, p->off, p->rows_per_cta};
     dim3 g1(ceil_div(res, p->rows_per_cta), k, bc);
     pwfs_rows_fwd<<<g1, kThreads, rows_smem(n, p->rows_per_cta), st>>>(ra);
+    mark();
     ColsArgs ca{p->fft, p->d_tw, p->d_mask, y, z, res, n, k, p->off, p->cols_per_cta};
     dim3 g2(ceil_div(n, p->cols_per_cta), k, bc);
     pwfs_cols<<<g2, kThreads, rows_smem(n, p->cols_per_cta), st>>>(ca);
+    mark();
     RowsInvArgs ia{p->fft, p->d_tw, z, p->d_weights, partial, n, k, p->inv_rows_per_cta, p->ksplit};
     dim3 g3(ceil_div(n, p->inv_rows_per_cta), p->ksplit, bc);
     pwfs_rows_inv<<<g3, kThreads, inv_smem(n, p->inv_rows_per_cta), st>>>(ia);
+    mark();
     dim3 g4(p->cam, bc);
     pwfs_bin<<<g4, 128, 0, st>>>(partial, frame + (size_t)b0 * p->cam * p->cam,
                                  raw ? raw + (size_t)b0 * n * n : nullptr, n, p->cam, p->bin, p->ksplit);
+    mark();
+    oopao_count_launches(4);
   }
   OOPAO_CUDA_TRY(cudaGetLastError());
   return OOPAO_OK;
@@ -614,6 +649,32 @@ extern "C" int oopao_pwfs_signal(const oopao_pwfs_plan* p, const float* frame, i
   for (int q = 0; q < 4; q++) { a.q_r0[q] = p->q_r0[q]; a.q_c0[q] = p->q_c0[q]; }
   a.units = p->slopes_units; a.norma_const = p->norma_const;
   pwfs_signal<<<batch, 256, 0, (cudaStream_t)stream>>>(a);
+  oopao_count_launches(1);
   OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_pwfs_set_profiling(oopao_pwfs_plan* p, int enable) {
+  OOPAO_CHECK_ARG(p, "NULL plan");
+  p->prof->enabled = enable != 0;
+  p->prof->used = 0;
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_pwfs_profile_read(oopao_pwfs_plan* p, double* ms, int* launches) {
+  OOPAO_CHECK_ARG(p && ms && launches, "NULL argument");
+  PwfsProfile* pr = p->prof;
+  for (int s = 0; s < 4; s++) { ms[s] = 0.0; launches[s] = 0; }
+  OOPAO_CHECK_ARG(pr->used % 5 == 0, "profile events out of step");
+  if (pr->used) OOPAO_CUDA_TRY(cudaEventSynchronize(pr->pool[pr->used - 1]));
+  for (size_t c = 0; c < pr->used; c += 5) {
+    for (int s = 0; s < 4; s++) {
+      float t = 0.f;
+      OOPAO_CUDA_TRY(cudaEventElapsedTime(&t, pr->pool[c + s], pr->pool[c + s + 1]));
+      ms[s] += t;
+      launches[s] += 1;
+    }
+  }
+  pr->used = 0;
   return OOPAO_OK;
 }

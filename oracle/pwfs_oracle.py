@@ -284,6 +284,20 @@ def wfs_raw(phase: np.ndarray, intensity: np.ndarray, tt: np.ndarray, geom: Pyra
     cube = phase[..., None] if single else phase
     B = cube.shape[2]
     out = np.zeros((B, geom.N, geom.N))
+    if workers > 1 and weight_vector is None:
+        # one modulation point per task on a thread pool, as the reference's
+        # joblib 'threads' backend does (OOPAO/Pyramid.py:741-746)
+        from concurrent.futures import ThreadPoolExecutor
+        with ThreadPoolExecutor(workers) as ex:
+            for b in range(B):
+                ph = cube[:, :, b]
+                maps = ex.map(lambda k: pyramid_transform_stack(
+                    (ph + tt[k].astype(np.float64))[None], amp, geom, workers=1)[0], range(K))
+                acc = np.zeros((geom.N, geom.N))
+                for m in maps:
+                    acc += m
+                out[b] = acc
+        return out[0] if single else out
     for b in range(B):
         acc = np.zeros((geom.N, geom.N))
         maps = []

@@ -55,8 +55,9 @@ def test_geometry_and_valid_pixels(system):
     np.testing.assert_array_equal(wfs.validI4Q, d['valid_i4q'])
     assert wfs.nSignal == int(d['n_signal'])
     if 'mask' in d:
-        np.testing.assert_array_equal(wfs.mask, d['mask'])
-        np.testing.assert_array_equal(dm.modes, d['modes'])
+        # transcendental functions may differ by one ulp between host libms
+        np.testing.assert_allclose(wfs.mask, d['mask'], rtol=0, atol=2e-7)
+        np.testing.assert_allclose(dm.modes, d['modes'], rtol=1e-14, atol=1e-300)
 
 
 def test_reference_signal(system):

@@ -29,13 +29,14 @@ def test_geometry(case):
     np.testing.assert_array_equal(pupil, d['pupil'])
     inten = O.source_intensity(pupil, O.n_photon('V0', 8), 1e-3, 8.0)
     np.testing.assert_array_equal(inten, d['intensity'])
+    # exact on the machine that wrote the fixtures; other libms may differ by one ulp
     if 'mask' in d:
-        np.testing.assert_array_equal(wfs.geom.mask, d['mask'])
-        np.testing.assert_allclose(wfs.geom.phasor, d['phasor'], rtol=0, atol=1e-15)
-        np.testing.assert_array_equal(wfs.tt, d['tt'])
+        np.testing.assert_allclose(wfs.geom.mask, d['mask'], rtol=0, atol=2e-7)
+        np.testing.assert_allclose(wfs.geom.phasor, d['phasor'], rtol=0, atol=1e-14)
+        np.testing.assert_allclose(wfs.tt, d['tt'], rtol=2e-7, atol=0)
     else:
-        np.testing.assert_array_equal(wfs.geom.mask[0], d['mask_row0'])
-        np.testing.assert_array_equal(wfs.geom.mask[:, wfs.geom.N // 2 - 3], d['mask_col_mid'])
+        np.testing.assert_allclose(wfs.geom.mask[0], d['mask_row0'], rtol=0, atol=2e-7)
+        np.testing.assert_allclose(wfs.geom.mask[:, wfs.geom.N // 2 - 3], d['mask_col_mid'], rtol=0, atol=2e-7)
         assert abs(np.real(wfs.geom.mask).astype(np.float64).sum() - d['mask_real_sum']) < 1e-9
         assert abs(np.imag(wfs.geom.mask).astype(np.float64).sum() - d['mask_imag_sum']) < 1e-9
 
@@ -57,10 +58,10 @@ def test_dm_modes(case):
     modes = O.dm_modes(p['res'], 8.0, p['n_subap'], 0.35, p['co'])
     assert modes.shape[1] == int(d['n_act'])
     if 'modes' in d:
-        np.testing.assert_array_equal(modes, d['modes'])
+        np.testing.assert_allclose(modes, d['modes'], rtol=1e-14, atol=1e-300)
     else:
         np.testing.assert_allclose(modes.sum(axis=0), d['modes_colsum'], rtol=1e-13)
-        np.testing.assert_array_equal(modes[:, 0], d['modes_col0'])
+        np.testing.assert_allclose(modes[:, 0], d['modes_col0'], rtol=1e-14, atol=1e-300)
 
 
 def test_dm_path(case):
