@@ -70,6 +70,13 @@ int oopao_pwfs_set_weights(oopao_pwfs_plan* plan, const float* weights_host);
 int oopao_pwfs_set_launch(oopao_pwfs_plan* plan, int rows_per_cta, int cols_per_cta,
                           int inv_rows_per_cta, int ksplit);
 
+/* Kernel variant (no reference counterpart): 1 = compile-time two-stage
+ * FFT plan for this n_fft (the default where one exists), 0 = generic
+ * runtime-planned kernels (any n_fft whose prime factors are <= 13).
+ * Setting 1 without a compile-time plan returns OOPAO_ERR_UNSUPPORTED. */
+int oopao_pwfs_set_variant(oopao_pwfs_plan* plan, int variant);
+int oopao_pwfs_get_variant(const oopao_pwfs_plan* plan);
+
 /* Bytes of device workspace oopao_pwfs_measure needs for `batch` items
  * processed in one chunk (a smaller workspace makes it loop over chunks;
  * it must hold at least one item). */

@@ -27,6 +27,8 @@ SIGNATURES = {
     'oopao_pwfs_set_amplitude': (c_int, [c_void_p, c_void_p]),
     'oopao_pwfs_set_weights': (c_int, [c_void_p, c_void_p]),
     'oopao_pwfs_set_launch': (c_int, [c_void_p, c_int, c_int, c_int, c_int]),
+    'oopao_pwfs_set_variant': (c_int, [c_void_p, c_int]),
+    'oopao_pwfs_get_variant': (c_int, [c_void_p]),
     'oopao_pwfs_workspace_bytes': (c_size_t, [c_void_p, c_int]),
     'oopao_pwfs_measure': (c_int, [c_void_p, c_void_p, c_double, c_int, c_void_p, c_void_p, c_void_p,
                                    c_size_t, c_void_p]),
@@ -68,7 +70,8 @@ def check(status, what=''):
 def call(name, *args):
     lib = load()
     st = getattr(lib, name)(*args)
-    if SIGNATURES[name][0] is c_int and name not in ('oopao_abi_version', 'oopao_pwfs_n_signal'):
+    if SIGNATURES[name][0] is c_int and name not in ('oopao_abi_version', 'oopao_pwfs_n_signal',
+                                                     'oopao_pwfs_get_variant'):
         check(st, name)
     return st
 

@@ -28,9 +28,8 @@ class CalibrationVault:
     def __init__(self, D, nTrunc: int = 0, display: bool = False, print_details: bool = False,
                  invert: bool = True):
         if invert:
-            dev = torch.device('cuda', torch.cuda.current_device()) if torch.cuda.is_available() else None
-            if dev is None:
-                raise OopaoError('CalibrationVault needs a CUDA device')
+            from .runtime import device
+            dev = device()
             Dt = torch.as_tensor(np.asarray(D, dtype=np.float64), device=dev)
             U, s, Vh = torch.linalg.svd(Dt, full_matrices=False)
             U, s, V = U.cpu().numpy(), s.cpu().numpy(), Vh.cpu().numpy()

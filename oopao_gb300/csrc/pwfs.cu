@@ -69,6 +69,8 @@ struct oopao_pwfs_plan {
   float* d_weights;  // [k] or null
   // launch shape
   int rows_per_cta, cols_per_cta, inv_rows_per_cta, ksplit;
+  const struct FastPasses* fast;  // compile-time plan for n, or null (generic kernels)
+  int variant;                    // 1 = use `fast` when available, 0 = generic
   // signal processing
   int sp_mode, nq, n2d, n_signal, cam2;
   int q_r0[4], q_c0[4];
@@ -210,6 +212,33 @@ __global__ void __launch_bounds__(kThreads) pwfs_rows_inv(RowsInvArgs a) {
   float* p = a.partial + (((size_t)b * a.ksplit + slot) * n + r0) * n;
   for (int idx = tid; idx < nl * n; idx += blockDim.x) p[idx] = acc[idx];
 }
+
+#include "pwfs_fast.cuh"
+namespace {
+// Compile-time plans (N = R1*R2, T threads per line, lines per CTA of the
+// three passes).  Sizes without an entry use the generic kernels.
+const FastPasses* fast_passes(int n) {
+  static const FastPasses f72 = make_fast<72, 8, 9, 9, 16, 16, 16>();
+  static const FastPasses f96 = make_fast<96, 8, 12, 12, 16, 16, 16>();
+  static const FastPasses f112 = make_fast<112, 16, 7, 8, 16, 16, 16>();
+  static const FastPasses f128 = make_fast<128, 16, 8, 8, 16, 16, 16>();
+  static const FastPasses f240 = make_fast<240, 16, 15, 16, 16, 16, 8>();
+  static const FastPasses f264 = make_fast<264, 24, 11, 12, 16, 16, 16>();
+  static const FastPasses f480 = make_fast<480, 24, 20, 12, 16, 8, 8>();
+  static const FastPasses f504 = make_fast<504, 24, 21, 12, 16, 8, 8>();
+  switch (n) {
+    case 72: return &f72;
+    case 96: return &f96;
+    case 112: return &f112;
+    case 128: return &f128;
+    case 240: return &f240;
+    case 264: return &f264;
+    case 480: return &f480;
+    case 504: return &f504;
+    default: return nullptr;
+  }
+}
+}  // namespace
 
 // One CTA per (camera row, batch item); thread = camera column.  Also writes
 // raw_data rows (sum of partials) when requested.
@@ -462,6 +491,15 @@ extern "C" int oopao_pwfs_plan_create(oopao_pwfs_plan** out, int res, int n, int
   cudaError_t e = cudaFuncSetAttribute(pwfs_rows_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(pwfs_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(pwfs_rows_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
+  p->fast = fast_passes(n);
+  p->variant = p->fast ? 1 : 0;
+  if (p->fast && e == cudaSuccess) {
+    e = cudaFuncSetAttribute(p->fast->rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->fast->smem_rows);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(p->fast->cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->fast->smem_cols);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(p->fast->inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->fast->smem_inv);
+  }
   if (e != cudaSuccess) {
     oopao_set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
     free_plan(p);
@@ -555,18 +593,34 @@ extern "C" int oopao_pwfs_measure(const oopao_pwfs_plan* p, const float* opd, do
   for (int b0 = 0; b0 < batch; b0 += chunk) {
     const int bc = std::min(chunk, batch - b0);
     mark();
+    const FastPasses* f = (p->variant == 1) ? p->fast : nullptr;
     RowsFwdArgs ra{p->fft, p->d_tw, opd + (size_t)b0 * res * res, (float)phase_scale, p->d_amp,
                    p->d_rowfac, p->d_colfac, y, res, n, k, p->off, p->rows_per_cta};
-    dim3 g1(ceil_div(res, p->rows_per_cta), k, bc);
-    pwfs_rows_fwd<<<g1, kThreads, rows_smem(n, p->rows_per_cta), st>>>(ra);
+    if (f) {
+      dim3 g1(ceil_div(res, f->l_rows), k, bc);
+      f->rows<<<g1, f->t * f->l_rows, f->smem_rows, st>>>(ra);
+    } else {
+      dim3 g1(ceil_div(res, p->rows_per_cta), k, bc);
+      pwfs_rows_fwd<<<g1, kThreads, rows_smem(n, p->rows_per_cta), st>>>(ra);
+    }
     mark();
     ColsArgs ca{p->fft, p->d_tw, p->d_mask, y, z, res, n, k, p->off, p->cols_per_cta};
-    dim3 g2(ceil_div(n, p->cols_per_cta), k, bc);
-    pwfs_cols<<<g2, kThreads, rows_smem(n, p->cols_per_cta), st>>>(ca);
+    if (f) {
+      dim3 g2(ceil_div(n, f->l_cols), k, bc);
+      f->cols<<<g2, f->t * f->l_cols, f->smem_cols, st>>>(ca);
+    } else {
+      dim3 g2(ceil_div(n, p->cols_per_cta), k, bc);
+      pwfs_cols<<<g2, kThreads, rows_smem(n, p->cols_per_cta), st>>>(ca);
+    }
     mark();
     RowsInvArgs ia{p->fft, p->d_tw, z, p->d_weights, partial, n, k, p->inv_rows_per_cta, p->ksplit};
-    dim3 g3(ceil_div(n, p->inv_rows_per_cta), p->ksplit, bc);
-    pwfs_rows_inv<<<g3, kThreads, inv_smem(n, p->inv_rows_per_cta), st>>>(ia);
+    if (f) {
+      dim3 g3(ceil_div(n, f->l_inv), p->ksplit, bc);
+      f->inv<<<g3, f->t * f->l_inv, f->smem_inv, st>>>(ia);
+    } else {
+      dim3 g3(ceil_div(n, p->inv_rows_per_cta), p->ksplit, bc);
+      pwfs_rows_inv<<<g3, kThreads, inv_smem(n, p->inv_rows_per_cta), st>>>(ia);
+    }
     mark();
     dim3 g4(p->cam, bc);
     pwfs_bin<<<g4, 128, 0, st>>>(partial, frame + (size_t)b0 * p->cam * p->cam,
@@ -678,3 +732,16 @@ extern "C" int oopao_pwfs_profile_read(oopao_pwfs_plan* p, double* ms, int* laun
   pr->used = 0;
   return OOPAO_OK;
 }
+
+extern "C" int oopao_pwfs_set_variant(oopao_pwfs_plan* p, int variant) {
+  OOPAO_CHECK_ARG(p, "NULL plan");
+  OOPAO_CHECK_ARG(variant == 0 || variant == 1, "variant must be 0 (generic) or 1 (compile-time plan)");
+  if (variant == 1 && !p->fast) {
+    oopao_set_last_error("no compile-time plan for this FFT size", __FILE__, __LINE__);
+    return OOPAO_ERR_UNSUPPORTED;
+  }
+  p->variant = variant;
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_pwfs_get_variant(const oopao_pwfs_plan* p) { return p ? p->variant : -1; }

@@ -1,0 +1,252 @@
+// Compile-time-planned propagation passes (N = R1*R2), see fft2.cuh.
+// Same inputs/outputs as the generic kernels in pwfs.cu; one shared-memory
+// exchange per line FFT and the forward->mask->inverse column chain kept in
+// registers.
+#pragma once
+#include "fft2.cuh"
+
+// ---- pass 1: field build + forward row FFT (j-fastest thread mapping) ----
+template <int N, int R1, int R2, int T, int L>
+__global__ void __launch_bounds__(T* L) pwfs_rows_fwd2(RowsFwdArgs a) {
+  constexpr int R1P = pad_odd(R1), LS = R2 * R1P;
+  constexpr int PBA = (R2 + T - 1) / T, PBB = (R1 + T - 1) / T;
+  extern __shared__ float2 sm[];
+  float2* tw = sm;      // tw[m*R1 + j] = W_N^{j m}
+  float2* xb = sm + N;  // [L][LS]
+  const int tid = threadIdx.x;
+  const int l = tid / T, t = tid - (tid / T) * T;
+  for (int i = tid; i < N; i += T * L) tw[i] = a.tw[(i % R1) * (i / R1)];
+  const int b = blockIdx.z, kk = blockIdx.y, row = blockIdx.x * L + l;
+  const bool active = row < a.res;
+  const int res = a.res, off = a.off;
+  const float* opd = a.opd + (size_t)b * res * res + (size_t)row * res;
+  const float* amp = a.amp + (size_t)row * res;
+  const float2* rf = a.rowfac + (size_t)kk * res;
+  const float2 cf = active ? a.colfac[(size_t)kk * res + row] : make_float2(0.f, 0.f);
+  float2* x = xb + l * LS;
+#pragma unroll
+  for (int p = 0; p < PBA; p++) {
+    const int j = t + p * T;
+    if (j < R2 && active) {
+      float2 v[R1];
+#pragma unroll
+      for (int m = 0; m < R1; m++) {
+        const int jc = j + m * R2 - off;
+        float2 e = make_float2(0.f, 0.f);
+        if (jc >= 0 && jc < res) {
+          const float am = amp[jc];
+          if (am != 0.f) {
+            float s, c;
+            sincosf(opd[jc] * a.phase_scale, &s, &c);
+            e = cmul(cmul(make_float2(am * c, am * s), rf[jc]), cf);
+          }
+        }
+        v[m] = e;
+      }
+      dft<R1, false>(v);
+#pragma unroll
+      for (int q = 0; q < R1; q++) x[j * R1P + q] = v[q];
+    }
+  }
+  __syncthreads();
+  float2* y = a.y + (((size_t)b * a.k + kk) * res + row) * N;
+#pragma unroll
+  for (int p = 0; p < PBB; p++) {
+    const int j = t + p * T;
+    if (j < R1 && active) {
+      float2 v[R2];
+#pragma unroll
+      for (int m = 0; m < R2; m++) {
+        const float2 u = x[m * R1P + j];
+        v[m] = (m == 0) ? u : cmul(u, tw[m * R1 + j]);
+      }
+      dft<R2, false>(v);
+#pragma unroll
+      for (int q = 0; q < R2; q++) y[j + q * R1] = v[q];
+    }
+  }
+}
+
+__host__ __device__ constexpr int odd_up(int v) { return (v % 2 == 0) ? v + 1 : v; }
+__host__ __device__ constexpr int imax(int a, int b) { return a > b ? a : b; }
+
+// ---- pass 2: column forward FFT, mask, inverse FFT (l-fastest mapping) ----
+template <int N, int R1, int R2, int T, int L>
+__global__ void __launch_bounds__(T* L) pwfs_cols2(ColsArgs a) {
+  constexpr int R1P = pad_odd(R1), R2P = pad_odd(R2);
+  constexpr int LS = odd_up(imax(R2 * R1P, R1 * R2P));
+  constexpr int PBA = (R2 + T - 1) / T;   // forward stage A / inverse stage B' butterflies
+  constexpr int PBB = (R1 + T - 1) / T;   // forward stage B / inverse stage A' butterflies
+  extern __shared__ float2 sm[];
+  float2* tw = sm;           // tw[m*R1 + j]  = W_N^{j m},  j < R1, m < R2
+  float2* twi = sm + N;      // twi[m*R2 + j] = W_N^{-j m}, j < R2, m < R1
+  float2* b1 = sm + 2 * N;   // [L][LS] forward exchange
+  float2* b2 = b1 + L * LS;  // [L][LS] inverse exchange
+  const int tid = threadIdx.x;
+  const int l = tid % L, t = tid / L;
+  for (int i = tid; i < N; i += T * L) {
+    tw[i] = a.tw[(i % R1) * (i / R1)];
+    const float2 w = a.tw[(i % R2) * (i / R2)];
+    twi[i] = make_float2(w.x, -w.y);
+  }
+  const int b = blockIdx.z, kk = blockIdx.y, c = blockIdx.x * L + l;
+  const bool active = c < N;
+  const int res = a.res, off = a.off;
+  const float2* y = a.y + ((size_t)b * a.k + kk) * res * N + c;
+  float2* x1 = b1 + l * LS;
+  float2* x2 = b2 + l * LS;
+  // forward stage A: rows e = j + m*R2, non-zero for off <= e < off + res
+#pragma unroll
+  for (int p = 0; p < PBA; p++) {
+    const int j = t + p * T;
+    if (j < R2) {
+      float2 v[R1];
+#pragma unroll
+      for (int m = 0; m < R1; m++) {
+        const int i = j + m * R2 - off;
+        v[m] = (active && i >= 0 && i < res) ? y[(size_t)i * N] : make_float2(0.f, 0.f);
+      }
+      dft<R1, false>(v);
+#pragma unroll
+      for (int q = 0; q < R1; q++) x1[j * R1P + q] = v[q];
+    }
+  }
+  __syncthreads();
+  // forward stage B, mask, inverse stage A' (radix R2, same registers)
+  const float2* mk = a.mask + c;
+#pragma unroll
+  for (int p = 0; p < PBB; p++) {
+    const int j = t + p * T;
+    if (j < R1) {
+      float2 v[R2];
+#pragma unroll
+      for (int m = 0; m < R2; m++) {
+        const float2 u = x1[m * R1P + j];
+        v[m] = (m == 0) ? u : cmul(u, tw[m * R1 + j]);
+      }
+      dft<R2, false>(v);
+#pragma unroll
+      for (int q = 0; q < R2; q++) {
+        const float2 mq = active ? mk[(size_t)(j + q * R1) * N] : make_float2(0.f, 0.f);
+        v[q] = cmul(v[q], mq);
+      }
+      dft<R2, true>(v);
+#pragma unroll
+      for (int q = 0; q < R2; q++) x2[j * R2P + q] = v[q];
+    }
+  }
+  __syncthreads();
+  // inverse stage B' (radix R1, span R2): outputs rows j + q*R2
+  float2* z = a.z + ((size_t)b * a.k + kk) * N * N + c;
+#pragma unroll
+  for (int p = 0; p < PBA; p++) {
+    const int j = t + p * T;
+    if (j < R2) {
+      float2 v[R1];
+#pragma unroll
+      for (int m = 0; m < R1; m++) {
+        const float2 u = x2[m * R2P + j];
+        v[m] = (m == 0) ? u : cmul(u, twi[m * R2 + j]);
+      }
+      dft<R1, true>(v);
+      if (active) {
+#pragma unroll
+        for (int q = 0; q < R1; q++) z[(size_t)(j + q * R2) * N] = v[q];
+      }
+    }
+  }
+}
+
+// ---- pass 3: row inverse FFT, |.|^2 summed over a range of points ----
+template <int N, int R1, int R2, int T, int L>
+__global__ void __launch_bounds__(T* L) pwfs_rows_inv2(RowsInvArgs a) {
+  constexpr int R2P = pad_odd(R2), LS = R1 * R2P;
+  constexpr int PBA = (R1 + T - 1) / T;  // inverse stage A' (radix R2) butterflies
+  constexpr int PBB = (R2 + T - 1) / T;  // inverse stage B' (radix R1) butterflies
+  extern __shared__ float2 sm[];
+  float2* twi = sm;          // twi[m*R2 + j] = W_N^{-j m}
+  float2* xb = sm + N;       // [2][L][LS]
+  const int tid = threadIdx.x;
+  const int l = tid / T, t = tid - (tid / T) * T;
+  for (int i = tid; i < N; i += T * L) {
+    const float2 w = a.tw[(i % R2) * (i / R2)];
+    twi[i] = make_float2(w.x, -w.y);
+  }
+  const int b = blockIdx.z, slot = blockIdx.y, row = blockIdx.x * L + l;
+  const bool active = row < N;
+  const int kbeg = (int)(((long long)slot * a.k) / a.ksplit);
+  const int kend = (int)(((long long)(slot + 1) * a.k) / a.ksplit);
+  float acc[PBB][R1];
+#pragma unroll
+  for (int p = 0; p < PBB; p++)
+#pragma unroll
+    for (int q = 0; q < R1; q++) acc[p][q] = 0.f;
+  __syncthreads();
+  for (int kk = kbeg; kk < kend; kk++) {
+    float2* x = xb + ((kk - kbeg) & 1) * L * LS + l * LS;
+    const float2* z = a.z + (((size_t)b * a.k + kk) * N + row) * N;
+#pragma unroll
+    for (int p = 0; p < PBA; p++) {
+      const int j = t + p * T;
+      if (j < R1) {
+        float2 v[R2];
+#pragma unroll
+        for (int m = 0; m < R2; m++) v[m] = active ? z[j + m * R1] : make_float2(0.f, 0.f);
+        dft<R2, true>(v);
+#pragma unroll
+        for (int q = 0; q < R2; q++) x[j * R2P + q] = v[q];
+      }
+    }
+    __syncthreads();
+    const float w = a.weights ? a.weights[kk] : 1.f;
+#pragma unroll
+    for (int p = 0; p < PBB; p++) {
+      const int j = t + p * T;
+      if (j < R2) {
+        float2 v[R1];
+#pragma unroll
+        for (int m = 0; m < R1; m++) {
+          const float2 u = x[m * R2P + j];
+          v[m] = (m == 0) ? u : cmul(u, twi[m * R2 + j]);
+        }
+        dft<R1, true>(v);
+#pragma unroll
+        for (int q = 0; q < R1; q++) acc[p][q] = fmaf(w, cabs2(v[q]), acc[p][q]);
+      }
+    }
+  }
+  if (!active) return;
+  float* out = a.partial + (((size_t)b * a.ksplit + slot) * N + row) * N;
+#pragma unroll
+  for (int p = 0; p < PBB; p++) {
+    const int j = t + p * T;
+    if (j < R2) {
+#pragma unroll
+      for (int q = 0; q < R1; q++) out[j + q * R2] = acc[p][q];
+    }
+  }
+}
+
+// ---- registry ----
+struct FastPasses {
+  int n, t, l_rows, l_cols, l_inv;
+  void (*rows)(RowsFwdArgs);
+  void (*cols)(ColsArgs);
+  void (*inv)(RowsInvArgs);
+  size_t smem_rows, smem_cols, smem_inv;
+};
+
+template <int N, int R1, int R2, int T, int LR, int LC, int LI>
+FastPasses make_fast() {
+  constexpr int R1P = pad_odd(R1), R2P = pad_odd(R2);
+  constexpr int LSC = odd_up(imax(R2 * R1P, R1 * R2P));
+  FastPasses f;
+  f.n = N; f.t = T; f.l_rows = LR; f.l_cols = LC; f.l_inv = LI;
+  f.rows = pwfs_rows_fwd2<N, R1, R2, T, LR>;
+  f.cols = pwfs_cols2<N, R1, R2, T, LC>;
+  f.inv = pwfs_rows_inv2<N, R1, R2, T, LI>;
+  f.smem_rows = sizeof(float2) * (N + (size_t)LR * R2 * R1P);
+  f.smem_cols = sizeof(float2) * (2 * N + 2 * (size_t)LC * LSC);
+  f.smem_inv = sizeof(float2) * (N + 2 * (size_t)LI * R1 * R2P);
+  return f;
+}

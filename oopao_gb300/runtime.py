@@ -9,9 +9,34 @@ import torch
 from .tools import OopaoError
 
 
+_linalg_loaded = False
+
+
+def _preload_torch_linalg():
+    """Load torch's CUDA linear-algebra library by absolute path.
+
+    torch opens it lazily by file name at the first ``torch.linalg`` call on a
+    GPU tensor; under some launchers (profilers that rewrite the loader
+    environment) that lookup fails.  Loading it once here makes the later
+    lookup resolve to the already-loaded library."""
+    global _linalg_loaded
+    if _linalg_loaded:
+        return
+    _linalg_loaded = True
+    import ctypes
+    import os
+    p = os.path.join(os.path.dirname(torch.__file__), 'lib', 'libtorch_cuda_linalg.so')
+    if os.path.exists(p):
+        try:
+            ctypes.CDLL(p, mode=ctypes.RTLD_GLOBAL)
+        except OSError:
+            pass
+
+
 def device():
     if not torch.cuda.is_available():
         raise OopaoError('oopao_gb300 needs a CUDA device (GB300); none is visible')
+    _preload_torch_linalg()
     return torch.device('cuda', torch.cuda.current_device())
 
 

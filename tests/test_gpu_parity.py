@@ -62,8 +62,11 @@ def test_geometry_and_valid_pixels(system):
 
 def test_reference_signal(system):
     name, d, (tel, ngs, dm, wfs) = system
+    # a symmetric geometry makes the float64 reference pure round-off (~1e-16);
+    # measure the error against the slope scale of an aberrated measurement
     ref = d['reference_2d']
-    err = np.linalg.norm(wfs.referenceSignal_2D - ref) / max(np.linalg.norm(ref), 1e-3 * np.sqrt(ref.size))
+    scale = max(np.linalg.norm(ref), np.linalg.norm(d['dm_signal_2D']))
+    err = np.linalg.norm(wfs.referenceSignal_2D - ref) / scale
     assert err < TOL_FP32, err
 
 
