@@ -65,10 +65,16 @@ int oopao_pwfs_set_amplitude(oopao_pwfs_plan* plan, const float* amp_host);
 /* Optional per-point weights [n_theta] (Pyramid.weight_vector, :750-755);
  * NULL restores the plain sum. */
 int oopao_pwfs_set_weights(oopao_pwfs_plan* plan, const float* weights_host);
-/* Launch shape (autotuner hook): lines per CTA of the three FFT passes and
- * the number of partial sums over modulation points.  0 keeps a value. */
+/* Launch shape (autotuner hook, no reference counterpart): lines per CTA of
+ * the generic FFT passes (0 keeps a value) and the number of partial sums
+ * over modulation points (must divide n_theta; 0 = automatic, -1 keeps). */
 int oopao_pwfs_set_launch(oopao_pwfs_plan* plan, int rows_per_cta, int cols_per_cta,
                           int inv_rows_per_cta, int ksplit);
+/* Bytes of row/column FFT intermediates one pass may hold (no reference
+ * counterpart).  oopao_pwfs_measure cuts a batch into passes of whole items
+ * (or whole groups of modulation points) of at most this size so that they
+ * stay in L2 between the three FFT passes.  0 restores the default (64 MiB). */
+int oopao_pwfs_set_pass_budget(oopao_pwfs_plan* plan, size_t bytes);
 
 /* Kernel variant (no reference counterpart): 1 = compile-time two-stage
  * FFT plan for this n_fft (the default where one exists), 0 = generic

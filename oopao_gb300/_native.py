@@ -27,6 +27,7 @@ SIGNATURES = {
     'oopao_pwfs_set_amplitude': (c_int, [c_void_p, c_void_p]),
     'oopao_pwfs_set_weights': (c_int, [c_void_p, c_void_p]),
     'oopao_pwfs_set_launch': (c_int, [c_void_p, c_int, c_int, c_int, c_int]),
+    'oopao_pwfs_set_pass_budget': (c_int, [c_void_p, c_size_t]),
     'oopao_pwfs_set_variant': (c_int, [c_void_p, c_int]),
     'oopao_pwfs_get_variant': (c_int, [c_void_p]),
     'oopao_pwfs_workspace_bytes': (c_size_t, [c_void_p, c_int]),
@@ -67,22 +68,48 @@ def check(status, what=''):
         raise OopaoError('%s failed (status %d): %s' % (what, status, msg))
 
 
+def _arg(a):
+    """Pointer for an array/tensor argument (the caller keeps `a` alive)."""
+    if a is None:
+        return None
+    if hasattr(a, 'data_ptr'):
+        if not a.is_contiguous():
+            raise OopaoError('non-contiguous tensor passed to the C ABI')
+        return a.data_ptr()
+    if hasattr(a, 'ctypes') and hasattr(a, 'flags'):
+        if not a.flags['C_CONTIGUOUS']:
+            raise OopaoError('non-contiguous array passed to the C ABI')
+        return a.ctypes.data
+    return a
+
+
 def call(name, *args):
+    """Call a C-ABI entry point.  numpy arrays and torch tensors may be passed
+    directly: they are referenced by `args` for the whole call, so their
+    memory cannot be released while the library reads it."""
     lib = load()
-    st = getattr(lib, name)(*args)
+    st = getattr(lib, name)(*[_arg(a) for a in args])
     if SIGNATURES[name][0] is c_int and name not in ('oopao_abi_version', 'oopao_pwfs_n_signal',
                                                      'oopao_pwfs_get_variant'):
         check(st, name)
     return st
 
 
+def host(a, dtype):
+    """C-contiguous host copy/view of `a` with the given dtype (hold the result
+    in a variable until the call that uses it has returned)."""
+    import numpy as np
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
 def ptr(t):
-    """Device/host address of a torch tensor or numpy array (None -> NULL)."""
+    """Device address of a torch tensor (None -> NULL).  Host arrays are passed
+    to ``call`` directly instead, so that they stay alive during the call."""
     if t is None:
         return None
     if hasattr(t, 'data_ptr'):
         return t.data_ptr()
-    return t.ctypes.data
+    raise OopaoError('ptr() takes torch tensors; pass numpy arrays to call() directly')
 
 
 def stream_handle(stream=None):

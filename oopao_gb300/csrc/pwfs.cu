@@ -36,15 +36,19 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr size_t kSmemLimit = 227 * 1024;
+constexpr size_t kDefaultPassBudget = 64ull << 20;
 
 }  // namespace
 
 // Per-kernel CUDA-event timing of oopao_pwfs_measure (bench instrumentation):
-// 5 events per chunk bracket the 4 kernels on the launching stream.
+// a start/end event pair on the launching stream around every launch, tagged
+// with its stage (0 rows, 1 columns, 2 row inverse, 3 reduce/bin).
 struct PwfsProfile {
   bool enabled = false;
   std::vector<cudaEvent_t> pool;
+  std::vector<int> stage;  // stage id of each start/end pair
   size_t used = 0;
+  bool open = false;
   cudaEvent_t next() {
     if (used == pool.size()) {
       cudaEvent_t e;
@@ -52,6 +56,14 @@ struct PwfsProfile {
       pool.push_back(e);
     }
     return pool[used++];
+  }
+  // called twice per launch: before (opens a pair) and after (closes it)
+  void mark(int s, cudaStream_t st) {
+    cudaEvent_t e = next();
+    if (!e) return;
+    cudaEventRecord(e, st);
+    if (!open) stage.push_back(s);
+    open = !open;
   }
 };
 
@@ -68,7 +80,9 @@ struct oopao_pwfs_plan {
   float* d_amp;      // [res*res]
   float* d_weights;  // [k] or null
   // launch shape
-  int rows_per_cta, cols_per_cta, inv_rows_per_cta, ksplit;
+  int rows_per_cta, cols_per_cta, inv_rows_per_cta;
+  int ksplit;        // partial slots over modulation points (divides k; 0 = automatic)
+  size_t l2_budget;  // bytes of FFT intermediates per pass (kept L2-resident)
   const struct FastPasses* fast;  // compile-time plan for n, or null (generic kernels)
   int variant;                    // 1 = use `fast` when available, 0 = generic
   // signal processing
@@ -92,8 +106,8 @@ struct RowsFwdArgs {
   const float* amp;     // [res][res]
   const float2* rowfac; // [K][res]
   const float2* colfac; // [K][res]
-  float2* y;            // [B][K][res][n]
-  int res, n, k, off, lines;
+  float2* y;            // [B][kp][res][n] for the points [k0, k0+kp) of this pass
+  int res, n, k0, kp, off, lines;
 };
 
 __global__ void __launch_bounds__(kThreads) pwfs_rows_fwd(RowsFwdArgs a) {
@@ -107,8 +121,8 @@ __global__ void __launch_bounds__(kThreads) pwfs_rows_fwd(RowsFwdArgs a) {
   const int nl = min(a.lines, a.res - i0);
   for (int t = tid; t < n; t += blockDim.x) tw[t] = a.tw[t];
   const float* opd = a.opd + (size_t)b * a.res * a.res;
-  const float2* rf = a.rowfac + (size_t)kk * a.res;
-  const float2* cf = a.colfac + (size_t)kk * a.res;
+  const float2* rf = a.rowfac + (size_t)(a.k0 + kk) * a.res;
+  const float2* cf = a.colfac + (size_t)(a.k0 + kk) * a.res;
   for (int idx = tid; idx < a.lines * n; idx += blockDim.x) {
     const int line = idx / n;
     const int x = idx - line * n;
@@ -127,7 +141,7 @@ __global__ void __launch_bounds__(kThreads) pwfs_rows_fwd(RowsFwdArgs a) {
   }
   __syncthreads();
   float2* out = fft_lines<false>(buf0, buf1, a.fft, tw, nl, n, tid, blockDim.x);
-  float2* y = a.y + (((size_t)b * a.k + kk) * a.res + i0) * n;
+  float2* y = a.y + (((size_t)b * a.kp + kk) * a.res + i0) * n;
   for (int idx = tid; idx < nl * n; idx += blockDim.x) y[idx] = out[idx];
 }
 
@@ -136,8 +150,8 @@ struct ColsArgs {
   const float2* tw;
   const float2* mask;  // [n][n]
   const float2* y;     // [B][K][res][n]
-  float2* z;           // [B][K][n][n]
-  int res, n, k, off, cols;
+  float2* z;           // [B][kp][n][n]
+  int res, n, kp, off, cols;
 };
 
 __global__ void __launch_bounds__(kThreads) pwfs_cols(ColsArgs a) {
@@ -149,7 +163,7 @@ __global__ void __launch_bounds__(kThreads) pwfs_cols(ColsArgs a) {
   const int tid = threadIdx.x;
   const int b = blockIdx.z, kk = blockIdx.y, c0 = blockIdx.x * C;
   for (int t = tid; t < n; t += blockDim.x) tw[t] = a.tw[t];
-  const float2* y = a.y + ((size_t)b * a.k + kk) * a.res * n;
+  const float2* y = a.y + ((size_t)b * a.kp + kk) * a.res * n;
   // gather: column c of the tile becomes line c; rows outside [off, off+res) are zero
   for (int idx = tid; idx < C * n; idx += blockDim.x) {
     const int c = idx % C;
@@ -169,7 +183,7 @@ __global__ void __launch_bounds__(kThreads) pwfs_cols(ColsArgs a) {
   }
   __syncthreads();
   float2* g = fft_lines<true>(f, other, a.fft, tw, C, n, tid, blockDim.x);
-  float2* z = a.z + ((size_t)b * a.k + kk) * n * n;
+  float2* z = a.z + ((size_t)b * a.kp + kk) * n * n;
   for (int idx = tid; idx < C * n; idx += blockDim.x) {
     const int c = idx % C;
     const int r = idx / C;
@@ -182,8 +196,11 @@ struct RowsInvArgs {
   const float2* tw;
   const float2* z;       // [B][K][n][n]
   const float* weights;  // [K] or null
-  float* partial;        // [B][ksplit][n][n]
-  int n, k, lines, ksplit;
+  float* partial;        // [B][ksplit][n][n] un-binned partial sums, or null
+  float* binned;         // [B][ksplit][cam][cam] binned partial sums (fused binning)
+  // this pass holds points [k0, k0+kp) of each item and processes slots
+  // [s0, s0+gridDim.y); slot s sums points [s*slot_pts, (s+1)*slot_pts)
+  int n, k0, kp, s0, slot_pts, ksplit, lines, bin, cam;
 };
 
 __global__ void __launch_bounds__(kThreads) pwfs_rows_inv(RowsInvArgs a) {
@@ -194,14 +211,13 @@ __global__ void __launch_bounds__(kThreads) pwfs_rows_inv(RowsInvArgs a) {
   float2* buf1 = buf0 + a.lines * n;
   float* acc = reinterpret_cast<float*>(buf1 + a.lines * n);
   const int tid = threadIdx.x;
-  const int b = blockIdx.z, slot = blockIdx.y, r0 = blockIdx.x * a.lines;
+  const int b = blockIdx.z, slot = a.s0 + blockIdx.y, r0 = blockIdx.x * a.lines;
   const int nl = min(a.lines, n - r0);
-  const int kbeg = (int)(((long long)slot * a.k) / a.ksplit);
-  const int kend = (int)(((long long)(slot + 1) * a.k) / a.ksplit);
+  const int kbeg = slot * a.slot_pts, kend = kbeg + a.slot_pts;
   for (int t = tid; t < n; t += blockDim.x) tw[t] = a.tw[t];
   for (int idx = tid; idx < a.lines * n; idx += blockDim.x) acc[idx] = 0.f;
   for (int kk = kbeg; kk < kend; kk++) {
-    const float2* z = a.z + (((size_t)b * a.k + kk) * n + r0) * n;
+    const float2* z = a.z + (((size_t)b * a.kp + (kk - a.k0)) * n + r0) * n;
     for (int idx = tid; idx < nl * n; idx += blockDim.x) buf0[idx] = z[idx];
     __syncthreads();
     float2* g = fft_lines<true>(buf0, buf1, a.fft, tw, nl, n, tid, blockDim.x);
@@ -434,7 +450,8 @@ extern "C" int oopao_pwfs_plan_create(oopao_pwfs_plan** out, int res, int n, int
   p->rows_per_cta = std::min(8, max_lines(n, false));
   p->cols_per_cta = std::min(16, max_lines(n, false));
   p->inv_rows_per_cta = std::min(8, max_lines(n, true));
-  p->ksplit = std::min(k, 8);
+  p->ksplit = 0;  // automatic
+  p->l2_budget = kDefaultPassBudget;
   p->slopes_units = 1.f;
   p->sp_mode = -1;
 
@@ -546,23 +563,100 @@ extern "C" int oopao_pwfs_set_launch(oopao_pwfs_plan* p, int rows, int cols, int
     OOPAO_CHECK_ARG(inv_smem(p->n, inv_rows) <= kSmemLimit, "inv_rows_per_cta exceeds shared memory");
     p->inv_rows_per_cta = inv_rows;
   }
-  if (ksplit > 0) {
-    OOPAO_CHECK_ARG(ksplit <= p->k, "ksplit must not exceed n_theta");
+  if (ksplit >= 0) {
+    OOPAO_CHECK_ARG(ksplit == 0 || (ksplit <= p->k && p->k % ksplit == 0),
+                    "ksplit must divide n_theta (0 = automatic)");
     p->ksplit = ksplit;
   }
   return OOPAO_OK;
 }
 
-namespace {
-size_t item_bytes(const oopao_pwfs_plan* p) {
-  return sizeof(float2) * (size_t)p->k * ((size_t)p->res * p->n + (size_t)p->n * p->n) +
-         sizeof(float) * (size_t)p->ksplit * p->n * p->n;
+extern "C" int oopao_pwfs_set_pass_budget(oopao_pwfs_plan* p, size_t bytes) {
+  OOPAO_CHECK_ARG(p, "NULL plan");
+  p->l2_budget = bytes ? bytes : kDefaultPassBudget;
+  return OOPAO_OK;
 }
+
+namespace {
+
+constexpr int kMaxSlotsBinned = 64;  // partial sums over modulation points, fused binning
+constexpr int kMaxSlotsRaw = 8;      // partial sums kept un-binned (raw_data requested)
+constexpr int kTargetCtas = 2 * 152;
+
+// How one oopao_pwfs_measure call is cut into passes: each pass holds the
+// row/column intermediates of `bc` items x `kp` points, sized to stay
+// resident in L2 between the three FFT passes; the row-inverse pass sums
+// `slot_pts` points per partial slot.
+struct PassPlan {
+  bool fast, fused;
+  int ksplit, slot_pts, bc, kp;
+  size_t unit_bytes, bytes;
+};
+
+PassPlan plan_passes(const oopao_pwfs_plan* p, int batch, bool want_raw, size_t units) {
+  PassPlan pp;
+  const FastPasses* f = (p->variant == 1) ? p->fast : nullptr;
+  pp.fast = f != nullptr;
+  pp.fused = pp.fast && !want_raw && (f->l_inv % p->bin == 0);
+  const int k = p->k;
+  pp.unit_bytes = ((size_t)p->res * p->n + (size_t)p->n * p->n) * sizeof(float2);
+  if (units < 1) units = 1;
+  if (units >= (size_t)k) {
+    pp.bc = (int)std::min<size_t>((size_t)batch, units / k);
+    pp.kp = k;
+  } else {
+    pp.bc = 1;
+    pp.kp = (int)units;
+  }
+  const int cap = pp.fused ? kMaxSlotsBinned : kMaxSlotsRaw;
+  if (p->ksplit > 0) {
+    pp.ksplit = p->ksplit;
+  } else {
+    const int row_blocks = ceil_div(p->n, pp.fast ? f->l_inv : p->inv_rows_per_cta);
+    const int want = ceil_div(kTargetCtas, row_blocks * pp.bc);
+    int best = 1;
+    for (int d = 1; d <= k && d <= cap; d++) {
+      if (k % d) continue;
+      best = d;
+      if (d >= want) break;
+    }
+    pp.ksplit = best;
+  }
+  if (!pp.fused && pp.ksplit > kMaxSlotsRaw) {
+    int d = kMaxSlotsRaw;
+    while (k % d) d--;
+    pp.ksplit = d;
+  }
+  pp.slot_pts = k / pp.ksplit;
+  if (pp.kp < k) pp.kp = std::max(pp.slot_pts, (pp.kp / pp.slot_pts) * pp.slot_pts);
+  const size_t part = pp.fused ? (size_t)p->cam * p->cam : (size_t)p->n * p->n;
+  pp.bytes = (size_t)pp.bc * pp.kp * pp.unit_bytes + (size_t)pp.bc * pp.ksplit * part * sizeof(float) + 512;
+  return pp;
+}
+
+size_t default_units(const oopao_pwfs_plan* p, int batch) {
+  const size_t unit = ((size_t)p->res * p->n + (size_t)p->n * p->n) * sizeof(float2);
+  size_t u = std::max<size_t>(1, p->l2_budget / unit);
+  return std::min<size_t>(u, (size_t)batch * p->k);
+}
+
 }  // namespace
 
 extern "C" size_t oopao_pwfs_workspace_bytes(const oopao_pwfs_plan* p, int batch) {
   if (!p || batch < 1) return 0;
-  return item_bytes(p) * (size_t)batch + 256;
+  const size_t u = default_units(p, batch);
+  return std::max(plan_passes(p, batch, false, u).bytes, plan_passes(p, batch, true, u).bytes);
+}
+
+__global__ void pwfs_reduce_binned(const float* __restrict__ binned, float* __restrict__ frame, int cam2,
+                                   int ksplit) {
+  const int b = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cam2) return;
+  const float* q = binned + (size_t)b * ksplit * cam2 + i;
+  float s = 0.f;
+  for (int t = 0; t < ksplit; t++) s += q[(size_t)t * cam2];
+  frame[(size_t)b * cam2 + i] = s;
 }
 
 extern "C" int oopao_pwfs_measure(const oopao_pwfs_plan* p, const float* opd, double phase_scale,
@@ -571,63 +665,79 @@ extern "C" int oopao_pwfs_measure(const oopao_pwfs_plan* p, const float* opd, do
   OOPAO_CHECK_ARG(p && opd && frame && ws, "NULL argument");
   OOPAO_CHECK_ARG(batch >= 1, "batch must be >= 1");
   cudaStream_t st = (cudaStream_t)stream;
-  const size_t per = item_bytes(p);
   uintptr_t base = ((uintptr_t)ws + 255) & ~(uintptr_t)255;
   const size_t usable = ws_bytes > (base - (uintptr_t)ws) ? ws_bytes - (base - (uintptr_t)ws) : 0;
-  const int chunk = (int)std::min<size_t>((size_t)batch, usable / per);
-  if (chunk < 1) {
-    oopao_set_last_error("workspace smaller than one batch item", __FILE__, __LINE__);
+  size_t units = default_units(p, batch);
+  PassPlan pp = plan_passes(p, batch, raw != nullptr, units);
+  while (pp.bytes > usable && units > 1) {
+    units = units / 2;
+    pp = plan_passes(p, batch, raw != nullptr, units);
+  }
+  if (pp.bytes > usable) {
+    oopao_set_last_error("workspace smaller than one pass needs", __FILE__, __LINE__);
     return OOPAO_ERR_WORKSPACE;
   }
-  const int n = p->n, res = p->res, k = p->k;
+  const int n = p->n, res = p->res, k = p->k, cam = p->cam;
   float2* y = (float2*)base;
-  float2* z = y + (size_t)chunk * k * res * n;
-  float* partial = (float*)(z + (size_t)chunk * k * n * n);
+  float2* z = y + (size_t)pp.bc * pp.kp * res * n;
+  float* part = (float*)(z + (size_t)pp.bc * pp.kp * n * n);
+  const FastPasses* f = pp.fast ? p->fast : nullptr;
   PwfsProfile* prof = p->prof->enabled ? p->prof : nullptr;
-  auto mark = [&]() {
-    if (prof) {
-      cudaEvent_t e = prof->next();
-      if (e) cudaEventRecord(e, st);
-    }
+  auto mark = [&](int stage) {
+    if (prof) prof->mark(stage, st);
   };
-  for (int b0 = 0; b0 < batch; b0 += chunk) {
-    const int bc = std::min(chunk, batch - b0);
-    mark();
-    const FastPasses* f = (p->variant == 1) ? p->fast : nullptr;
-    RowsFwdArgs ra{p->fft, p->d_tw, opd + (size_t)b0 * res * res, (float)phase_scale, p->d_amp,
-                   p->d_rowfac, p->d_colfac, y, res, n, k, p->off, p->rows_per_cta};
-    if (f) {
-      dim3 g1(ceil_div(res, f->l_rows), k, bc);
-      f->rows<<<g1, f->t * f->l_rows, f->smem_rows, st>>>(ra);
-    } else {
-      dim3 g1(ceil_div(res, p->rows_per_cta), k, bc);
-      pwfs_rows_fwd<<<g1, kThreads, rows_smem(n, p->rows_per_cta), st>>>(ra);
+  int launches = 0;
+  for (int b0 = 0; b0 < batch; b0 += pp.bc) {
+    const int bc = std::min(pp.bc, batch - b0);
+    for (int k0 = 0; k0 < k; k0 += pp.kp) {
+      const int kc = std::min(pp.kp, k - k0);
+      RowsFwdArgs ra{p->fft, p->d_tw, opd + (size_t)b0 * res * res, (float)phase_scale, p->d_amp,
+                     p->d_rowfac, p->d_colfac, y, res, n, k0, kc, p->off, p->rows_per_cta};
+      mark(0);
+      if (f) {
+        dim3 g1(ceil_div(res, f->l_rows), kc, bc);
+        f->rows<<<g1, f->t * f->l_rows, f->smem_rows, st>>>(ra);
+      } else {
+        dim3 g1(ceil_div(res, p->rows_per_cta), kc, bc);
+        pwfs_rows_fwd<<<g1, kThreads, rows_smem(n, p->rows_per_cta), st>>>(ra);
+      }
+      mark(0);
+      ColsArgs ca{p->fft, p->d_tw, p->d_mask, y, z, res, n, kc, p->off, p->cols_per_cta};
+      mark(1);
+      if (f) {
+        dim3 g2(ceil_div(n, f->l_cols), kc, bc);
+        f->cols<<<g2, f->t * f->l_cols, f->smem_cols, st>>>(ca);
+      } else {
+        dim3 g2(ceil_div(n, p->cols_per_cta), kc, bc);
+        pwfs_cols<<<g2, kThreads, rows_smem(n, p->cols_per_cta), st>>>(ca);
+      }
+      mark(1);
+      RowsInvArgs ia{p->fft, p->d_tw, z, p->d_weights, pp.fused ? nullptr : part, pp.fused ? part : nullptr,
+                     n, k0, kc, k0 / pp.slot_pts, pp.slot_pts, pp.ksplit, p->inv_rows_per_cta, p->bin, cam};
+      mark(2);
+      if (f) {
+        dim3 g3(ceil_div(n, f->l_inv), kc / pp.slot_pts, bc);
+        f->inv<<<g3, f->t * f->l_inv, f->smem_inv, st>>>(ia);
+      } else {
+        dim3 g3(ceil_div(n, p->inv_rows_per_cta), kc / pp.slot_pts, bc);
+        pwfs_rows_inv<<<g3, kThreads, inv_smem(n, p->inv_rows_per_cta), st>>>(ia);
+      }
+      mark(2);
+      launches += 3;
     }
-    mark();
-    ColsArgs ca{p->fft, p->d_tw, p->d_mask, y, z, res, n, k, p->off, p->cols_per_cta};
-    if (f) {
-      dim3 g2(ceil_div(n, f->l_cols), k, bc);
-      f->cols<<<g2, f->t * f->l_cols, f->smem_cols, st>>>(ca);
+    mark(3);
+    if (pp.fused) {
+      dim3 g4(ceil_div(cam * cam, 256), bc);
+      pwfs_reduce_binned<<<g4, 256, 0, st>>>(part, frame + (size_t)b0 * cam * cam, cam * cam, pp.ksplit);
     } else {
-      dim3 g2(ceil_div(n, p->cols_per_cta), k, bc);
-      pwfs_cols<<<g2, kThreads, rows_smem(n, p->cols_per_cta), st>>>(ca);
+      dim3 g4(cam, bc);
+      pwfs_bin<<<g4, 128, 0, st>>>(part, frame + (size_t)b0 * cam * cam, raw ? raw + (size_t)b0 * n * n : nullptr,
+                                   n, cam, p->bin, pp.ksplit);
     }
-    mark();
-    RowsInvArgs ia{p->fft, p->d_tw, z, p->d_weights, partial, n, k, p->inv_rows_per_cta, p->ksplit};
-    if (f) {
-      dim3 g3(ceil_div(n, f->l_inv), p->ksplit, bc);
-      f->inv<<<g3, f->t * f->l_inv, f->smem_inv, st>>>(ia);
-    } else {
-      dim3 g3(ceil_div(n, p->inv_rows_per_cta), p->ksplit, bc);
-      pwfs_rows_inv<<<g3, kThreads, inv_smem(n, p->inv_rows_per_cta), st>>>(ia);
-    }
-    mark();
-    dim3 g4(p->cam, bc);
-    pwfs_bin<<<g4, 128, 0, st>>>(partial, frame + (size_t)b0 * p->cam * p->cam,
-                                 raw ? raw + (size_t)b0 * n * n : nullptr, n, p->cam, p->bin, p->ksplit);
-    mark();
-    oopao_count_launches(4);
+    mark(3);
+    launches += 1;
   }
+  oopao_count_launches(launches);
   OOPAO_CUDA_TRY(cudaGetLastError());
   return OOPAO_OK;
 }
@@ -712,6 +822,8 @@ extern "C" int oopao_pwfs_set_profiling(oopao_pwfs_plan* p, int enable) {
   OOPAO_CHECK_ARG(p, "NULL plan");
   p->prof->enabled = enable != 0;
   p->prof->used = 0;
+  p->prof->stage.clear();
+  p->prof->open = false;
   return OOPAO_OK;
 }
 
@@ -719,17 +831,16 @@ extern "C" int oopao_pwfs_profile_read(oopao_pwfs_plan* p, double* ms, int* laun
   OOPAO_CHECK_ARG(p && ms && launches, "NULL argument");
   PwfsProfile* pr = p->prof;
   for (int s = 0; s < 4; s++) { ms[s] = 0.0; launches[s] = 0; }
-  OOPAO_CHECK_ARG(pr->used % 5 == 0, "profile events out of step");
+  OOPAO_CHECK_ARG(pr->used % 2 == 0 && pr->used / 2 == pr->stage.size(), "profile events out of step");
   if (pr->used) OOPAO_CUDA_TRY(cudaEventSynchronize(pr->pool[pr->used - 1]));
-  for (size_t c = 0; c < pr->used; c += 5) {
-    for (int s = 0; s < 4; s++) {
-      float t = 0.f;
-      OOPAO_CUDA_TRY(cudaEventElapsedTime(&t, pr->pool[c + s], pr->pool[c + s + 1]));
-      ms[s] += t;
-      launches[s] += 1;
-    }
+  for (size_t c = 0; c < pr->stage.size(); c++) {
+    float t = 0.f;
+    OOPAO_CUDA_TRY(cudaEventElapsedTime(&t, pr->pool[2 * c], pr->pool[2 * c + 1]));
+    ms[pr->stage[c]] += t;
+    launches[pr->stage[c]] += 1;
   }
   pr->used = 0;
+  pr->stage.clear();
   return OOPAO_OK;
 }
 

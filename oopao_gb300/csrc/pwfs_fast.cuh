@@ -21,8 +21,8 @@ __global__ void __launch_bounds__(T* L) pwfs_rows_fwd2(RowsFwdArgs a) {
   const int res = a.res, off = a.off;
   const float* opd = a.opd + (size_t)b * res * res + (size_t)row * res;
   const float* amp = a.amp + (size_t)row * res;
-  const float2* rf = a.rowfac + (size_t)kk * res;
-  const float2 cf = active ? a.colfac[(size_t)kk * res + row] : make_float2(0.f, 0.f);
+  const float2* rf = a.rowfac + (size_t)(a.k0 + kk) * res;
+  const float2 cf = active ? a.colfac[(size_t)(a.k0 + kk) * res + row] : make_float2(0.f, 0.f);
   float2* x = xb + l * LS;
 #pragma unroll
   for (int p = 0; p < PBA; p++) {
@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(T* L) pwfs_rows_fwd2(RowsFwdArgs a) {
     }
   }
   __syncthreads();
-  float2* y = a.y + (((size_t)b * a.k + kk) * res + row) * N;
+  float2* y = a.y + (((size_t)b * a.kp + kk) * res + row) * N;
 #pragma unroll
   for (int p = 0; p < PBB; p++) {
     const int j = t + p * T;
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(T* L) pwfs_cols2(ColsArgs a) {
   const int b = blockIdx.z, kk = blockIdx.y, c = blockIdx.x * L + l;
   const bool active = c < N;
   const int res = a.res, off = a.off;
-  const float2* y = a.y + ((size_t)b * a.k + kk) * res * N + c;
+  const float2* y = a.y + ((size_t)b * a.kp + kk) * res * N + c;
   float2* x1 = b1 + l * LS;
   float2* x2 = b2 + l * LS;
   // forward stage A: rows e = j + m*R2, non-zero for off <= e < off + res
@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(T* L) pwfs_cols2(ColsArgs a) {
   }
   __syncthreads();
   // inverse stage B' (radix R1, span R2): outputs rows j + q*R2
-  float2* z = a.z + ((size_t)b * a.k + kk) * N * N + c;
+  float2* z = a.z + ((size_t)b * a.kp + kk) * N * N + c;
 #pragma unroll
   for (int p = 0; p < PBA; p++) {
     const int j = t + p * T;
@@ -172,10 +172,9 @@ __global__ void __launch_bounds__(T* L) pwfs_rows_inv2(RowsInvArgs a) {
     const float2 w = a.tw[(i % R2) * (i / R2)];
     twi[i] = make_float2(w.x, -w.y);
   }
-  const int b = blockIdx.z, slot = blockIdx.y, row = blockIdx.x * L + l;
+  const int b = blockIdx.z, slot = a.s0 + blockIdx.y, row = blockIdx.x * L + l;
   const bool active = row < N;
-  const int kbeg = (int)(((long long)slot * a.k) / a.ksplit);
-  const int kend = (int)(((long long)(slot + 1) * a.k) / a.ksplit);
+  const int kbeg = slot * a.slot_pts, kend = kbeg + a.slot_pts;
   float acc[PBB][R1];
 #pragma unroll
   for (int p = 0; p < PBB; p++)
@@ -184,7 +183,7 @@ __global__ void __launch_bounds__(T* L) pwfs_rows_inv2(RowsInvArgs a) {
   __syncthreads();
   for (int kk = kbeg; kk < kend; kk++) {
     float2* x = xb + ((kk - kbeg) & 1) * L * LS + l * LS;
-    const float2* z = a.z + (((size_t)b * a.k + kk) * N + row) * N;
+    const float2* z = a.z + (((size_t)b * a.kp + (kk - a.k0)) * N + row) * N;
 #pragma unroll
     for (int p = 0; p < PBA; p++) {
       const int j = t + p * T;
@@ -215,15 +214,46 @@ __global__ void __launch_bounds__(T* L) pwfs_rows_inv2(RowsInvArgs a) {
       }
     }
   }
-  if (!active) return;
-  float* out = a.partial + (((size_t)b * a.ksplit + slot) * N + row) * N;
+  if (a.partial) {
+    // un-binned partial rows (raw_data requested)
+    if (active) {
+      float* out = a.partial + (((size_t)b * a.ksplit + slot) * N + row) * N;
+#pragma unroll
+      for (int p = 0; p < PBB; p++) {
+        const int j = t + p * T;
+        if (j < R2) {
+#pragma unroll
+          for (int q = 0; q < R1; q++) out[j + q * R2] = acc[p][q];
+        }
+      }
+    }
+    return;
+  }
+  // fused detector binning: the CTA's L rows are L/bin whole camera rows
+  __syncthreads();
+  float* rows = reinterpret_cast<float*>(xb);  // [L][N]
 #pragma unroll
   for (int p = 0; p < PBB; p++) {
     const int j = t + p * T;
     if (j < R2) {
 #pragma unroll
-      for (int q = 0; q < R1; q++) out[j + q * R2] = acc[p][q];
+      for (int q = 0; q < R1; q++) rows[l * N + j + q * R2] = active ? acc[p][q] : 0.f;
     }
+  }
+  __syncthreads();
+  const int bin = a.bin, cam = a.cam, ncr = L / bin, cr0 = (blockIdx.x * L) / bin;
+  float* out = a.binned + ((size_t)b * a.ksplit + slot) * cam * cam;
+  for (int i = tid; i < ncr * cam; i += T * L) {
+    const int cr = i / cam, cx = i - (i / cam) * cam;
+    if (cr0 + cr >= cam) continue;
+    float s = 0.f;
+    for (int dy = 0; dy < bin; dy++) {
+      const float* r = rows + (cr * bin + dy) * N + cx * bin;
+      float rs = 0.f;
+      for (int dx = 0; dx < bin; dx++) rs += r[dx];
+      s += rs;
+    }
+    out[(cr0 + cr) * cam + cx] = s;
   }
 }
 

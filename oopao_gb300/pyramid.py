@@ -33,8 +33,8 @@ class _Plan:
         h = N.c_void_p()
         m = np.ascontiguousarray(mask_c64, dtype=np.complex64)
         p = None if path is None else np.ascontiguousarray(np.asarray(path, dtype=np.float64))
-        N.call('oopao_pwfs_plan_create', N.ctypes.byref(h), res, n, cam, self.k, N.ptr(m),
-               None if p is None else N.ptr(p), float(tt_scale), int(bool(psf_centering)))
+        N.call('oopao_pwfs_plan_create', N.ctypes.byref(h), res, n, cam, self.k, m, p,
+               float(tt_scale), int(bool(psf_centering)))
         self.h = h
         self._amp_key = None
 
@@ -49,8 +49,8 @@ class _Plan:
     def set_amplitude(self, intensity, key):
         if key is not None and key == self._amp_key:
             return
-        amp = np.sqrt(np.asarray(intensity, dtype=np.float64) / self.k).astype(np.float32)
-        N.call('oopao_pwfs_set_amplitude', self.h, N.ptr(np.ascontiguousarray(amp)))
+        amp = N.host(np.sqrt(np.asarray(intensity, dtype=np.float64) / self.k), np.float32)
+        N.call('oopao_pwfs_set_amplitude', self.h, amp)
         self._amp_key = key
 
     def workspace_bytes(self, batch):
@@ -331,8 +331,8 @@ class Pyramid:
         if self._plan is None:
             self._plan = self._make_plan(self.modulation_path)
             if self.weight_vector is not None:
-                w = np.asarray(self.weight_vector, dtype=np.float64) / self.nTheta
-                N.call('oopao_pwfs_set_weights', self._plan.h, N.ptr(np.ascontiguousarray(w, dtype=np.float32)))
+                w = N.host(np.asarray(self.weight_vector, dtype=np.float64) / self.nTheta, np.float32)
+                N.call('oopao_pwfs_set_weights', self._plan.h, w)
             self._signal_configured = False
         return self._plan
 
@@ -399,17 +399,17 @@ class Pyramid:
         plan = plan or self.plan
         mode = SP_MODES[self.postProcessing]
         ref = self.referenceSignal_2D
-        ref_arr = None if np.isscalar(ref) else np.ascontiguousarray(np.asarray(ref, dtype=np.float32))
+        ref_arr = None if np.isscalar(ref) else N.host(ref, np.float32)
         if mode <= 2:
             npx, org = self._quadrant_origins()
-            valid = np.ascontiguousarray(self.validI4Q, dtype=np.uint8)
-            orgp = N.ptr(np.ascontiguousarray(org))
-            N.call('oopao_pwfs_set_signal_processing', plan.h, mode, npx, orgp, N.ptr(valid),
-                   N.ptr(ref_arr), float(self.slopesUnits), float(self._norma_const()))
+            valid = N.host(self.validI4Q, np.uint8)
+            org = N.host(org, np.int32)
+            N.call('oopao_pwfs_set_signal_processing', plan.h, mode, npx, org, valid, ref_arr,
+                   float(self.slopesUnits), float(self._norma_const()))
         else:
-            valid = np.ascontiguousarray(self.validSignal, dtype=np.uint8)
-            N.call('oopao_pwfs_set_signal_processing', plan.h, mode, 0, None, N.ptr(valid),
-                   N.ptr(ref_arr), float(self.slopesUnits), float(self._norma_const()))
+            valid = N.host(self.validSignal, np.uint8)
+            N.call('oopao_pwfs_set_signal_processing', plan.h, mode, 0, None, valid, ref_arr,
+                   float(self.slopesUnits), float(self._norma_const()))
         self._signal_configured = True
 
     def _signals(self, frame_dev, plan=None):

@@ -28,9 +28,10 @@ def make_plan(N, res, n, cam, mask, path, psf_centering=True, amp=None):
     m = np.ascontiguousarray(mask, dtype=np.complex64)
     p = None if path is None else np.ascontiguousarray(path, dtype=np.float64)
     N.call('oopao_pwfs_plan_create', ctypes.byref(h), res, n, cam, 1 if path is None else len(path),
-           N.ptr(m), None if p is None else N.ptr(p), 1.0, int(psf_centering))
+           m, p, 1.0, int(psf_centering))
     if amp is not None:
-        N.call('oopao_pwfs_set_amplitude', h, N.ptr(np.ascontiguousarray(amp, dtype=np.float32)))
+        a = np.ascontiguousarray(amp, dtype=np.float32)
+        N.call('oopao_pwfs_set_amplitude', h, a)
     return h
 
 
@@ -140,14 +141,14 @@ def test_signal_processing(lib, mode):
                 O.grab_quadrant(frames[0], q + 1, geom),
                 frames[0][org[2 * q]:org[2 * q] + nq, org[2 * q + 1]:org[2 * q + 1] + nq])
         if mode == 'slopesMaps':
-            N.call('oopao_pwfs_set_signal_processing', h, 0, nq, N.ptr(org),
-                   N.ptr(np.ascontiguousarray(valid, dtype=np.uint8)),
-                   N.ptr(np.ascontiguousarray(ref2d, dtype=np.float32)), 1.0, 0.0)
+            v8 = np.ascontiguousarray(valid, dtype=np.uint8)
+            r32 = np.ascontiguousarray(ref2d, dtype=np.float32)
+            N.call('oopao_pwfs_set_signal_processing', h, 0, nq, org, v8, r32, 1.0, 0.0)
             n2d = 2 * nq * nq
         else:
             vs = frames[0] >= 0.9 * frames[0].max()
-            N.call('oopao_pwfs_set_signal_processing', h, 3, 0, None,
-                   N.ptr(np.ascontiguousarray(vs, dtype=np.uint8)), None, 1.0, 0.0)
+            v8 = np.ascontiguousarray(vs, dtype=np.uint8)
+            N.call('oopao_pwfs_set_signal_processing', h, 3, 0, None, v8, None, 1.0, 0.0)
             n2d = geom.cam ** 2
         ns = N.load().oopao_pwfs_n_signal(h)
         f = torch.as_tensor(frames.astype(np.float32), device='cuda')
