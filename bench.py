@@ -162,16 +162,20 @@ def load_traffic(kernel):
         return None
 
 
-def kernel_bytes(kernel, res, n, cam, k, bc, ksplit):
-    """Algorithmic (compulsory) DRAM bytes of one launch over bc batch items."""
-    units = bc * k
+def kernel_bytes(kernel, res, n, cam, units, items, launches):
+    """Algorithmic (compulsory) DRAM bytes of a kernel summed over the timed
+    region: `units` (item, modulation point) pairs over `items` frames in
+    `launches` launches.  Per unit (complex64 intermediates): the row pass
+    writes res x N, the column pass reads res x N and writes N x N, the
+    row-inverse pass reads N x N; per item: the OPD (4 res^2) and the camera
+    frame (4 cam^2); per launch: tables (amplitude 4 res^2, mask 8 N^2)."""
     if kernel == 'pwfs_rows_fwd':
-        return units * 8 * res * n + bc * 4 * res * res + 4 * res * res
+        return units * 8 * res * n + items * 4 * res * res + launches * 4 * res * res
     if kernel == 'pwfs_cols':
-        return units * (8 * res * n + 8 * n * n) + 8 * n * n
+        return units * (8 * res * n + 8 * n * n) + launches * 8 * n * n
     if kernel == 'pwfs_rows_inv':
-        return units * 8 * n * n + bc * ksplit * 4 * n * n
-    return bc * ksplit * 4 * n * n + bc * 4 * cam * cam
+        return units * 8 * n * n + items * 4 * cam * cam
+    return items * 4 * cam * cam
 
 
 KERNELS = ['pwfs_rows_fwd', 'pwfs_cols', 'pwfs_rows_inv', 'pwfs_bin']
@@ -297,16 +301,17 @@ def run_ours(args):
     totals = {KERNELS[i]: ms[i] for i in range(4)}
     top = max(totals, key=totals.get)
     ti = KERNELS.index(top)
-    # per launch: chunks of max_batch items; bytes summed over the launches of the timed region
-    chunks = [min(wfs.max_batch, NMODES - b0) for b0 in range(0, NMODES, wfs.max_batch)] * 2 * args.steps
-    byts = sum(kernel_bytes(top, RES, n, cam, k, bc, ksplit) for bc in chunks)
+    items = frames_step * args.steps
+    units = items * k
+    nl = cnt[ti]
+    byts = kernel_bytes(top, RES, n, cam, units, items, nl)
     achieved = byts / (totals[top] / 1000.0) / 1e9
     peak, peak_kind = load_peaks()
     tr = load_traffic(top)
     traffic = None
     if tr is not None:
-        units_per_launch = np.mean(chunks) * k
-        traffic = float(tr['dram_bytes_per_unit']) * units_per_launch
+        # committed ncu capture: DRAM bytes per (item, point) unit, scaled to one launch here
+        traffic = float(tr['dram_bytes_per_unit']) * units / max(nl, 1)
     share = totals[top] / max(sum(totals.values()), 1e-12)
 
     # ---- end to end through the public API (host M2C in, host vault out)

@@ -72,8 +72,9 @@ int oopao_pwfs_set_launch(oopao_pwfs_plan* plan, int rows_per_cta, int cols_per_
                           int inv_rows_per_cta, int ksplit);
 /* Bytes of row/column FFT intermediates one pass may hold (no reference
  * counterpart).  oopao_pwfs_measure cuts a batch into passes of whole items
- * (or whole groups of modulation points) of at most this size so that they
- * stay in L2 between the three FFT passes.  0 restores the default (64 MiB). */
+ * (or whole groups of modulation points) of at most this size; a budget
+ * under the L2 size keeps them L2-resident between the three FFT passes.
+ * 0 restores the default (4 GiB). */
 int oopao_pwfs_set_pass_budget(oopao_pwfs_plan* plan, size_t bytes);
 
 /* Kernel variant (no reference counterpart): 1 = compile-time two-stage

@@ -24,15 +24,37 @@ import torch
 from .tools import OopaoError
 
 
+def _svd_fp64_gpu(D):
+    """Thin SVD D = U diag(s) V of an interaction matrix, float64 on the GPU.
+
+    Tall matrices go through the Gram matrix: eigh(D^T D) = V^T diag(s^2) V,
+    U = D V^T / s (one small symmetric eigenproblem instead of an iterative
+    SVD of the tall matrix).  Squaring the condition number costs at most
+    ~1e-16 * cond^2 relative accuracy on the smallest singular values, so a
+    full SVD is used instead when cond(D) > 1e6 or D is wide."""
+    from .runtime import device
+    dev = device()
+    Dt = torch.as_tensor(np.asarray(D, dtype=np.float64), device=dev)
+    m, n = Dt.shape
+    if m >= n:
+        ev, W = torch.linalg.eigh(Dt.T @ Dt)
+        ev = torch.flip(ev, [0])
+        W = torch.flip(W, [1])
+        smax = torch.sqrt(torch.clamp(ev[0], min=0))
+        smin = torch.sqrt(torch.clamp(ev[-1], min=0))
+        if float(smin) > 1e-6 * float(smax):
+            s = torch.sqrt(ev)
+            U = (Dt @ W) / s[None, :]
+            return U.cpu().numpy(), s.cpu().numpy(), W.T.contiguous().cpu().numpy()
+    U, s, Vh = torch.linalg.svd(Dt, full_matrices=False, driver='gesvd')
+    return U.cpu().numpy(), s.cpu().numpy(), Vh.cpu().numpy()
+
+
 class CalibrationVault:
     def __init__(self, D, nTrunc: int = 0, display: bool = False, print_details: bool = False,
                  invert: bool = True):
         if invert:
-            from .runtime import device
-            dev = device()
-            Dt = torch.as_tensor(np.asarray(D, dtype=np.float64), device=dev)
-            U, s, Vh = torch.linalg.svd(Dt, full_matrices=False)
-            U, s, V = U.cpu().numpy(), s.cpu().numpy(), Vh.cpu().numpy()
+            U, s, V = _svd_fp64_gpu(D)
             self.s = s
             self.S = np.diag(s)
             self.eigenValues = s

@@ -36,7 +36,11 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr size_t kSmemLimit = 227 * 1024;
-constexpr size_t kDefaultPassBudget = 64ull << 20;
+// Measured on GB300: passes small enough to keep the intermediates in L2
+// (<= 128 MiB) lose to large passes streaming through HBM, because the
+// per-pass launch gaps and the small grids cost more than the DRAM traffic
+// at these sizes (the passes are issue-bound, not bandwidth-bound).
+constexpr size_t kDefaultPassBudget = 4ull << 30;
 
 }  // namespace
 

@@ -104,6 +104,9 @@ def test_interaction_matrix(system, method):
     # stroke 1e-8 m: the column is a difference of O(1) slopes; FP32 cancellation
     # makes 1e-4 the meaningful bound here
     assert rel(calib.D, d['im_D']) < 1e-4
+    # the float64 pseudo-inverse of the same matrix matches the reference's SVD
+    ref_vault = og.CalibrationVault(d['im_D'])
+    assert rel(ref_vault.M, d['im_M']) < 1e-10
     calib_pp = og.InteractionMatrix(ngs, tel, dm, wfs, M2C=d['im_m2c'], stroke=1e-8, single_pass=False,
                                     method=method)
     assert rel(calib_pp.D, d['im_pp_D']) < 1e-4
