@@ -101,6 +101,26 @@ int oopao_pwfs_measure(const oopao_pwfs_plan* plan, const float* opd, double pha
                        int batch, float* frame, float* raw, void* workspace,
                        size_t workspace_bytes, void* stream);
 
+/* Allocation-free variant of oopao_pwfs_measure.  It has no counterpart in
+ * the reference.  It is for callers that cannot allocate device memory while
+ * they measure: a real-time control loop that forbids allocation once it
+ * runs, or a host framework that owns the GPU allocator.  The FFT
+ * intermediates live in a 64 MiB array compiled into the library, which every
+ * GPU that loads the library holds until the process exits; nothing is
+ * allocated or freed by this call.  Arguments as oopao_pwfs_measure, without
+ * the workspace.
+ * - A plan whose smallest pass (one group of modulation points of one item)
+ *   needs more than 64 MiB is rejected with OOPAO_ERR_WORKSPACE.
+ * - The first call on a device looks up the array's device address (set-up,
+ *   once per device, with that device current); make that first call before
+ *   any stream capture.
+ * - All calls share the one array: calls whose kernels overlap on the GPU
+ *   (other streams, other host threads) race.  Serialise them.
+ * - The plan itself is created (and allocated) beforehand at set-up time;
+ *   per-kernel profiling must be off. */
+int oopao_pwfs_measure_noalloc(const oopao_pwfs_plan* plan, const float* opd, double phase_scale,
+                               int batch, float* frame, float* raw, void* stream);
+
 /* Per-kernel timing (instrumentation, no reference counterpart): when
  * enabled, every oopao_pwfs_measure records CUDA events around its four
  * kernels (row FFT, column FFT/mask/IFFT, row IFFT/|.|^2, binning) on its

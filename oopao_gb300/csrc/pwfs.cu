@@ -27,6 +27,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -860,3 +861,64 @@ extern "C" int oopao_pwfs_set_variant(oopao_pwfs_plan* p, int variant) {
 }
 
 extern "C" int oopao_pwfs_get_variant(const oopao_pwfs_plan* p) { return p ? p->variant : -1; }
+
+// ---------------------------------------------------------------------------
+// Allocation-free measurement.
+//
+// Some callers cannot allocate device memory when they measure: a real-time
+// AO control loop that forbids allocation once it runs (an allocation can
+// block on the driver or synchronise the device), or a host framework that
+// owns the GPU allocator and exposes no way to obtain scratch memory.  For
+// them the FFT intermediates live in a fixed array compiled into this
+// library.  Every GPU that loads the library holds these bytes until the
+// process exits, so the size is kept modest.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr size_t kNoAllocScratchBytes = 64ull << 20;  // 64 MiB per device
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_scratch_addr[kNoAllocMaxDevices] = {};
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_pwfs_noalloc_scratch[kNoAllocScratchBytes];
+
+extern "C" int oopao_pwfs_measure_noalloc(const oopao_pwfs_plan* p, const float* opd, double phase_scale,
+                                          int batch, float* frame, float* raw, void* stream) {
+  OOPAO_CHECK_ARG(p && opd && frame, "NULL argument");
+  OOPAO_CHECK_ARG(batch >= 1, "batch must be >= 1");
+  OOPAO_CHECK_ARG(!p->prof->enabled,
+                  "per-kernel profiling creates CUDA events; disable it for the allocation-free entry point");
+  int dev = -1;
+  OOPAO_CUDA_TRY(cudaGetDevice(&dev));
+  OOPAO_CHECK_ARG(dev >= 0 && dev < kNoAllocMaxDevices, "device index outside the allocation-free scratch table");
+  OOPAO_CHECK_ARG(dev == p->device, "the current device is not the device the plan was created on");
+  void* scratch = nullptr;
+  {
+    // set-up, once per device, with that device current: the host-side name
+    // of the array is not a device address, so look the address up
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_scratch_addr[dev]) {
+      void* addr = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&addr, g_pwfs_noalloc_scratch);
+      if (e != cudaSuccess || addr == nullptr) {
+        oopao_set_last_error(e != cudaSuccess ? cudaGetErrorString(e) : "symbol address is NULL", __FILE__,
+                             __LINE__);
+        return OOPAO_ERR_CUDA;
+      }
+      g_noalloc_scratch_addr[dev] = addr;
+    }
+    scratch = g_noalloc_scratch_addr[dev];
+  }
+  // the smallest pass (one slot of modulation points of one item) must fit
+  const PassPlan smallest = plan_passes(p, 1, raw != nullptr, 1);
+  if (smallest.bytes > kNoAllocScratchBytes) {
+    char msg[200];
+    snprintf(msg, sizeof(msg), "one pass of this plan needs %zu bytes, more than the %zu-byte allocation-free scratch",
+             smallest.bytes, kNoAllocScratchBytes);
+    oopao_set_last_error(msg, __FILE__, __LINE__);
+    return OOPAO_ERR_WORKSPACE;
+  }
+  // every scratch byte a pass reads is written earlier in the same call, so
+  // nothing left by a previous call needs clearing
+  return oopao_pwfs_measure(p, opd, phase_scale, batch, frame, raw, scratch, kNoAllocScratchBytes, stream);
+}
