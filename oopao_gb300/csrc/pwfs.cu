@@ -80,8 +80,13 @@ struct oopao_pwfs_plan {
   FftPlan fft;
   float2* d_tw;      // [n]      exp(-2 pi i t / n)
   float2* d_mask;    // [n*n]
-  float2* d_rowfac;  // [k*res]  exp(i x_k t_j s) rho(j+off) / n^2
+  float2* d_rowfac;  // [k*res]  exp(i x_k t_j s) rho(j+off) / n^2 (per point)
   float2* d_colfac;  // [k*res]  exp(i y_k t_i s) rho(i+off)
+  // points with equal x_k share their row transform (a symmetric modulation
+  // circle has ~K/2+1 distinct x_k): group table and point -> group map
+  int ngroups;
+  float2* d_growfac;  // [ngroups*res]
+  int* d_group;       // [k]
   float* d_amp;      // [res*res]
   float* d_weights;  // [k] or null
   // launch shape
@@ -103,16 +108,30 @@ struct oopao_pwfs_plan {
 // Kernels
 // ---------------------------------------------------------------------------
 
+// Pupil field amp * exp(i opd * scale) of each item, computed once per pass
+// (shared by every modulation point).
+__global__ void pwfs_field(const float* __restrict__ opd, float scale, const float* __restrict__ amp,
+                           float2* __restrict__ field, int npix) {
+  const int b = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npix) return;
+  const float am = amp[i];
+  float2 v = make_float2(0.f, 0.f);
+  if (am != 0.f) {
+    float s, c;
+    sincosf(opd[(size_t)b * npix + i] * scale, &s, &c);
+    v = make_float2(am * c, am * s);
+  }
+  field[(size_t)b * npix + i] = v;
+}
+
 struct RowsFwdArgs {
   FftPlan fft;
   const float2* tw;
-  const float* opd;     // [B][res][res]
-  float phase_scale;
-  const float* amp;     // [res][res]
-  const float2* rowfac; // [K][res]
-  const float2* colfac; // [K][res]
-  float2* y;            // [B][kp][res][n] for the points [k0, k0+kp) of this pass
-  int res, n, k0, kp, off, lines;
+  const float2* field;   // [B][res][res] amp * exp(i phase) of this pass's items
+  const float2* rowfac;  // [groups][res] column-direction phasor of each row-transform group
+  float2* y;             // [B][ng][res][n] row transforms of groups [g0, g0+ng)
+  int res, n, g0, ng, off, lines;
 };
 
 __global__ void __launch_bounds__(kThreads) pwfs_rows_fwd(RowsFwdArgs a) {
@@ -122,41 +141,34 @@ __global__ void __launch_bounds__(kThreads) pwfs_rows_fwd(RowsFwdArgs a) {
   float2* buf0 = smem + n;
   float2* buf1 = buf0 + a.lines * n;
   const int tid = threadIdx.x;
-  const int b = blockIdx.z, kk = blockIdx.y, i0 = blockIdx.x * a.lines;
+  const int b = blockIdx.z, g = blockIdx.y, i0 = blockIdx.x * a.lines;
   const int nl = min(a.lines, a.res - i0);
   for (int t = tid; t < n; t += blockDim.x) tw[t] = a.tw[t];
-  const float* opd = a.opd + (size_t)b * a.res * a.res;
-  const float2* rf = a.rowfac + (size_t)(a.k0 + kk) * a.res;
-  const float2* cf = a.colfac + (size_t)(a.k0 + kk) * a.res;
+  const float2* fld = a.field + (size_t)b * a.res * a.res;
+  const float2* rf = a.rowfac + (size_t)(a.g0 + g) * a.res;
   for (int idx = tid; idx < a.lines * n; idx += blockDim.x) {
     const int line = idx / n;
     const int x = idx - line * n;
     const int j = x - a.off;
     float2 v = make_float2(0.f, 0.f);
-    if (line < nl && j >= 0 && j < a.res) {
-      const int i = i0 + line;
-      const float am = a.amp[i * a.res + j];
-      if (am != 0.f) {
-        float s, c;
-        sincosf(opd[i * a.res + j] * a.phase_scale, &s, &c);
-        v = cmul(cmul(make_float2(am * c, am * s), rf[j]), cf[i]);
-      }
-    }
+    if (line < nl && j >= 0 && j < a.res) v = cmul(fld[(i0 + line) * a.res + j], rf[j]);
     buf0[idx] = v;
   }
   __syncthreads();
   float2* out = fft_lines<false>(buf0, buf1, a.fft, tw, nl, n, tid, blockDim.x);
-  float2* y = a.y + (((size_t)b * a.kp + kk) * a.res + i0) * n;
+  float2* y = a.y + (((size_t)b * a.ng + g) * a.res + i0) * n;
   for (int idx = tid; idx < nl * n; idx += blockDim.x) y[idx] = out[idx];
 }
 
 struct ColsArgs {
   FftPlan fft;
   const float2* tw;
-  const float2* mask;  // [n][n]
-  const float2* y;     // [B][K][res][n]
-  float2* z;           // [B][kp][n][n]
-  int res, n, kp, off, cols;
+  const float2* mask;    // [n][n]
+  const float2* y;       // [B][ng][res][n]
+  const int* group;      // [K] row-transform group of each point, or null (group = point - k0)
+  const float2* colfac;  // [K][res] row-direction phasor of each point
+  float2* z;             // [B][kp][n][n] for the points [k0, k0+kp)
+  int res, n, k0, kp, ng, off, cols;
 };
 
 __global__ void __launch_bounds__(kThreads) pwfs_cols(ColsArgs a) {
@@ -167,15 +179,18 @@ __global__ void __launch_bounds__(kThreads) pwfs_cols(ColsArgs a) {
   float2* buf1 = buf0 + C * n;
   const int tid = threadIdx.x;
   const int b = blockIdx.z, kk = blockIdx.y, c0 = blockIdx.x * C;
+  const int kabs = a.k0 + kk;
+  const int g = a.group ? a.group[kabs] : kk;
   for (int t = tid; t < n; t += blockDim.x) tw[t] = a.tw[t];
-  const float2* y = a.y + ((size_t)b * a.kp + kk) * a.res * n;
+  const float2* y = a.y + ((size_t)b * a.ng + g) * a.res * n;
+  const float2* cf = a.colfac + (size_t)kabs * a.res;
   // gather: column c of the tile becomes line c; rows outside [off, off+res) are zero
   for (int idx = tid; idx < C * n; idx += blockDim.x) {
     const int c = idx % C;
     const int r = idx / C;
     const int i = r - a.off;
     float2 v = make_float2(0.f, 0.f);
-    if (c0 + c < n && i >= 0 && i < a.res) v = y[(size_t)i * n + c0 + c];
+    if (c0 + c < n && i >= 0 && i < a.res) v = cmul(y[(size_t)i * n + c0 + c], cf[i]);
     buf0[c * n + r] = v;
   }
   __syncthreads();
@@ -187,12 +202,12 @@ __global__ void __launch_bounds__(kThreads) pwfs_cols(ColsArgs a) {
     if (c0 + c < n) f[c * n + r] = cmul(f[c * n + r], a.mask[(size_t)r * n + c0 + c]);
   }
   __syncthreads();
-  float2* g = fft_lines<true>(f, other, a.fft, tw, C, n, tid, blockDim.x);
+  float2* gg = fft_lines<true>(f, other, a.fft, tw, C, n, tid, blockDim.x);
   float2* z = a.z + ((size_t)b * a.kp + kk) * n * n;
   for (int idx = tid; idx < C * n; idx += blockDim.x) {
     const int c = idx % C;
     const int r = idx / C;
-    if (c0 + c < n) z[(size_t)r * n + c0 + c] = g[c * n + r];
+    if (c0 + c < n) z[(size_t)r * n + c0 + c] = gg[c * n + r];
   }
 }
 
@@ -239,14 +254,16 @@ namespace {
 // Compile-time plans (N = R1*R2, T threads per line, lines per CTA of the
 // three passes).  Sizes without an entry use the generic kernels.
 const FastPasses* fast_passes(int n) {
-  static const FastPasses f72 = make_fast<72, 8, 9, 9, 16, 16, 16>();
-  static const FastPasses f96 = make_fast<96, 8, 12, 12, 16, 16, 16>();
+  // row-inverse lines per CTA are a multiple of the usual N/cam so the
+  // detector binning fuses into that pass (6 for the default geometry)
+  static const FastPasses f72 = make_fast<72, 8, 9, 9, 16, 16, 12>();
+  static const FastPasses f96 = make_fast<96, 8, 12, 12, 16, 16, 12>();
   static const FastPasses f112 = make_fast<112, 16, 7, 8, 16, 16, 16>();
   static const FastPasses f128 = make_fast<128, 16, 8, 8, 16, 16, 16>();
-  static const FastPasses f240 = make_fast<240, 16, 15, 16, 16, 16, 8>();
-  static const FastPasses f264 = make_fast<264, 24, 11, 12, 16, 16, 16>();
-  static const FastPasses f480 = make_fast<480, 24, 20, 12, 16, 8, 8>();
-  static const FastPasses f504 = make_fast<504, 24, 21, 12, 16, 8, 8>();
+  static const FastPasses f240 = make_fast<240, 16, 15, 16, 16, 16, 12>();
+  static const FastPasses f264 = make_fast<264, 24, 11, 12, 16, 16, 12>();
+  static const FastPasses f480 = make_fast<480, 24, 20, 12, 16, 8, 12>();
+  static const FastPasses f504 = make_fast<504, 24, 21, 12, 16, 8, 12>();
   switch (n) {
     case 72: return &f72;
     case 96: return &f96;
@@ -413,6 +430,8 @@ void free_plan(oopao_pwfs_plan* p) {
   cudaFree(p->d_mask);
   cudaFree(p->d_rowfac);
   cudaFree(p->d_colfac);
+  cudaFree(p->d_growfac);
+  cudaFree(p->d_group);
   cudaFree(p->d_amp);
   cudaFree(p->d_weights);
   cudaFree(p->d_valid);
@@ -492,6 +511,23 @@ extern "C" int oopao_pwfs_plan_create(oopao_pwfs_plan** out, int res, int n, int
       colfac[(size_t)kk * res + j] = make_float2((float)(dr * pr - di * pi), (float)(dr * pi + di * pr));
     }
   }
+  // row-transform groups: points whose x_k agree to 1e-12 share rowfac
+  std::vector<double> gx;
+  std::vector<int> group(k);
+  std::vector<float2> growfac;
+  for (int kk = 0; kk < k; kk++) {
+    const double xk = path_host ? path_host[2 * kk] : 0.0;
+    int g = -1;
+    for (size_t q = 0; q < gx.size(); q++)
+      if (fabs(gx[q] - xk) <= 1e-12 * std::max(1.0, fabs(xk))) { g = (int)q; break; }
+    if (g < 0) {
+      g = (int)gx.size();
+      gx.push_back(xk);
+      growfac.insert(growfac.end(), rowfac.begin() + (size_t)kk * res, rowfac.begin() + (size_t)(kk + 1) * res);
+    }
+    group[kk] = g;
+  }
+  p->ngroups = (int)gx.size();
   std::vector<float> ones((size_t)res * res, 0.f);
 #define ALLOC_COPY(dst, src, bytes)                                   \
   do {                                                                \
@@ -508,6 +544,8 @@ extern "C" int oopao_pwfs_plan_create(oopao_pwfs_plan** out, int res, int n, int
   ALLOC_COPY(p->d_mask, mask_host, sizeof(float2) * (size_t)n * n);
   ALLOC_COPY(p->d_rowfac, rowfac.data(), sizeof(float2) * rowfac.size());
   ALLOC_COPY(p->d_colfac, colfac.data(), sizeof(float2) * colfac.size());
+  ALLOC_COPY(p->d_growfac, growfac.data(), sizeof(float2) * growfac.size());
+  ALLOC_COPY(p->d_group, group.data(), sizeof(int) * group.size());
   ALLOC_COPY(p->d_amp, ones.data(), sizeof(float) * ones.size());
 #undef ALLOC_COPY
   cudaError_t e = cudaFuncSetAttribute(pwfs_rows_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
@@ -635,7 +673,8 @@ PassPlan plan_passes(const oopao_pwfs_plan* p, int batch, bool want_raw, size_t 
   pp.slot_pts = k / pp.ksplit;
   if (pp.kp < k) pp.kp = std::max(pp.slot_pts, (pp.kp / pp.slot_pts) * pp.slot_pts);
   const size_t part = pp.fused ? (size_t)p->cam * p->cam : (size_t)p->n * p->n;
-  pp.bytes = (size_t)pp.bc * pp.kp * pp.unit_bytes + (size_t)pp.bc * pp.ksplit * part * sizeof(float) + 512;
+  pp.bytes = (size_t)pp.bc * pp.kp * pp.unit_bytes + (size_t)pp.bc * pp.ksplit * part * sizeof(float) +
+             (size_t)pp.bc * p->res * p->res * sizeof(float2) + 1024;
   return pp;
 }
 
@@ -685,7 +724,8 @@ extern "C" int oopao_pwfs_measure(const oopao_pwfs_plan* p, const float* opd, do
   const int n = p->n, res = p->res, k = p->k, cam = p->cam;
   float2* y = (float2*)base;
   float2* z = y + (size_t)pp.bc * pp.kp * res * n;
-  float* part = (float*)(z + (size_t)pp.bc * pp.kp * n * n);
+  float2* field = z + (size_t)pp.bc * pp.kp * n * n;
+  float* part = (float*)(field + (size_t)pp.bc * res * res);
   const FastPasses* f = pp.fast ? p->fast : nullptr;
   PwfsProfile* prof = p->prof->enabled ? p->prof : nullptr;
   auto mark = [&](int stage) {
@@ -694,20 +734,32 @@ extern "C" int oopao_pwfs_measure(const oopao_pwfs_plan* p, const float* opd, do
   int launches = 0;
   for (int b0 = 0; b0 < batch; b0 += pp.bc) {
     const int bc = std::min(pp.bc, batch - b0);
+    mark(0);
+    {
+      dim3 g0(ceil_div(res * res, 256), bc);
+      pwfs_field<<<g0, 256, 0, st>>>(opd + (size_t)b0 * res * res, (float)phase_scale, p->d_amp, field,
+                                     res * res);
+    }
+    mark(0);
+    launches += 1;
     for (int k0 = 0; k0 < k; k0 += pp.kp) {
       const int kc = std::min(pp.kp, k - k0);
-      RowsFwdArgs ra{p->fft, p->d_tw, opd + (size_t)b0 * res * res, (float)phase_scale, p->d_amp,
-                     p->d_rowfac, p->d_colfac, y, res, n, k0, kc, p->off, p->rows_per_cta};
+      // whole items: one row transform per distinct x_k; otherwise one per point
+      const bool grouped = (kc == k);
+      const float2* gtab = grouped ? p->d_growfac : p->d_rowfac;
+      const int g0 = grouped ? 0 : k0, ng = grouped ? p->ngroups : kc;
+      RowsFwdArgs ra{p->fft, p->d_tw, field, gtab, y, res, n, g0, ng, p->off, p->rows_per_cta};
       mark(0);
       if (f) {
-        dim3 g1(ceil_div(res, f->l_rows), kc, bc);
+        dim3 g1(ceil_div(res, f->l_rows), ng, bc);
         f->rows<<<g1, f->t * f->l_rows, f->smem_rows, st>>>(ra);
       } else {
-        dim3 g1(ceil_div(res, p->rows_per_cta), kc, bc);
+        dim3 g1(ceil_div(res, p->rows_per_cta), ng, bc);
         pwfs_rows_fwd<<<g1, kThreads, rows_smem(n, p->rows_per_cta), st>>>(ra);
       }
       mark(0);
-      ColsArgs ca{p->fft, p->d_tw, p->d_mask, y, z, res, n, kc, p->off, p->cols_per_cta};
+      ColsArgs ca{p->fft, p->d_tw, p->d_mask, y, grouped ? p->d_group : nullptr, p->d_colfac, z,
+                  res, n, k0, kc, ng, p->off, p->cols_per_cta};
       mark(1);
       if (f) {
         dim3 g2(ceil_div(n, f->l_cols), kc, bc);

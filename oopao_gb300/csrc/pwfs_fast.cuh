@@ -5,10 +5,50 @@
 #pragma once
 #include "fft2.cuh"
 
-// ---- pass 1: field build + forward row FFT (j-fastest thread mapping) ----
+__host__ __device__ constexpr int odd_up(int v) { return (v % 2 == 0) ? v + 1 : v; }
+__host__ __device__ constexpr int imax(int a, int b) { return a > b ? a : b; }
+
+// Shared-memory bank conflicts of the exchange buffer of a j-fastest pass
+// (thread tid -> line tid/T, butterfly tid%T): stage-A writes at
+// line*LS + j*RP (j < nw) and stage-B reads at line*LS + j (j < nr), 8-byte
+// words, counted per 16-thread phase.  Used at compile time to pick the line
+// stride.
+__host__ __device__ constexpr int xchg_conflicts(int LS, int T, int L, int RP, int nw, int nr) {
+  int total = 0;
+  for (int pat = 0; pat < 2; pat++) {
+    const int nj = pat == 0 ? nw : nr, stride = pat == 0 ? RP : 1;
+    for (int base = 0; base < T * L; base += 16) {
+      int cnt[16] = {};
+      for (int u = 0; u < 16 && base + u < T * L; u++) {
+        const int tid = base + u, l = tid / T, t = tid % T;
+        if (t >= nj) continue;
+        cnt[(l * LS + t * stride) % 16]++;
+      }
+      int mx = 0;
+      for (int i = 0; i < 16; i++) mx = cnt[i] > mx ? cnt[i] : mx;
+      total += mx > 0 ? mx - 1 : 0;
+    }
+  }
+  return total;
+}
+
+__host__ __device__ constexpr int xchg_stride(int min_ls, int T, int L, int RP, int nw, int nr) {
+  int best = min_ls, best_c = 1 << 30;
+  for (int ls = min_ls; ls < min_ls + 16; ls++) {
+    const int c = xchg_conflicts(ls, T, L, RP, nw, nr);
+    if (c < best_c) {
+      best_c = c;
+      best = ls;
+    }
+  }
+  return best;
+}
+
+// ---- pass 1: forward row FFT of field * row phasor (j-fastest mapping) ----
 template <int N, int R1, int R2, int T, int L>
 __global__ void __launch_bounds__(T* L) pwfs_rows_fwd2(RowsFwdArgs a) {
-  constexpr int R1P = pad_odd(R1), LS = R2 * R1P;
+  constexpr int R1P = pad_odd(R1);
+  constexpr int LS = xchg_stride(R2 * R1P, T, L, R1P, R2, R1);
   constexpr int PBA = (R2 + T - 1) / T, PBB = (R1 + T - 1) / T;
   extern __shared__ float2 sm[];
   float2* tw = sm;      // tw[m*R1 + j] = W_N^{j m}
@@ -16,13 +56,11 @@ __global__ void __launch_bounds__(T* L) pwfs_rows_fwd2(RowsFwdArgs a) {
   const int tid = threadIdx.x;
   const int l = tid / T, t = tid - (tid / T) * T;
   for (int i = tid; i < N; i += T * L) tw[i] = a.tw[(i % R1) * (i / R1)];
-  const int b = blockIdx.z, kk = blockIdx.y, row = blockIdx.x * L + l;
+  const int b = blockIdx.z, g = blockIdx.y, row = blockIdx.x * L + l;
   const bool active = row < a.res;
   const int res = a.res, off = a.off;
-  const float* opd = a.opd + (size_t)b * res * res + (size_t)row * res;
-  const float* amp = a.amp + (size_t)row * res;
-  const float2* rf = a.rowfac + (size_t)(a.k0 + kk) * res;
-  const float2 cf = active ? a.colfac[(size_t)(a.k0 + kk) * res + row] : make_float2(0.f, 0.f);
+  const float2* fld = a.field + ((size_t)b * res + row) * res;
+  const float2* rf = a.rowfac + (size_t)(a.g0 + g) * res;
   float2* x = xb + l * LS;
 #pragma unroll
   for (int p = 0; p < PBA; p++) {
@@ -32,16 +70,7 @@ __global__ void __launch_bounds__(T* L) pwfs_rows_fwd2(RowsFwdArgs a) {
 #pragma unroll
       for (int m = 0; m < R1; m++) {
         const int jc = j + m * R2 - off;
-        float2 e = make_float2(0.f, 0.f);
-        if (jc >= 0 && jc < res) {
-          const float am = amp[jc];
-          if (am != 0.f) {
-            float s, c;
-            sincosf(opd[jc] * a.phase_scale, &s, &c);
-            e = cmul(cmul(make_float2(am * c, am * s), rf[jc]), cf);
-          }
-        }
-        v[m] = e;
+        v[m] = (jc >= 0 && jc < res) ? cmul(fld[jc], rf[jc]) : make_float2(0.f, 0.f);
       }
       dft<R1, false>(v);
 #pragma unroll
@@ -49,7 +78,7 @@ __global__ void __launch_bounds__(T* L) pwfs_rows_fwd2(RowsFwdArgs a) {
     }
   }
   __syncthreads();
-  float2* y = a.y + (((size_t)b * a.kp + kk) * res + row) * N;
+  float2* y = a.y + (((size_t)b * a.ng + g) * res + row) * N;
 #pragma unroll
   for (int p = 0; p < PBB; p++) {
     const int j = t + p * T;
@@ -67,10 +96,7 @@ __global__ void __launch_bounds__(T* L) pwfs_rows_fwd2(RowsFwdArgs a) {
   }
 }
 
-__host__ __device__ constexpr int odd_up(int v) { return (v % 2 == 0) ? v + 1 : v; }
-__host__ __device__ constexpr int imax(int a, int b) { return a > b ? a : b; }
-
-// ---- pass 2: column forward FFT, mask, inverse FFT (l-fastest mapping) ----
+// ---- pass 2: column phasor, forward FFT, mask, inverse FFT (l-fastest) ----
 template <int N, int R1, int R2, int T, int L>
 __global__ void __launch_bounds__(T* L) pwfs_cols2(ColsArgs a) {
   constexpr int R1P = pad_odd(R1), R2P = pad_odd(R2);
@@ -90,9 +116,12 @@ __global__ void __launch_bounds__(T* L) pwfs_cols2(ColsArgs a) {
     twi[i] = make_float2(w.x, -w.y);
   }
   const int b = blockIdx.z, kk = blockIdx.y, c = blockIdx.x * L + l;
+  const int kabs = a.k0 + kk;
+  const int g = a.group ? a.group[kabs] : kk;
   const bool active = c < N;
   const int res = a.res, off = a.off;
-  const float2* y = a.y + ((size_t)b * a.kp + kk) * res * N + c;
+  const float2* y = a.y + ((size_t)b * a.ng + g) * res * N + c;
+  const float2* cf = a.colfac + (size_t)kabs * res;
   float2* x1 = b1 + l * LS;
   float2* x2 = b2 + l * LS;
   // forward stage A: rows e = j + m*R2, non-zero for off <= e < off + res
@@ -104,7 +133,7 @@ __global__ void __launch_bounds__(T* L) pwfs_cols2(ColsArgs a) {
 #pragma unroll
       for (int m = 0; m < R1; m++) {
         const int i = j + m * R2 - off;
-        v[m] = (active && i >= 0 && i < res) ? y[(size_t)i * N] : make_float2(0.f, 0.f);
+        v[m] = (active && i >= 0 && i < res) ? cmul(y[(size_t)i * N], cf[i]) : make_float2(0.f, 0.f);
       }
       dft<R1, false>(v);
 #pragma unroll
@@ -157,10 +186,11 @@ __global__ void __launch_bounds__(T* L) pwfs_cols2(ColsArgs a) {
   }
 }
 
-// ---- pass 3: row inverse FFT, |.|^2 summed over a range of points ----
+// ---- pass 3: row inverse FFT, |.|^2 summed over a slot of points, binning ----
 template <int N, int R1, int R2, int T, int L>
 __global__ void __launch_bounds__(T* L) pwfs_rows_inv2(RowsInvArgs a) {
-  constexpr int R2P = pad_odd(R2), LS = R1 * R2P;
+  constexpr int R2P = pad_odd(R2);
+  constexpr int LS = xchg_stride(R1 * R2P, T, L, R2P, R1, R2);
   constexpr int PBA = (R1 + T - 1) / T;  // inverse stage A' (radix R2) butterflies
   constexpr int PBB = (R2 + T - 1) / T;  // inverse stage B' (radix R1) butterflies
   extern __shared__ float2 sm[];
@@ -269,14 +299,16 @@ struct FastPasses {
 template <int N, int R1, int R2, int T, int LR, int LC, int LI>
 FastPasses make_fast() {
   constexpr int R1P = pad_odd(R1), R2P = pad_odd(R2);
+  constexpr int LSR = xchg_stride(R2 * R1P, T, LR, R1P, R2, R1);
   constexpr int LSC = odd_up(imax(R2 * R1P, R1 * R2P));
+  constexpr int LSI = xchg_stride(R1 * R2P, T, LI, R2P, R1, R2);
   FastPasses f;
   f.n = N; f.t = T; f.l_rows = LR; f.l_cols = LC; f.l_inv = LI;
   f.rows = pwfs_rows_fwd2<N, R1, R2, T, LR>;
   f.cols = pwfs_cols2<N, R1, R2, T, LC>;
   f.inv = pwfs_rows_inv2<N, R1, R2, T, LI>;
-  f.smem_rows = sizeof(float2) * (N + (size_t)LR * R2 * R1P);
+  f.smem_rows = sizeof(float2) * (N + (size_t)LR * LSR);
   f.smem_cols = sizeof(float2) * (2 * N + 2 * (size_t)LC * LSC);
-  f.smem_inv = sizeof(float2) * (N + 2 * (size_t)LI * R1 * R2P);
+  f.smem_inv = sizeof(float2) * (N + 2 * (size_t)LI * LSI);
   return f;
 }
