@@ -164,6 +164,41 @@ int oopao_pwfs_signal(const oopao_pwfs_plan* plan, const float* frame, int batch
  * ------------------------------------------------------------------------ */
 int oopao_dm_opd_f32(const float* modes_t, const float* coefs, int n_act, int n_pix, int batch,
                      float scale, float* opd, void* stream);
+/* Adjoint of the projection (no reference counterpart; used by the
+ * gradients of wfs.signal with respect to dm.coefs):
+ * out[a][b] = scale * sum_p modes_t[a][p] * g[b][p];
+ * g: device [batch][n_pix]; out: device [n_act][batch]. */
+int oopao_dm_vjp_f32(const float* modes_t, const float* g, int n_act, int n_pix, int batch, float scale,
+                     float* out, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Tangent (JVP) and adjoint (VJP) of the propagation.  No reference
+ * counterpart: the reference obtains derivatives only by finite push-pull
+ * differences (OOPAO/calibration/InteractionMatrix.py:117-158).  Available
+ * for n_fft in {72, 112, 128, 264, 504} (compile-time plans), otherwise
+ * OOPAO_ERR_UNSUPPORTED.  Workspace: oopao_pwfs_ad_workspace_bytes.
+ * ------------------------------------------------------------------------ */
+size_t oopao_pwfs_ad_workspace_bytes(const oopao_pwfs_plan* plan, int batch);
+/* dframe[b] = d frame / d opd at opd0 applied to dopd[b].
+ * opd0: device [opd0_batch][res][res] operating points (opd0_batch 1 = one
+ * point shared by all tangents, e.g. an interaction matrix at a flat
+ * wavefront; or batch); dopd: device [batch][res][res]; dframe: device
+ * [batch][cam][cam].  The phase is opd*phase_scale. */
+int oopao_pwfs_jvp(const oopao_pwfs_plan* plan, const float* opd0, int opd0_batch, const float* dopd,
+                   double phase_scale, int batch, float* dframe, void* workspace, size_t workspace_bytes,
+                   void* stream);
+/* opd_bar[b] = (d frame / d opd at opd[b])^T fbar[b]; opd, opd_bar: device
+ * [batch][res][res]; fbar: device [batch][cam][cam].  Each modulation
+ * point's field is recomputed, not stored. */
+int oopao_pwfs_vjp(const oopao_pwfs_plan* plan, const float* opd, const float* fbar, double phase_scale,
+                   int batch, float* opd_bar, void* workspace, size_t workspace_bytes, void* stream);
+/* Tangent and adjoint of signalProcessing for slopesMaps and
+ * slopesMaps_incidence_flux (quotient rule through the normalisation).
+ * frame0: device [frame0_batch][cam][cam] operating-point frames. */
+int oopao_pwfs_signal_jvp(const oopao_pwfs_plan* plan, const float* frame0, int frame0_batch,
+                          const float* dframe, int batch, float* dsignal_2d, float* dsignal, void* stream);
+int oopao_pwfs_signal_vjp(const oopao_pwfs_plan* plan, const float* frame0, int frame0_batch,
+                          const float* sbar, int batch, float* fbar, void* stream);
 
 #ifdef __cplusplus
 }

@@ -41,6 +41,14 @@ SIGNATURES = {
     'oopao_pwfs_n_signal': (c_int, [c_void_p]),
     'oopao_pwfs_signal': (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     'oopao_dm_opd_f32': (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_float, c_void_p, c_void_p]),
+    'oopao_dm_vjp_f32': (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_float, c_void_p, c_void_p]),
+    'oopao_pwfs_ad_workspace_bytes': (c_size_t, [c_void_p, c_int]),
+    'oopao_pwfs_jvp': (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_double, c_int, c_void_p, c_void_p,
+                               c_size_t, c_void_p]),
+    'oopao_pwfs_vjp': (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_int, c_void_p, c_void_p, c_size_t,
+                               c_void_p]),
+    'oopao_pwfs_signal_jvp': (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
+    'oopao_pwfs_signal_vjp': (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),
 }
 
 _lib = None

@@ -98,7 +98,53 @@ __global__ void __launch_bounds__(256) dm_gemm(const float* __restrict__ modes_t
   }
 }
 
+// Adjoint of the projection: out[a][b] = scale * sum_p modes_t[a][p] g[b][p].
+// One CTA per (actuator, group of 8 batch columns); fixed-order block
+// reduction, so the result is deterministic.
+constexpr int kVjpCols = 8;
+
+__global__ void __launch_bounds__(256) dm_vjp(const float* __restrict__ modes_t, const float* __restrict__ g,
+                                              int n_act, int n_pix, int batch, float scale,
+                                              float* __restrict__ out) {
+  __shared__ float red[kVjpCols][8];
+  const int a = blockIdx.x, b0 = blockIdx.y * kVjpCols;
+  const float* m = modes_t + (size_t)a * n_pix;
+  float acc[kVjpCols];
+#pragma unroll
+  for (int c = 0; c < kVjpCols; c++) acc[c] = 0.f;
+  for (int p = threadIdx.x; p < n_pix; p += blockDim.x) {
+    const float v = m[p];
+#pragma unroll
+    for (int c = 0; c < kVjpCols; c++)
+      if (b0 + c < batch) acc[c] = fmaf(v, g[(size_t)(b0 + c) * n_pix + p], acc[c]);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+  for (int c = 0; c < kVjpCols; c++) {
+    float s = acc[c];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (l == 0) red[c][w] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < kVjpCols && b0 + (int)threadIdx.x < batch) {
+    float s = 0.f;
+    for (int i = 0; i < 8; i++) s += red[threadIdx.x][i];
+    out[(size_t)a * batch + b0 + threadIdx.x] = s * scale;
+  }
+}
+
 }  // namespace
+
+extern "C" int oopao_dm_vjp_f32(const float* modes_t, const float* g, int n_act, int n_pix, int batch, float scale,
+                                float* out, void* stream) {
+  OOPAO_CHECK_ARG(modes_t && g && out, "NULL argument");
+  OOPAO_CHECK_ARG(n_act > 0 && n_pix > 0 && batch > 0, "sizes must be positive");
+  dim3 grid(n_act, ceil_div(batch, kVjpCols));
+  dm_vjp<<<grid, 256, 0, (cudaStream_t)stream>>>(modes_t, g, n_act, n_pix, batch, scale, out);
+  oopao_count_launches(1);
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}
 
 extern "C" int oopao_dm_opd_f32(const float* modes_t, const float* coefs, int n_act, int n_pix,
                                 int batch, float scale, float* opd, void* stream) {

@@ -87,6 +87,9 @@ struct oopao_pwfs_plan {
   int ngroups;
   float2* d_growfac;  // [ngroups*res]
   int* d_group;       // [k]
+  // adjoint column pass: conjugate mask and a unit row phasor [k][n]
+  float2* d_mask_conj;
+  float2* d_ones;
   float* d_amp;      // [res*res]
   float* d_weights;  // [k] or null
   // launch shape
@@ -102,6 +105,7 @@ struct oopao_pwfs_plan {
   unsigned char* d_valid;
   float* d_ref2d;
   int* d_sig_index;
+  int* d_sig_inv;  // [n2d] signal entry of each 2-D map cell, or -1
 };
 
 // ---------------------------------------------------------------------------
@@ -432,6 +436,9 @@ void free_plan(oopao_pwfs_plan* p) {
   cudaFree(p->d_colfac);
   cudaFree(p->d_growfac);
   cudaFree(p->d_group);
+  cudaFree(p->d_mask_conj);
+  cudaFree(p->d_ones);
+  cudaFree(p->d_sig_inv);
   cudaFree(p->d_amp);
   cudaFree(p->d_weights);
   cudaFree(p->d_valid);
@@ -546,6 +553,13 @@ extern "C" int oopao_pwfs_plan_create(oopao_pwfs_plan** out, int res, int n, int
   ALLOC_COPY(p->d_colfac, colfac.data(), sizeof(float2) * colfac.size());
   ALLOC_COPY(p->d_growfac, growfac.data(), sizeof(float2) * growfac.size());
   ALLOC_COPY(p->d_group, group.data(), sizeof(int) * group.size());
+  {
+    std::vector<float2> mc((size_t)n * n), ones((size_t)k * n, make_float2(1.f, 0.f));
+    const float2* m = reinterpret_cast<const float2*>(mask_host);
+    for (size_t i = 0; i < mc.size(); i++) mc[i] = make_float2(m[i].x, -m[i].y);
+    ALLOC_COPY(p->d_mask_conj, mc.data(), sizeof(float2) * mc.size());
+    ALLOC_COPY(p->d_ones, ones.data(), sizeof(float2) * ones.size());
+  }
   ALLOC_COPY(p->d_amp, ones.data(), sizeof(float) * ones.size());
 #undef ALLOC_COPY
   cudaError_t e = cudaFuncSetAttribute(pwfs_rows_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
@@ -845,6 +859,14 @@ extern "C" int oopao_pwfs_set_signal_processing(oopao_pwfs_plan* p, int mode, in
   }
   OOPAO_CUDA_TRY(cudaMalloc((void**)&p->d_sig_index, sizeof(int) * idx.size()));
   OOPAO_CUDA_TRY(cudaMemcpy(p->d_sig_index, idx.data(), sizeof(int) * idx.size(), cudaMemcpyHostToDevice));
+  {
+    std::vector<int> inv(n2d, -1);
+    for (size_t t = 0; t < idx.size(); t++) inv[idx[t]] = (int)t;
+    cudaFree(p->d_sig_inv);
+    p->d_sig_inv = nullptr;
+    OOPAO_CUDA_TRY(cudaMalloc((void**)&p->d_sig_inv, sizeof(int) * inv.size()));
+    OOPAO_CUDA_TRY(cudaMemcpy(p->d_sig_inv, inv.data(), sizeof(int) * inv.size(), cudaMemcpyHostToDevice));
+  }
   p->sp_mode = mode;
   p->nq = nq;
   p->n2d = n2d;
@@ -856,6 +878,166 @@ extern "C" int oopao_pwfs_set_signal_processing(oopao_pwfs_plan* p, int mode, in
 }
 
 extern "C" int oopao_pwfs_n_signal(const oopao_pwfs_plan* p) { return p ? p->n_signal : -1; }
+
+// Tangent / adjoint of the slopesMaps signal (signalProcessing
+// OOPAO/Pyramid.py:838-854): s = units (Q/norma - ref), Q = (Sx, Sy) linear
+// in the masked quadrants, norma = mean over valid cells of the quadrant sum
+// (a constant for slopesMaps_incidence_flux).
+struct SignalAdArgs {
+  const float* frame0;  // [B or 1][cam][cam] operating-point frames
+  int frame0_per_item;
+  const float* dframe;  // tangent frames [B][cam][cam]
+  const float* sbar;    // signal cotangents [B][n_signal]
+  float* dsig2d;        // [B][n2d]
+  float* dsig;          // [B][n_signal]
+  float* fbar;          // [B][cam][cam]
+  const unsigned char* valid;
+  const int* sig_index;
+  const int* sig_inv;
+  int mode, cam, nq, n2d, n_signal, n_valid;
+  int q_r0[4], q_c0[4];
+  float units, norma_const;
+};
+
+__device__ __forceinline__ void quad_values(const float* fr, const SignalAdArgs& a, int r, int c, float* v) {
+#pragma unroll
+  for (int q = 0; q < 4; q++) v[q] = fr[(a.q_r0[q] + r) * a.cam + a.q_c0[q] + c];
+}
+
+__global__ void pwfs_signal_jvp(SignalAdArgs a) {
+  __shared__ float red[33];
+  const int b = blockIdx.x;
+  const float* f0 = a.frame0 + (a.frame0_per_item ? (size_t)b * a.cam * a.cam : 0);
+  const float* df = a.dframe + (size_t)b * a.cam * a.cam;
+  const int nq2 = a.nq * a.nq;
+  float p0 = 0.f, p1 = 0.f;
+  for (int idx = threadIdx.x; idx < nq2; idx += blockDim.x) {
+    if (!a.valid[idx]) continue;
+    float v0[4], v1[4];
+    quad_values(f0, a, idx / a.nq, idx % a.nq, v0);
+    quad_values(df, a, idx / a.nq, idx % a.nq, v1);
+    p0 += ((v0[0] + v0[1]) + v0[2]) + v0[3];
+    p1 += ((v1[0] + v1[1]) + v1[2]) + v1[3];
+  }
+  const float s0 = block_sum(p0, red);
+  const float s1 = block_sum(p1, red);
+  const float n0 = a.mode == 0 ? s0 / (float)a.n_valid : a.norma_const;
+  const float dn = a.mode == 0 ? s1 / (float)a.n_valid : 0.f;
+  float* s2 = a.dsig2d + (size_t)b * a.n2d;
+  for (int idx = threadIdx.x; idx < nq2; idx += blockDim.x) {
+    float sx = 0.f, sy = 0.f, dx = 0.f, dy = 0.f;
+    if (a.valid[idx]) {
+      float v0[4], v1[4];
+      quad_values(f0, a, idx / a.nq, idx % a.nq, v0);
+      quad_values(df, a, idx / a.nq, idx % a.nq, v1);
+      sx = ((v0[0] - v0[1]) + v0[3]) - v0[2];
+      sy = ((v0[0] - v0[3]) + v0[1]) - v0[2];
+      dx = ((v1[0] - v1[1]) + v1[3]) - v1[2];
+      dy = ((v1[0] - v1[3]) + v1[1]) - v1[2];
+    }
+    s2[idx] = a.units * (dx / n0 - sx * dn / (n0 * n0));
+    s2[nq2 + idx] = a.units * (dy / n0 - sy * dn / (n0 * n0));
+  }
+  __syncthreads();
+  float* sg = a.dsig + (size_t)b * a.n_signal;
+  for (int t = threadIdx.x; t < a.n_signal; t += blockDim.x) sg[t] = s2[a.sig_index[t]];
+}
+
+__global__ void pwfs_signal_vjp(SignalAdArgs a) {
+  __shared__ float red[33];
+  const int b = blockIdx.x;
+  const float* f0 = a.frame0 + (a.frame0_per_item ? (size_t)b * a.cam * a.cam : 0);
+  const float* sb = a.sbar + (size_t)b * a.n_signal;
+  const int nq2 = a.nq * a.nq;
+  float p0 = 0.f, pq = 0.f;
+  for (int idx = threadIdx.x; idx < nq2; idx += blockDim.x) {
+    if (!a.valid[idx]) continue;
+    float v0[4];
+    quad_values(f0, a, idx / a.nq, idx % a.nq, v0);
+    p0 += ((v0[0] + v0[1]) + v0[2]) + v0[3];
+    const int ix = a.sig_inv[idx], iy = a.sig_inv[nq2 + idx];
+    const float qx = ix >= 0 ? sb[ix] : 0.f, qy = iy >= 0 ? sb[iy] : 0.f;
+    const float sx = ((v0[0] - v0[1]) + v0[3]) - v0[2];
+    const float sy = ((v0[0] - v0[3]) + v0[1]) - v0[2];
+    pq += qx * sx + qy * sy;
+  }
+  const float s0 = block_sum(p0, red);
+  const float sq = block_sum(pq, red);
+  const float n0 = a.mode == 0 ? s0 / (float)a.n_valid : a.norma_const;
+  const float nbar = a.mode == 0 ? -a.units * sq / (n0 * n0) : 0.f;
+  const float dn = a.mode == 0 ? nbar / (float)a.n_valid : 0.f;
+  float* fb = a.fbar + (size_t)b * a.cam * a.cam;
+  for (int i = threadIdx.x; i < a.cam * a.cam; i += blockDim.x) fb[i] = 0.f;
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < nq2; idx += blockDim.x) {
+    if (!a.valid[idx]) continue;
+    const int r = idx / a.nq, c = idx % a.nq;
+    const int ix = a.sig_inv[idx], iy = a.sig_inv[nq2 + idx];
+    const float qx = (ix >= 0 ? sb[ix] : 0.f) * a.units / n0;
+    const float qy = (iy >= 0 ? sb[iy] : 0.f) * a.units / n0;
+    fb[(a.q_r0[0] + r) * a.cam + a.q_c0[0] + c] = qx + qy + dn;
+    fb[(a.q_r0[1] + r) * a.cam + a.q_c0[1] + c] = -qx + qy + dn;
+    fb[(a.q_r0[2] + r) * a.cam + a.q_c0[2] + c] = -qx - qy + dn;
+    fb[(a.q_r0[3] + r) * a.cam + a.q_c0[3] + c] = qx - qy + dn;
+  }
+}
+
+namespace {
+int signal_ad_args(const oopao_pwfs_plan* p, SignalAdArgs* a) {
+  OOPAO_CHECK_ARG(p->sp_mode == 0 || p->sp_mode == 1,
+                  "signal tangent/adjoint support slopesMaps and slopesMaps_incidence_flux");
+  memset(a, 0, sizeof(*a));
+  a->valid = p->d_valid;
+  a->sig_index = p->d_sig_index;
+  a->sig_inv = p->d_sig_inv;
+  a->mode = p->sp_mode;
+  a->cam = p->cam;
+  a->nq = p->nq;
+  a->n2d = p->n2d;
+  a->n_signal = p->n_signal;
+  a->n_valid = p->cam2;
+  for (int q = 0; q < 4; q++) { a->q_r0[q] = p->q_r0[q]; a->q_c0[q] = p->q_c0[q]; }
+  a->units = p->slopes_units;
+  a->norma_const = p->norma_const;
+  return OOPAO_OK;
+}
+}  // namespace
+
+extern "C" int oopao_pwfs_signal_jvp(const oopao_pwfs_plan* p, const float* frame0, int frame0_batch,
+                                     const float* dframe, int batch, float* dsignal_2d, float* dsignal,
+                                     void* stream) {
+  OOPAO_CHECK_ARG(p && frame0 && dframe && dsignal_2d && dsignal, "NULL argument");
+  OOPAO_CHECK_ARG(batch >= 1 && (frame0_batch == 1 || frame0_batch == batch), "frame0_batch must be 1 or batch");
+  SignalAdArgs a;
+  int s = signal_ad_args(p, &a);
+  if (s) return s;
+  a.frame0 = frame0;
+  a.frame0_per_item = frame0_batch != 1;
+  a.dframe = dframe;
+  a.dsig2d = dsignal_2d;
+  a.dsig = dsignal;
+  pwfs_signal_jvp<<<batch, 256, 0, (cudaStream_t)stream>>>(a);
+  oopao_count_launches(1);
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_pwfs_signal_vjp(const oopao_pwfs_plan* p, const float* frame0, int frame0_batch,
+                                     const float* sbar, int batch, float* fbar, void* stream) {
+  OOPAO_CHECK_ARG(p && frame0 && sbar && fbar, "NULL argument");
+  OOPAO_CHECK_ARG(batch >= 1 && (frame0_batch == 1 || frame0_batch == batch), "frame0_batch must be 1 or batch");
+  SignalAdArgs a;
+  int s = signal_ad_args(p, &a);
+  if (s) return s;
+  a.frame0 = frame0;
+  a.frame0_per_item = frame0_batch != 1;
+  a.sbar = sbar;
+  a.fbar = fbar;
+  pwfs_signal_vjp<<<batch, 256, 0, (cudaStream_t)stream>>>(a);
+  oopao_count_launches(1);
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}
 
 extern "C" int oopao_pwfs_signal(const oopao_pwfs_plan* p, const float* frame, int batch,
                                  float* signal_2d, float* signal, float* norma, void* stream) {
@@ -898,6 +1080,231 @@ extern "C" int oopao_pwfs_profile_read(oopao_pwfs_plan* p, double* ms, int* laun
   }
   pr->used = 0;
   pr->stage.clear();
+  return OOPAO_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Tangent (JVP) and adjoint (VJP) of the propagation, see pwfs_ad.cuh.
+// ---------------------------------------------------------------------------
+#include "pwfs_ad.cuh"
+
+namespace {
+
+const AdPasses* ad_passes(int n) {
+  static const AdPasses a72 = make_ad<72, 8, 9, 9, 12>();
+  static const AdPasses a112 = make_ad<112, 16, 7, 8, 16>();
+  static const AdPasses a128 = make_ad<128, 16, 8, 8, 16>();
+  static const AdPasses a264 = make_ad<264, 24, 11, 12, 12>();
+  static const AdPasses a504 = make_ad<504, 24, 21, 12, 12>();
+  switch (n) {
+    case 72: return &a72;
+    case 112: return &a112;
+    case 128: return &a128;
+    case 264: return &a264;
+    case 504: return &a504;
+    default: return nullptr;
+  }
+}
+
+int ad_setup(const oopao_pwfs_plan* p, const AdPasses** out) {
+  const AdPasses* a = ad_passes(p->n);
+  if (!a || !p->fast || p->variant != 1) {
+    oopao_set_last_error("tangent/adjoint passes exist for n_fft in {72,112,128,264,504} only", __FILE__, __LINE__);
+    return OOPAO_ERR_UNSUPPORTED;
+  }
+  cudaError_t e = cudaFuncSetAttribute(a->field, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a->smem_field);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(a->jvp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a->smem_jvp);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(a->vjp_a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a->smem_vjp_a);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(a->vjp_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a->smem_vjp_b);
+  if (e != cudaSuccess) {
+    oopao_set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+    return OOPAO_ERR_CUDA;
+  }
+  *out = a;
+  return OOPAO_OK;
+}
+
+// i * dopd * scale * amp * exp(i opd0 * scale): tangent of the pupil field
+__global__ void pwfs_field_tangent(const float* __restrict__ opd0, const float* __restrict__ dopd, float scale,
+                                   const float* __restrict__ amp, float2* __restrict__ out, int npix,
+                                   int opd0_per_item) {
+  const int b = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npix) return;
+  const float am = amp[i];
+  float2 v = make_float2(0.f, 0.f);
+  if (am != 0.f) {
+    float s, c;
+    sincosf(opd0[(opd0_per_item ? (size_t)b * npix : 0) + i] * scale, &s, &c);
+    const float d = dopd[(size_t)b * npix + i] * scale * am;
+    v = make_float2(-s * d, c * d);
+  }
+  out[(size_t)b * npix + i] = v;
+}
+
+__global__ void pwfs_reduce_scaled(const float* __restrict__ part, float* __restrict__ out, int m, int ksplit,
+                                   float scale) {
+  const int b = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const float* q = part + (size_t)b * ksplit * m + i;
+  float s = 0.f;
+  for (int t = 0; t < ksplit; t++) s += q[(size_t)t * m];
+  out[(size_t)b * m + i] = s * scale;
+}
+
+int ad_ksplit(const oopao_pwfs_plan* p, int rows, int bc, int cap) {
+  const int want = ceil_div(kTargetCtas, std::max(1, ceil_div(rows, 12) * bc));
+  int best = 1;
+  for (int d = 1; d <= p->k && d <= cap; d++) {
+    if (p->k % d) continue;
+    best = d;
+    if (d >= want) break;
+  }
+  return best;
+}
+
+size_t ad_item_bytes(const oopao_pwfs_plan* p, int ksplit, bool vjp) {
+  const size_t yz = (size_t)p->k * ((size_t)p->res * p->n + (size_t)p->n * p->n) * sizeof(float2);
+  const size_t fld = (size_t)p->res * p->res * sizeof(float2);
+  const size_t part = (size_t)ksplit * (vjp ? (size_t)p->res * p->res : (size_t)p->cam * p->cam) * sizeof(float);
+  return yz + fld + part;
+}
+
+}  // namespace
+
+extern "C" size_t oopao_pwfs_ad_workspace_bytes(const oopao_pwfs_plan* p, int batch) {
+  if (!p || batch < 1) return 0;
+  const size_t g = (size_t)p->k * p->n * p->n * sizeof(float2) + (size_t)p->res * p->res * sizeof(float2);
+  size_t per = std::max(ad_item_bytes(p, std::min(p->k, kMaxSlotsBinned), false),
+                        ad_item_bytes(p, std::min(p->k, kMaxSlotsBinned), true));
+  const size_t cap_items = std::max<size_t>(1, p->l2_budget / per);
+  return g + per * std::min<size_t>((size_t)batch, cap_items) + 4096;
+}
+
+extern "C" int oopao_pwfs_jvp(const oopao_pwfs_plan* p, const float* opd0, int opd0_batch, const float* dopd,
+                              double phase_scale, int batch, float* dframe, void* ws, size_t ws_bytes,
+                              void* stream) {
+  OOPAO_CHECK_ARG(p && opd0 && dopd && dframe && ws, "NULL argument");
+  OOPAO_CHECK_ARG(batch >= 1 && (opd0_batch == 1 || opd0_batch == batch), "opd0_batch must be 1 or batch");
+  const AdPasses* ad = nullptr;
+  int st0 = ad_setup(p, &ad);
+  if (st0) return st0;
+  OOPAO_CHECK_ARG(ad->l % p->bin == 0, "tangent pass needs the camera binning to divide its row block");
+  cudaStream_t st = (cudaStream_t)stream;
+  const FastPasses* f = p->fast;
+  const int n = p->n, res = p->res, k = p->k, cam = p->cam;
+  uintptr_t base = ((uintptr_t)ws + 255) & ~(uintptr_t)255;
+  const size_t usable = ws_bytes - (base - (uintptr_t)ws);
+  float2* g = (float2*)base;  // [k][n][n] operating-point fields
+  float2* w0 = g + (size_t)k * n * n;
+  char* chunk = (char*)(w0 + (size_t)res * res);
+  const size_t fixed = (size_t)(chunk - (char*)ws);
+  OOPAO_CHECK_ARG(usable > fixed, "workspace smaller than the operating-point fields");
+  // items per chunk (per-item operating points: one item per chunk)
+  int bc = opd0_batch == 1 ? batch : 1;
+  int ks = ad_ksplit(p, n, bc, kMaxSlotsBinned);
+  while (bc > 1 && fixed + (size_t)bc * ad_item_bytes(p, ks, false) > ws_bytes) {
+    bc = (bc + 1) / 2;
+    ks = ad_ksplit(p, n, bc, kMaxSlotsBinned);
+  }
+  if (fixed + (size_t)bc * ad_item_bytes(p, ks, false) > ws_bytes) {
+    oopao_set_last_error("workspace smaller than one tangent item", __FILE__, __LINE__);
+    return OOPAO_ERR_WORKSPACE;
+  }
+  float2* y = (float2*)chunk;
+  float2* z = y + (size_t)bc * k * res * n;
+  float2* fld = z + (size_t)bc * k * n * n;
+  float* part = (float*)(fld + (size_t)bc * res * res);
+  const int slot_pts = k / ks;
+  int launches = 0;
+  auto forward_to_z = [&](const float2* field, int nb) {
+    RowsFwdArgs ra{p->fft, p->d_tw, field, p->d_growfac, y, res, n, 0, p->ngroups, p->off, 0};
+    f->rows<<<dim3(ceil_div(res, f->l_rows), p->ngroups, nb), f->t * f->l_rows, f->smem_rows, st>>>(ra);
+    ColsArgs ca{p->fft, p->d_tw, p->d_mask, y, p->d_group, p->d_colfac, z, res, n, 0, k, p->ngroups, p->off, 0};
+    f->cols<<<dim3(ceil_div(n, f->l_cols), k, nb), f->t * f->l_cols, f->smem_cols, st>>>(ca);
+    launches += 2;
+  };
+  for (int b0 = 0; b0 < batch; b0 += bc) {
+    const int nb = std::min(bc, batch - b0);
+    if (b0 == 0 || opd0_batch != 1) {
+      // operating-point fields G_k of item b0 (or of the shared point)
+      const float* o0 = opd0 + (opd0_batch == 1 ? 0 : (size_t)b0 * res * res);
+      pwfs_field<<<dim3(ceil_div(res * res, 256), 1), 256, 0, st>>>(o0, (float)phase_scale, p->d_amp, w0,
+                                                                  res * res);
+      forward_to_z(w0, 1);
+      AdFieldArgs fa{p->d_tw, z, g, k};
+      ad->field<<<dim3(ceil_div(n, ad->l), k, 1), ad->t * ad->l, ad->smem_field, st>>>(fa);
+      launches += 2;
+    }
+    const float* o0 = opd0 + (opd0_batch == 1 ? 0 : (size_t)b0 * res * res);
+    pwfs_field_tangent<<<dim3(ceil_div(res * res, 256), nb), 256, 0, st>>>(
+        o0, dopd + (size_t)b0 * res * res, (float)phase_scale, p->d_amp, fld, res * res, 0);
+    forward_to_z(fld, nb);
+    AdJvpArgs ja{p->d_tw, z, g, p->d_weights, part, 0, k, 0, slot_pts, ks, p->bin, cam};
+    ad->jvp<<<dim3(ceil_div(n, ad->l), ks, nb), ad->t * ad->l, ad->smem_jvp, st>>>(ja);
+    pwfs_reduce_binned<<<dim3(ceil_div(cam * cam, 256), nb), 256, 0, st>>>(part, dframe + (size_t)b0 * cam * cam,
+                                                                           cam * cam, ks);
+    launches += 3;
+  }
+  oopao_count_launches(launches);
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_pwfs_vjp(const oopao_pwfs_plan* p, const float* opd, const float* fbar, double phase_scale,
+                              int batch, float* opd_bar, void* ws, size_t ws_bytes, void* stream) {
+  OOPAO_CHECK_ARG(p && opd && fbar && opd_bar && ws, "NULL argument");
+  OOPAO_CHECK_ARG(batch >= 1, "batch must be >= 1");
+  const AdPasses* ad = nullptr;
+  int st0 = ad_setup(p, &ad);
+  if (st0) return st0;
+  cudaStream_t st = (cudaStream_t)stream;
+  const FastPasses* f = p->fast;
+  const int n = p->n, res = p->res, k = p->k, cam = p->cam;
+  uintptr_t base = ((uintptr_t)ws + 255) & ~(uintptr_t)255;
+  const size_t slack = (size_t)(base - (uintptr_t)ws) + 256;
+  int bc = batch;
+  int ks = ad_ksplit(p, res, bc, kMaxSlotsBinned);
+  while (bc > 1 && slack + (size_t)bc * ad_item_bytes(p, ks, true) > ws_bytes) {
+    bc = (bc + 1) / 2;
+    ks = ad_ksplit(p, res, bc, kMaxSlotsBinned);
+  }
+  if (slack + (size_t)bc * ad_item_bytes(p, ks, true) > ws_bytes) {
+    oopao_set_last_error("workspace smaller than one adjoint item", __FILE__, __LINE__);
+    return OOPAO_ERR_WORKSPACE;
+  }
+  float2* y = (float2*)base;
+  float2* z = y + (size_t)bc * k * res * n;
+  float2* fld = z + (size_t)bc * k * n * n;
+  float* part = (float*)(fld + (size_t)bc * res * res);
+  const int slot_pts = k / ks;
+  int launches = 0;
+  for (int b0 = 0; b0 < batch; b0 += bc) {
+    const int nb = std::min(bc, batch - b0);
+    pwfs_field<<<dim3(ceil_div(res * res, 256), nb), 256, 0, st>>>(opd + (size_t)b0 * res * res,
+                                                                   (float)phase_scale, p->d_amp, fld, res * res);
+    RowsFwdArgs ra{p->fft, p->d_tw, fld, p->d_growfac, y, res, n, 0, p->ngroups, p->off, 0};
+    f->rows<<<dim3(ceil_div(res, f->l_rows), p->ngroups, nb), f->t * f->l_rows, f->smem_rows, st>>>(ra);
+    ColsArgs ca{p->fft, p->d_tw, p->d_mask, y, p->d_group, p->d_colfac, z, res, n, 0, k, p->ngroups, p->off, 0};
+    f->cols<<<dim3(ceil_div(n, f->l_cols), k, nb), f->t * f->l_cols, f->smem_cols, st>>>(ca);
+    // Gbar and its row FFT, in place over z
+    AdVjpAArgs va{p->d_tw, z, z, fbar + (size_t)b0 * cam * cam, p->d_weights, 0, k, p->bin, cam};
+    ad->vjp_a<<<dim3(ceil_div(n, ad->l), k, nb), ad->t * ad->l, ad->smem_vjp_a, st>>>(va);
+    // column FFT, conj(mask), column IFFT over full columns, in place
+    ColsArgs cb{p->fft, p->d_tw, p->d_mask_conj, z, nullptr, p->d_ones, z, n, n, 0, k, k, 0, 0};
+    f->cols<<<dim3(ceil_div(n, f->l_cols), k, nb), f->t * f->l_cols, f->smem_cols, st>>>(cb);
+    AdVjpBArgs vb{p->d_tw, z, fld, p->d_growfac, p->d_group, 0, p->d_colfac, part, 0, k, 0, slot_pts, ks, res,
+                  p->off};
+    ad->vjp_b<<<dim3(ceil_div(res, ad->l), ks, nb), ad->t * ad->l, ad->smem_vjp_b, st>>>(vb);
+    pwfs_reduce_scaled<<<dim3(ceil_div(res * res, 256), nb), 256, 0, st>>>(
+        part, opd_bar + (size_t)b0 * res * res, res * res, ks, (float)phase_scale);
+    launches += 7;
+  }
+  oopao_count_launches(launches);
+  OOPAO_CUDA_TRY(cudaGetLastError());
   return OOPAO_OK;
 }
 
