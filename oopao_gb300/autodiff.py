@@ -164,7 +164,7 @@ class _DMProject(torch.autograd.Function):
 
     @staticmethod
     def jvp(ctx, dc, _):
-        return ctx.dm.opd_device(dc.contiguous()), None
+        return ctx.dm.opd_device(dc.contiguous())
 
 
 def dm_signal(wfs, dm, coefs):
@@ -195,6 +195,12 @@ def jvp_interaction_matrix(ngs, tel, dm, wfs, M2C, phase_offset=None, chunk=256)
     return torch.cat(cols).T
 
 
+def _as_device(a, dev):
+    if torch.is_tensor(a):
+        return a.detach().to(device=dev, dtype=torch.float32)
+    return torch.as_tensor(np.asarray(a), dtype=torch.float32, device=dev)
+
+
 def lift_estimate(wfs, dm, M2C, target, n_iter=5, x0=None, damping=0.0):
     """Gauss-Newton modal estimation (the LiFT update of OOPAO/LiFT.py:297-330,
     P_ML = (H^T H)^-1 H^T, with the pyramid signal in place of the PSF):
@@ -202,9 +208,9 @@ def lift_estimate(wfs, dm, M2C, target, n_iter=5, x0=None, damping=0.0):
     batched tangents at the current estimate.  Returns x [nModes]."""
     dev = wfs._dev
     m2c = torch.as_tensor(np.ascontiguousarray(M2C, dtype=np.float32), device=dev)
-    t = torch.as_tensor(np.asarray(target), dtype=torch.float32, device=dev).reshape(-1)
+    t = _as_device(target, dev).reshape(-1)
     x = torch.zeros(m2c.shape[1], dtype=torch.float32, device=dev) if x0 is None else \
-        torch.as_tensor(x0, dtype=torch.float32, device=dev).clone()
+        _as_device(x0, dev).clone()
     scale = _scale(wfs)
     for _ in range(n_iter):
         opd = dm.opd_device((m2c @ x)[:, None].contiguous())
@@ -226,10 +232,10 @@ def modal_gradient_descent(wfs, dm, M2C, targets, n_iter=200, lr=1e-2, x0=None):
     and the loss history."""
     dev = wfs._dev
     m2c = torch.as_tensor(np.ascontiguousarray(M2C, dtype=np.float32), device=dev)
-    t = torch.as_tensor(np.asarray(targets), dtype=torch.float32, device=dev)
+    t = _as_device(targets, dev)
     B = t.shape[0]
     x = torch.zeros((m2c.shape[1], B), dtype=torch.float32, device=dev) if x0 is None else \
-        torch.as_tensor(x0, dtype=torch.float32, device=dev).clone()
+        _as_device(x0, dev).clone()
     x.requires_grad_(True)
     opt = torch.optim.Adam([x], lr=lr)
     hist = []
