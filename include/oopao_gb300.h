@@ -77,12 +77,16 @@ int oopao_pwfs_set_launch(oopao_pwfs_plan* plan, int rows_per_cta, int cols_per_
  * 0 restores the default (4 GiB). */
 int oopao_pwfs_set_pass_budget(oopao_pwfs_plan* plan, size_t bytes);
 
-/* Kernel variant (no reference counterpart): 1 = compile-time two-stage
- * FFT plan for this n_fft (the default where one exists), 0 = generic
- * runtime-planned kernels (any n_fft whose prime factors are <= 13).
- * Setting 1 without a compile-time plan returns OOPAO_ERR_UNSUPPORTED. */
+/* Kernel variant (autotuner hook, no reference counterpart): 0 = generic
+ * runtime-planned kernels (any n_fft whose prime factors are <= 13),
+ * 1..oopao_pwfs_num_variants = compile-time two-stage FFT plans for this
+ * n_fft (1 is the default where one exists).  An index beyond the count
+ * returns OOPAO_ERR_UNSUPPORTED.  variant_info fills info[6] with
+ * (R1, R2, threads per line, row / column / row-inverse lines per CTA). */
 int oopao_pwfs_set_variant(oopao_pwfs_plan* plan, int variant);
 int oopao_pwfs_get_variant(const oopao_pwfs_plan* plan);
+int oopao_pwfs_num_variants(const oopao_pwfs_plan* plan);
+int oopao_pwfs_variant_info(const oopao_pwfs_plan* plan, int variant, int* info);
 
 /* Bytes of device workspace oopao_pwfs_measure needs for `batch` items
  * processed in one chunk (a smaller workspace makes it loop over chunks;
@@ -164,6 +168,34 @@ int oopao_pwfs_signal(const oopao_pwfs_plan* plan, const float* frame, int batch
  * ------------------------------------------------------------------------ */
 int oopao_dm_opd_f32(const float* modes_t, const float* coefs, int n_act, int n_pix, int batch,
                      float scale, float* opd, void* stream);
+/* opd = (modes @ coefs)^T * scale + base: the DM shape added to an incoming
+ * OPD in one pass (DeformableMirror.relay, OOPAO/DeformableMirror.py:441-447:
+ * src.OPD_no_pupil += dm.OPD).  base: device [batch][n_pix] or NULL. */
+int oopao_dm_opd_acc_f32(const float* modes_t, const float* coefs, int n_act, int n_pix, int batch,
+                         float scale, const float* base, float* opd, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Closed-loop step (tutorials/AO_closed_loop_Pyramid_WFS.py:601-639,
+ * OOPAO/closed_loop/run_cl.py:176-217).  `step` is a device int counter:
+ * oopao_cl_screen reads it, oopao_cl_integrate advances it, so a captured
+ * CUDA graph of one step replays later steps without host updates.
+ * ------------------------------------------------------------------------ */
+/* Frozen-flow turbulence: opd[res][res] = sum over layers of the periodic
+ * screen q (device [heights[q]][widths[q]], OPD in m) sampled bilinearly at
+ * (y0[q] + i + vy[q]*step, x0[q] + j + vx[q]*step) (pixels).  Host arrays of
+ * n_layers <= 35 entries. */
+int oopao_cl_screen(int n_layers, const float* const* screens, const int* heights, const int* widths,
+                    const float* y0, const float* x0, const float* vy, const float* vx, int res,
+                    const int* step, float* opd, void* stream);
+/* Integrator: coefs -= gain * R @ s (R device [n_act][n_sig]); advances
+ * *step by one when step is not NULL. */
+int oopao_cl_integrate(const float* R, const float* s, int n_act, int n_sig, float gain, float* coefs,
+                       int* step, void* stream);
+/* Residual wavefront RMS over pupil pixels idx[npup] (device) written to
+ * out[*step] (device, out_len entries). */
+int oopao_cl_pupil_rms(const float* opd, const int* idx, int npup, const int* step, float* out, int out_len,
+                       void* stream);
+
 /* Adjoint of the projection (no reference counterpart; used by the
  * gradients of wfs.signal with respect to dm.coefs):
  * out[a][b] = scale * sum_p modes_t[a][p] * g[b][p];

@@ -30,6 +30,8 @@ SIGNATURES = {
     'oopao_pwfs_set_pass_budget': (c_int, [c_void_p, c_size_t]),
     'oopao_pwfs_set_variant': (c_int, [c_void_p, c_int]),
     'oopao_pwfs_get_variant': (c_int, [c_void_p]),
+    'oopao_pwfs_num_variants': (c_int, [c_void_p]),
+    'oopao_pwfs_variant_info': (c_int, [c_void_p, c_int, c_void_p]),
     'oopao_pwfs_workspace_bytes': (c_size_t, [c_void_p, c_int]),
     'oopao_pwfs_measure': (c_int, [c_void_p, c_void_p, c_double, c_int, c_void_p, c_void_p, c_void_p,
                                    c_size_t, c_void_p]),
@@ -42,6 +44,12 @@ SIGNATURES = {
     'oopao_pwfs_signal': (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     'oopao_dm_opd_f32': (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_float, c_void_p, c_void_p]),
     'oopao_dm_vjp_f32': (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_float, c_void_p, c_void_p]),
+    'oopao_dm_opd_acc_f32': (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_float, c_void_p, c_void_p,
+                                     c_void_p]),
+    'oopao_cl_screen': (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                c_int, c_void_p, c_void_p, c_void_p]),
+    'oopao_cl_integrate': (c_int, [c_void_p, c_void_p, c_int, c_int, c_float, c_void_p, c_void_p, c_void_p]),
+    'oopao_cl_pupil_rms': (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_int, c_void_p]),
     'oopao_pwfs_ad_workspace_bytes': (c_size_t, [c_void_p, c_int]),
     'oopao_pwfs_jvp': (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_double, c_int, c_void_p, c_void_p,
                                c_size_t, c_void_p]),
@@ -99,7 +107,7 @@ def call(name, *args):
     lib = load()
     st = getattr(lib, name)(*[_arg(a) for a in args])
     if SIGNATURES[name][0] is c_int and name not in ('oopao_abi_version', 'oopao_pwfs_n_signal',
-                                                     'oopao_pwfs_get_variant'):
+                                                     'oopao_pwfs_get_variant', 'oopao_pwfs_num_variants'):
         check(st, name)
     return st
 

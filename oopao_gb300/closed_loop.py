@@ -1,0 +1,198 @@
+"""Closed-loop AO step on the GPU, captured in a CUDA graph.
+
+One step follows ``tutorials/AO_closed_loop_Pyramid_WFS.py:601-639`` and
+``OOPAO/closed_loop/run_cl.py:176-217``:
+
+    turbulence OPD of the step  ->  + DM shape (modes @ coefs)
+    ->  modulated pyramid frame  ->  slopes
+    ->  coefs -= gain * reconstructor @ slopes       (frame delay 1 or 2)
+    + residual wavefront RMS over the pupil (logged on the device)
+
+Every operation is a launch of ``liboopao_gb300`` on preallocated buffers; a
+device step counter carries the time index, so the captured graph is
+replayed as is for every later step (``ClosedLoop.run``).
+
+The turbulence is a set of periodic von Karman layers translated by frozen
+flow (``VonKarmanLayers``).  It stands in for the reference's infinite
+phase screens (``OOPAO/Atmosphere.py:410-531``), whose extrusion and
+sub-pixel shift (skimage ``warp``) are not reproduced here.
+"""
+import numpy as np
+import torch
+
+from . import _native as N
+from .tools import OopaoError
+
+
+class VonKarmanLayers:
+    """Periodic von Karman OPD layers (FFT method: white Gaussian noise
+    filtered by the von Karman phase spectrum 0.023 r0^-5/3 (f^2 + L0^-2)^-11/6,
+    seeded), with frozen-flow velocities in pixels per loop step."""
+
+    def __init__(self, tel, r0, L0, fractionalR0=(1.0,), windSpeed=(10.,), windDirection=(0.,),
+                 wavelength=500e-9, size_factor=4, seed=0):
+        res = tel.resolution
+        n = 1
+        while n < size_factor * res:
+            n *= 2
+        dx = tel.D / res
+        rng = np.random.default_rng(seed)
+        f = np.fft.fftfreq(n, d=dx)
+        fx, fy = np.meshgrid(f, f)
+        f2 = fx ** 2 + fy ** 2
+        self.screens, self.vy, self.vx = [], [], []
+        self.size = n
+        df = 1.0 / (n * dx)
+        for q, frac in enumerate(fractionalR0):
+            r0l = r0 * frac ** (-3.0 / 5.0)
+            psd = 0.023 * r0l ** (-5.0 / 3.0) * (f2 + 1.0 / L0 ** 2) ** (-11.0 / 6.0)
+            psd[0, 0] = 0.0
+            noise = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+            phase = np.real(np.fft.ifft2(noise * np.sqrt(psd) * df)) * n * n
+            self.screens.append((phase * wavelength / (2 * np.pi)).astype(np.float32))
+            v = windSpeed[q] * tel.samplingTime / dx
+            ang = np.deg2rad(windDirection[q])
+            self.vy.append(v * np.sin(ang))
+            self.vx.append(v * np.cos(ang))
+
+    def origin(self, res):
+        """Screen pixel under pupil pixel (0, 0) at step 0 (the screen centre)."""
+        return (self.size - res) / 2.0
+
+    def opd(self, step, res):
+        """Host evaluation of the layers at a step (bilinear, periodic), float64."""
+        out = np.zeros((res, res))
+        o = self.origin(res)
+        ii, jj = np.meshgrid(np.arange(res), np.arange(res), indexing='ij')
+        for s, vy, vx in zip(self.screens, self.vy, self.vx):
+            n = s.shape[0]
+            y = o + ii + vy * step
+            x = o + jj + vx * step
+            y0, x0 = np.floor(y), np.floor(x)
+            dy, dx = y - y0, x - x0
+            y0, x0 = y0.astype(int) % n, x0.astype(int) % n
+            y1, x1 = (y0 + 1) % n, (x0 + 1) % n
+            s64 = s.astype(np.float64)
+            out += (1 - dy) * ((1 - dx) * s64[y0, x0] + dx * s64[y0, x1]) + \
+                dy * ((1 - dx) * s64[y1, x0] + dx * s64[y1, x1])
+        return out
+
+
+class ClosedLoop:
+    def __init__(self, tel, ngs, dm, wfs, reconstructor, gain=0.4, frame_delay=1, layers=None,
+                 max_steps=100000):
+        if frame_delay not in (1, 2):
+            raise OopaoError('frame_delay must be 1 or 2')
+        self.tel, self.ngs, self.dm, self.wfs = tel, ngs, dm, wfs
+        self.dev = wfs._dev
+        self.gain = float(gain)
+        self.frame_delay = frame_delay
+        res = tel.resolution
+        self.res = res
+        R = np.asarray(reconstructor, dtype=np.float32)
+        if R.shape != (dm.nValidAct, wfs.nSignal):
+            raise OopaoError('reconstructor must be [nValidAct, nSignal]')
+        d = self.dev
+        self.R = torch.as_tensor(np.ascontiguousarray(R), device=d)
+        self.coefs = torch.zeros(dm.nValidAct, dtype=torch.float32, device=d)
+        self.step_counter = torch.zeros(1, dtype=torch.int32, device=d)
+        self.opd_atm = torch.zeros((1, res, res), dtype=torch.float32, device=d)
+        self.opd = torch.zeros((1, res, res), dtype=torch.float32, device=d)
+        cam = wfs._cam_eff
+        self.frame = torch.zeros((1, cam, cam), dtype=torch.float32, device=d)
+        self.s2d = torch.zeros((1, wfs.validSignal.size), dtype=torch.float32, device=d)
+        self.s = torch.zeros((1, wfs.nSignal), dtype=torch.float32, device=d)
+        self.s_prev = torch.zeros_like(self.s)
+        self.max_steps = max_steps
+        self.wfe = torch.zeros(max_steps, dtype=torch.float32, device=d)
+        idx = np.flatnonzero(tel.pupil.reshape(-1)).astype(np.int32)
+        self.pupil_idx = torch.as_tensor(idx, device=d)
+        self.scale = 2 * np.pi / ngs.wavelength
+        # static configuration: amplitude, signal processing, workspace
+        ngs ** tel
+        plan = wfs.plan
+        plan.set_amplitude(ngs.intensity, wfs._amplitude_key())
+        wfs._configure_signal(plan)
+        self.plan = plan
+        self.ws_bytes = plan.workspace_bytes(1)
+        self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=d)
+        self.layers = layers
+        if layers is not None:
+            self._scr = [torch.as_tensor(s, device=d) for s in layers.screens]
+            nl = len(self._scr)
+            self._scr_ptr = (N.c_void_p * nl)(*[t.data_ptr() for t in self._scr])
+            self._h = (N.ctypes.c_int * nl)(*[t.shape[0] for t in self._scr])
+            self._w = (N.ctypes.c_int * nl)(*[t.shape[1] for t in self._scr])
+            c = np.array([layers.origin(res)] * nl, np.float32)
+            self._y0 = (N.ctypes.c_float * nl)(*c)
+            self._x0 = (N.ctypes.c_float * nl)(*c)
+            self._vy = (N.ctypes.c_float * nl)(*np.float32(layers.vy))
+            self._vx = (N.ctypes.c_float * nl)(*np.float32(layers.vx))
+        self.graph = None
+
+    def reset(self):
+        self.coefs.zero_()
+        self.step_counter.zero_()
+        self.s_prev.zero_()
+        self.wfe.zero_()
+
+    def _launch_step(self):
+        st = N.stream_handle()
+        dm, wfs = self.dm, self.wfs
+        base = None
+        if self.layers is not None:
+            N.call('oopao_cl_screen', len(self._scr), self._scr_ptr, self._h, self._w, self._y0, self._x0,
+                   self._vy, self._vx, self.res, self.step_counter, self.opd_atm, st)
+            base = self.opd_atm
+        N.call('oopao_dm_opd_acc_f32', dm._modes_t, self.coefs, dm.nValidAct, self.res * self.res, 1, 1.0, base,
+               self.opd, st)
+        N.call('oopao_cl_pupil_rms', self.opd, self.pupil_idx, self.pupil_idx.numel(), self.step_counter,
+               self.wfe, self.max_steps, st)
+        N.call('oopao_pwfs_measure', self.plan.h, self.opd, self.scale, 1, self.frame, None, self.ws,
+               self.ws_bytes, st)
+        N.call('oopao_pwfs_signal', self.plan.h, self.frame, 1, self.s2d, self.s, None, st)
+        if self.frame_delay == 1:
+            N.call('oopao_cl_integrate', self.R, self.s, self.R.shape[0], self.R.shape[1], self.gain, self.coefs,
+                   self.step_counter, st)
+        else:
+            N.call('oopao_cl_integrate', self.R, self.s_prev, self.R.shape[0], self.R.shape[1], self.gain,
+                   self.coefs, self.step_counter, st)
+            self.s_prev.copy_(self.s)
+
+    def step(self):
+        """One eager step (no graph)."""
+        self._launch_step()
+
+    def capture(self):
+        """Capture one step in a CUDA graph (after eager warm-up steps)."""
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            for _ in range(2):
+                self._launch_step()
+        torch.cuda.current_stream().wait_stream(s)
+        self.reset()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self._launch_step()
+        self.graph = g
+        self.reset()
+        torch.cuda.synchronize()
+        return g
+
+    def run(self, n_steps, graph=True):
+        """Run n steps (graph replay when captured)."""
+        if graph and self.graph is None:
+            self.capture()
+        for _ in range(n_steps):
+            if graph:
+                self.graph.replay()
+            else:
+                self._launch_step()
+
+    @property
+    def residual_wfe(self):
+        """Residual RMS OPD over the pupil per step so far (m), host copy."""
+        n = int(self.step_counter.item())
+        return self.wfe[:n].double().cpu().numpy()

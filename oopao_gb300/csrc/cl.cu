@@ -1,0 +1,141 @@
+// Closed-loop step kernels (tutorials/AO_closed_loop_Pyramid_WFS.py:601-639,
+// OOPAO/closed_loop/run_cl.py:176-217): turbulence OPD of the step, DM shape
+// added to it, reconstructor MVM + integrator, residual wavefront RMS.
+//
+// A device step counter drives the time index, so a CUDA graph capturing one
+// step replays every later step without host involvement: the screen kernel
+// reads the counter, the integrator kernel advances it.
+#include "common.cuh"
+
+namespace {
+
+struct ScreenLayer {
+  const float* screen;  // [h][w] OPD (m), periodic
+  int h, w;
+  float y0, x0;         // position of pupil pixel (0,0) at step 0 (pixels)
+  float vy, vx;         // displacement per step (pixels)
+};
+
+constexpr int kMaxLayers = 35;
+
+struct ScreenArgs {
+  ScreenLayer layer[kMaxLayers];
+  int n_layers, res;
+  const int* step;
+  float* opd;  // [res][res]
+};
+
+__device__ __forceinline__ int wrap(int i, int n) {
+  i %= n;
+  return i < 0 ? i + n : i;
+}
+
+// Frozen flow: each layer is translated by (vy, vx) pixels per step and
+// sampled bilinearly (periodic screens); layers are summed.
+__global__ void cl_screen(ScreenArgs a) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.res * a.res) return;
+  const int i = p / a.res, j = p - (p / a.res) * a.res;
+  const float t = (float)(*a.step);
+  float s = 0.f;
+  for (int q = 0; q < a.n_layers; q++) {
+    const ScreenLayer& L = a.layer[q];
+    const float y = L.y0 + i + L.vy * t, x = L.x0 + j + L.vx * t;
+    const float fy = floorf(y), fx = floorf(x);
+    const float dy = y - fy, dx = x - fx;
+    const int y0 = wrap((int)fy, L.h), x0 = wrap((int)fx, L.w);
+    const int y1 = wrap(y0 + 1, L.h), x1 = wrap(x0 + 1, L.w);
+    const float v00 = L.screen[(size_t)y0 * L.w + x0], v01 = L.screen[(size_t)y0 * L.w + x1];
+    const float v10 = L.screen[(size_t)y1 * L.w + x0], v11 = L.screen[(size_t)y1 * L.w + x1];
+    s += (1.f - dy) * ((1.f - dx) * v00 + dx * v01) + dy * ((1.f - dx) * v10 + dx * v11);
+  }
+  a.opd[p] = s;
+}
+
+// coefs[a] -= gain * sum_j R[a][j] s[j]  (one warp per actuator); block 0
+// thread 0 advances the step counter.
+__global__ void cl_integrate(const float* __restrict__ R, const float* __restrict__ s, int n_act, int n_sig,
+                             float gain, float* __restrict__ coefs, int* step) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp < n_act) {
+    const float* r = R + (size_t)warp * n_sig;
+    float acc = 0.f;
+    for (int j = lane; j < n_sig; j += 32) acc = fmaf(r[j], s[j], acc);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) coefs[warp] -= gain * acc;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && step) *step += 1;
+}
+
+// RMS of (opd - mean) over the pupil pixels idx[0..npup) -> out[*step].
+__global__ void cl_pupil_rms(const float* __restrict__ opd, const int* __restrict__ idx, int npup,
+                             const int* step, float* out, int out_len) {
+  __shared__ double red[2][32];
+  double s = 0.0, s2 = 0.0;
+  for (int i = threadIdx.x; i < npup; i += blockDim.x) {
+    const double v = opd[idx[i]];
+    s += v;
+    s2 += v * v;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_xor_sync(0xffffffffu, s, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    red[0][w] = s;
+    red[1][w] = s2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+      a += red[0][i];
+      b += red[1][i];
+    }
+    const double m = a / npup;
+    const int t = step ? *step : 0;
+    if (t >= 0 && t < out_len) out[t] = (float)sqrt(fmax(b / npup - m * m, 0.0));
+  }
+}
+
+}  // namespace
+
+extern "C" int oopao_cl_screen(int n_layers, const float* const* screens, const int* heights, const int* widths,
+                               const float* y0, const float* x0, const float* vy, const float* vx, int res,
+                               const int* step, float* opd, void* stream) {
+  OOPAO_CHECK_ARG(n_layers >= 1 && n_layers <= kMaxLayers, "1 to 35 layers");
+  OOPAO_CHECK_ARG(screens && heights && widths && y0 && x0 && vy && vx && step && opd, "NULL argument");
+  ScreenArgs a;
+  a.n_layers = n_layers;
+  a.res = res;
+  a.step = step;
+  a.opd = opd;
+  for (int q = 0; q < n_layers; q++) {
+    OOPAO_CHECK_ARG(screens[q] && heights[q] > 1 && widths[q] > 1, "bad layer");
+    a.layer[q] = ScreenLayer{screens[q], heights[q], widths[q], y0[q], x0[q], vy[q], vx[q]};
+  }
+  cl_screen<<<ceil_div(res * res, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  oopao_count_launches(1);
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_cl_integrate(const float* R, const float* s, int n_act, int n_sig, float gain, float* coefs,
+                                  int* step, void* stream) {
+  OOPAO_CHECK_ARG(R && s && coefs, "NULL argument");
+  OOPAO_CHECK_ARG(n_act > 0 && n_sig > 0, "sizes must be positive");
+  cl_integrate<<<ceil_div(n_act * 32, 256), 256, 0, (cudaStream_t)stream>>>(R, s, n_act, n_sig, gain, coefs, step);
+  oopao_count_launches(1);
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_cl_pupil_rms(const float* opd, const int* idx, int npup, const int* step, float* out,
+                                  int out_len, void* stream) {
+  OOPAO_CHECK_ARG(opd && idx && out && npup > 0, "bad argument");
+  cl_pupil_rms<<<1, 1024, 0, (cudaStream_t)stream>>>(opd, idx, npup, step, out, out_len);
+  oopao_count_launches(1);
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}

@@ -20,7 +20,8 @@ template <int NB>
 __global__ void __launch_bounds__(kGemvThreads) dm_gemv(const float* __restrict__ modes_t,
                                                         const float* __restrict__ coefs, int n_act,
                                                         int n_pix, int batch, float scale,
-                                                        float* __restrict__ opd) {
+                                                        float* __restrict__ opd,
+                                                        const float* __restrict__ base) {
   __shared__ float cs[kGemvChunk * NB];
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   float acc[NB];
@@ -46,7 +47,7 @@ __global__ void __launch_bounds__(kGemvThreads) dm_gemv(const float* __restrict_
   if (p < n_pix) {
 #pragma unroll
     for (int b = 0; b < NB; b++)
-      if (b < batch) opd[(size_t)b * n_pix + p] = acc[b] * scale;
+      if (b < batch) opd[(size_t)b * n_pix + p] = acc[b] * scale + (base ? base[(size_t)b * n_pix + p] : 0.f);
   }
 }
 
@@ -54,7 +55,8 @@ constexpr int BM = 64, BN = 64, BK = 16;
 
 __global__ void __launch_bounds__(256) dm_gemm(const float* __restrict__ modes_t,
                                                const float* __restrict__ coefs, int n_act, int n_pix,
-                                               int batch, float scale, float* __restrict__ opd) {
+                                               int batch, float scale, float* __restrict__ opd,
+                                               const float* __restrict__ base) {
   __shared__ float As[BK][BM];  // coefs[a][b]
   __shared__ float Bs[BK][BN];  // modes_t[a][p]
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
@@ -93,7 +95,8 @@ __global__ void __launch_bounds__(256) dm_gemm(const float* __restrict__ modes_t
 #pragma unroll
     for (int j = 0; j < 4; j++) {
       const int p = p0 + tx * 4 + j;
-      if (p < n_pix) opd[(size_t)b * n_pix + p] = acc[i][j] * scale;
+      if (p < n_pix)
+        opd[(size_t)b * n_pix + p] = acc[i][j] * scale + (base ? base[(size_t)b * n_pix + p] : 0.f);
     }
   }
 }
@@ -146,23 +149,28 @@ extern "C" int oopao_dm_vjp_f32(const float* modes_t, const float* g, int n_act,
   return OOPAO_OK;
 }
 
-extern "C" int oopao_dm_opd_f32(const float* modes_t, const float* coefs, int n_act, int n_pix,
-                                int batch, float scale, float* opd, void* stream) {
+extern "C" int oopao_dm_opd_acc_f32(const float* modes_t, const float* coefs, int n_act, int n_pix, int batch,
+                                    float scale, const float* base, float* opd, void* stream) {
   OOPAO_CHECK_ARG(modes_t && coefs && opd, "NULL argument");
   OOPAO_CHECK_ARG(n_act > 0 && n_pix > 0 && batch > 0, "sizes must be positive");
   cudaStream_t st = (cudaStream_t)stream;
   const int g = ceil_div(n_pix, kGemvThreads);
   if (batch == 1) {
-    dm_gemv<1><<<g, kGemvThreads, 0, st>>>(modes_t, coefs, n_act, n_pix, batch, scale, opd);
+    dm_gemv<1><<<g, kGemvThreads, 0, st>>>(modes_t, coefs, n_act, n_pix, batch, scale, opd, base);
   } else if (batch <= 4) {
-    dm_gemv<4><<<g, kGemvThreads, 0, st>>>(modes_t, coefs, n_act, n_pix, batch, scale, opd);
+    dm_gemv<4><<<g, kGemvThreads, 0, st>>>(modes_t, coefs, n_act, n_pix, batch, scale, opd, base);
   } else if (batch <= 8) {
-    dm_gemv<8><<<g, kGemvThreads, 0, st>>>(modes_t, coefs, n_act, n_pix, batch, scale, opd);
+    dm_gemv<8><<<g, kGemvThreads, 0, st>>>(modes_t, coefs, n_act, n_pix, batch, scale, opd, base);
   } else {
     dim3 grid(ceil_div(n_pix, BN), ceil_div(batch, BM));
-    dm_gemm<<<grid, 256, 0, st>>>(modes_t, coefs, n_act, n_pix, batch, scale, opd);
+    dm_gemm<<<grid, 256, 0, st>>>(modes_t, coefs, n_act, n_pix, batch, scale, opd, base);
   }
   oopao_count_launches(1);
   OOPAO_CUDA_TRY(cudaGetLastError());
   return OOPAO_OK;
+}
+
+extern "C" int oopao_dm_opd_f32(const float* modes_t, const float* coefs, int n_act, int n_pix,
+                                int batch, float scale, float* opd, void* stream) {
+  return oopao_dm_opd_acc_f32(modes_t, coefs, n_act, n_pix, batch, scale, nullptr, opd, stream);
 }

@@ -257,28 +257,49 @@ __global__ void __launch_bounds__(kThreads) pwfs_rows_inv(RowsInvArgs a) {
 namespace {
 // Compile-time plans (N = R1*R2, T threads per line, lines per CTA of the
 // three passes).  Sizes without an entry use the generic kernels.
-const FastPasses* fast_passes(int n) {
-  // row-inverse lines per CTA are a multiple of the usual N/cam so the
-  // detector binning fuses into that pass (6 for the default geometry)
-  static const FastPasses f72 = make_fast<72, 8, 9, 9, 16, 16, 12>();
-  static const FastPasses f96 = make_fast<96, 8, 12, 12, 16, 16, 12>();
-  static const FastPasses f112 = make_fast<112, 16, 7, 8, 16, 16, 16>();
-  static const FastPasses f128 = make_fast<128, 16, 8, 8, 16, 16, 16>();
-  static const FastPasses f240 = make_fast<240, 16, 15, 16, 16, 16, 12>();
-  static const FastPasses f264 = make_fast<264, 24, 11, 12, 16, 16, 12>();
-  static const FastPasses f480 = make_fast<480, 24, 20, 12, 16, 8, 12>();
-  static const FastPasses f504 = make_fast<504, 24, 21, 12, 16, 8, 12>();
+// Candidates per N (the autotuner picks one per plan).  Row-inverse lines per
+// CTA are a multiple of the usual N/cam so the detector binning fuses into
+// that pass (6 for the default geometry).
+int fast_candidates(int n, const FastPasses** out) {
+  static const FastPasses f72[] = {make_fast<72, 8, 9, 9, 16, 16, 12>()};
+  static const FastPasses f96[] = {make_fast<96, 8, 12, 12, 16, 16, 12>()};
+  static const FastPasses f112[] = {make_fast<112, 16, 7, 8, 16, 16, 16>()};
+  static const FastPasses f128[] = {make_fast<128, 16, 8, 8, 16, 16, 16>()};
+  static const FastPasses f240[] = {make_fast<240, 16, 15, 16, 16, 16, 12>()};
+  static const FastPasses f264[] = {make_fast<264, 24, 11, 12, 16, 16, 12>(),
+                                    make_fast<264, 24, 11, 24, 8, 8, 12>(),
+                                    make_fast<264, 11, 24, 12, 16, 16, 12>()};
+  static const FastPasses f480[] = {make_fast<480, 24, 20, 12, 16, 8, 12>()};
+  static const FastPasses f504[] = {make_fast<504, 24, 21, 12, 16, 8, 12>(),
+                                    make_fast<504, 24, 21, 24, 8, 8, 12>(),
+                                    make_fast<504, 21, 24, 12, 16, 8, 12>(),
+                                    make_fast<504, 24, 21, 24, 8, 16, 6>()};
+#define OOPAO_CANDS(arr) (*out = arr, (int)(sizeof(arr) / sizeof(arr[0])))
   switch (n) {
-    case 72: return &f72;
-    case 96: return &f96;
-    case 112: return &f112;
-    case 128: return &f128;
-    case 240: return &f240;
-    case 264: return &f264;
-    case 480: return &f480;
-    case 504: return &f504;
-    default: return nullptr;
+    case 72: return OOPAO_CANDS(f72);
+    case 96: return OOPAO_CANDS(f96);
+    case 112: return OOPAO_CANDS(f112);
+    case 128: return OOPAO_CANDS(f128);
+    case 240: return OOPAO_CANDS(f240);
+    case 264: return OOPAO_CANDS(f264);
+    case 480: return OOPAO_CANDS(f480);
+    case 504: return OOPAO_CANDS(f504);
+    default: *out = nullptr; return 0;
   }
+#undef OOPAO_CANDS
+}
+
+const FastPasses* fast_passes(int n, int idx = 0) {
+  const FastPasses* c = nullptr;
+  const int cnt = fast_candidates(n, &c);
+  return (idx >= 0 && idx < cnt) ? c + idx : nullptr;
+}
+
+cudaError_t fast_attrs(const FastPasses* f) {
+  cudaError_t e = cudaFuncSetAttribute(f->rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->smem_rows);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(f->cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->smem_cols);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(f->inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->smem_inv);
+  return e;
 }
 }  // namespace
 
@@ -565,15 +586,9 @@ extern "C" int oopao_pwfs_plan_create(oopao_pwfs_plan** out, int res, int n, int
   cudaError_t e = cudaFuncSetAttribute(pwfs_rows_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(pwfs_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(pwfs_rows_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
-  p->fast = fast_passes(n);
+  p->fast = fast_passes(n, 0);
   p->variant = p->fast ? 1 : 0;
-  if (p->fast && e == cudaSuccess) {
-    e = cudaFuncSetAttribute(p->fast->rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->fast->smem_rows);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(p->fast->cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->fast->smem_cols);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(p->fast->inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->fast->smem_inv);
-  }
+  if (p->fast && e == cudaSuccess) e = fast_attrs(p->fast);
   if (e != cudaSuccess) {
     oopao_set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
     free_plan(p);
@@ -652,7 +667,7 @@ struct PassPlan {
 
 PassPlan plan_passes(const oopao_pwfs_plan* p, int batch, bool want_raw, size_t units) {
   PassPlan pp;
-  const FastPasses* f = (p->variant == 1) ? p->fast : nullptr;
+  const FastPasses* f = (p->variant >= 1) ? p->fast : nullptr;
   pp.fast = f != nullptr;
   pp.fused = pp.fast && !want_raw && (f->l_inv % p->bin == 0);
   const int k = p->k;
@@ -1108,7 +1123,7 @@ const AdPasses* ad_passes(int n) {
 
 int ad_setup(const oopao_pwfs_plan* p, const AdPasses** out) {
   const AdPasses* a = ad_passes(p->n);
-  if (!a || !p->fast || p->variant != 1) {
+  if (!a || !p->fast || p->variant < 1) {
     oopao_set_last_error("tangent/adjoint passes exist for n_fft in {72,112,128,264,504} only", __FILE__, __LINE__);
     return OOPAO_ERR_UNSUPPORTED;
   }
@@ -1310,12 +1325,36 @@ extern "C" int oopao_pwfs_vjp(const oopao_pwfs_plan* p, const float* opd, const 
 
 extern "C" int oopao_pwfs_set_variant(oopao_pwfs_plan* p, int variant) {
   OOPAO_CHECK_ARG(p, "NULL plan");
-  OOPAO_CHECK_ARG(variant == 0 || variant == 1, "variant must be 0 (generic) or 1 (compile-time plan)");
-  if (variant == 1 && !p->fast) {
-    oopao_set_last_error("no compile-time plan for this FFT size", __FILE__, __LINE__);
+  const FastPasses* c = nullptr;
+  const int cnt = fast_candidates(p->n, &c);
+  OOPAO_CHECK_ARG(variant >= 0, "variant must be 0 (generic) or a compile-time plan index >= 1");
+  if (variant > cnt) {
+    oopao_set_last_error("no such compile-time plan for this FFT size", __FILE__, __LINE__);
     return OOPAO_ERR_UNSUPPORTED;
   }
+  if (variant >= 1) {
+    const FastPasses* f = c + (variant - 1);
+    OOPAO_CUDA_TRY(fast_attrs(f));
+    p->fast = f;
+  }
   p->variant = variant;
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_pwfs_num_variants(const oopao_pwfs_plan* p) {
+  if (!p) return -1;
+  const FastPasses* c = nullptr;
+  return fast_candidates(p->n, &c);
+}
+
+extern "C" int oopao_pwfs_variant_info(const oopao_pwfs_plan* p, int variant, int* info) {
+  OOPAO_CHECK_ARG(p && info, "NULL argument");
+  const FastPasses* c = nullptr;
+  const int cnt = fast_candidates(p->n, &c);
+  OOPAO_CHECK_ARG(variant >= 1 && variant <= cnt, "no such compile-time plan");
+  const FastPasses* f = c + (variant - 1);
+  info[0] = f->r1; info[1] = f->r2; info[2] = f->t;
+  info[3] = f->l_rows; info[4] = f->l_cols; info[5] = f->l_inv;
   return OOPAO_OK;
 }
 

@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(T* L) pwfs_rows_inv2(RowsInvArgs a) {
 
 // ---- registry ----
 struct FastPasses {
-  int n, t, l_rows, l_cols, l_inv;
+  int n, r1, r2, t, l_rows, l_cols, l_inv;
   void (*rows)(RowsFwdArgs);
   void (*cols)(ColsArgs);
   void (*inv)(RowsInvArgs);
@@ -303,7 +303,7 @@ FastPasses make_fast() {
   constexpr int LSC = odd_up(imax(R2 * R1P, R1 * R2P));
   constexpr int LSI = xchg_stride(R1 * R2P, T, LI, R2P, R1, R2);
   FastPasses f;
-  f.n = N; f.t = T; f.l_rows = LR; f.l_cols = LC; f.l_inv = LI;
+  f.n = N; f.r1 = R1; f.r2 = R2; f.t = T; f.l_rows = LR; f.l_cols = LC; f.l_inv = LI;
   f.rows = pwfs_rows_fwd2<N, R1, R2, T, LR>;
   f.cols = pwfs_cols2<N, R1, R2, T, LC>;
   f.inv = pwfs_rows_inv2<N, R1, R2, T, LI>;

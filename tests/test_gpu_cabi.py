@@ -87,12 +87,21 @@ def test_variants_agree(lib, n, res, cam):
     h = make_plan(N, res, n, cam, mask, path, amp=amp)
     try:
         assert N.load().oopao_pwfs_get_variant(h) == 1
+        nv = N.load().oopao_pwfs_num_variants(h)
+        assert nv >= 1
         phase = rng.standard_normal((2, res, res))
-        f1, r1 = measure(N, h, phase, n, cam)
         N.call('oopao_pwfs_set_variant', h, 0)
         f0, r0 = measure(N, h, phase, n, cam)
-        assert O.rel_l2(r1, r0) < 2e-6
-        assert O.rel_l2(f1, f0) < 2e-6
+        f0b, _ = measure(N, h, phase, n, cam, want_raw=False)
+        for v in range(1, nv + 1):
+            N.call('oopao_pwfs_set_variant', h, v)
+            f1, r1 = measure(N, h, phase, n, cam)
+            assert O.rel_l2(r1, r0) < 2e-6, v
+            assert O.rel_l2(f1, f0) < 2e-6, v
+            # binned path (no raw_data requested) agrees as well
+            f1b, _ = measure(N, h, phase, n, cam, want_raw=False)
+            assert O.rel_l2(f1b, f0b) < 2e-6, v
+        assert N.load().oopao_pwfs_set_variant(h, nv + 1) == 2
     finally:
         N.load().oopao_pwfs_plan_destroy(h)
 
@@ -190,7 +199,8 @@ def test_invalid_arguments_are_rejected(lib):
     try:
         st = N.load().oopao_pwfs_measure(h, None, 1.0, 1, None, None, None, 0, None)
         assert st == 1
-        assert N.load().oopao_pwfs_set_variant(h, 7) == 1
+        assert N.load().oopao_pwfs_set_variant(h, -1) == 1
+        assert N.load().oopao_pwfs_set_variant(h, 7) == 2
         # workspace smaller than one item
         import torch
         x = torch.zeros((1, 24, 24), device='cuda')
