@@ -70,21 +70,99 @@ def kl_like_basis(modes, pupil, n_modes, diameter=8.0, r0=0.15, L0=25.0):
     cov[r < 1e-9] = c * gamma(5 / 6) / 2 ** (1 / 6)
     ev, vec = np.linalg.eigh(cov)
     vec = vec[:, np.argsort(ev)[::-1][:n_modes]]
-    opd = w @ vec
-    vec = vec / opd.std(axis=0)[None]
+    # RMS over the pupil of w @ vec from the Gram matrix (no per-mode OPD maps)
+    npup = w.shape[0]
+    gram = w.T @ w
+    mean = (w.sum(axis=0) @ vec) / npup
+    msq = np.einsum('ij,ij->j', vec, gram @ vec) / npup
+    vec = vec / np.sqrt(np.maximum(msq - mean ** 2, 1e-300))[None]
     return np.ascontiguousarray(vec)
 
 
-def build_system(dev_index):
+def build_system(dev_index, res=RES, nsub=NSUB, mod=MOD, ntheta=NTHETA, max_batch=100):
     import oopao_gb300 as og
     with _quiet():
-        tel = og.Telescope(resolution=RES, diameter=8.0, samplingTime=1e-3)
+        tel = og.Telescope(resolution=res, diameter=8.0, samplingTime=1e-3)
         ngs = og.Source(optBand='V0', magnitude=8)
         ngs * tel
-        dm = og.DeformableMirror(tel, nSubap=NSUB, mechCoupling=0.35)
-        wfs = og.Pyramid(nSubap=NSUB, telescope=tel, modulation=MOD, lightRatio=0.5,
-                         nTheta_user_defined=NTHETA, max_batch=100)
+        dm = og.DeformableMirror(tel, nSubap=nsub, mechCoupling=0.35)
+        wfs = og.Pyramid(nSubap=nsub, telescope=tel, modulation=mod, lightRatio=0.5,
+                         nTheta_user_defined=ntheta, max_batch=max_batch)
     return tel, ngs, dm, wfs
+
+
+def _timed(fn):
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = fn()
+    torch.cuda.synchronize()
+    return out, time.perf_counter() - t0
+
+
+def im_comparison(tel, ngs, dm, wfs, m2c, n_per_mode, with_error=True):
+    """Interaction-matrix build times of one system: the plain per-mode
+    push-pull GPU path (operator path ngs**tel*dm*wfs per mode, timed on
+    `n_per_mode` modes and scaled to all), the batched push-pull path and
+    the batched tangent (JVP) path; JVP error against a float64 derivative."""
+    from oopao_gb300.calibration import InteractionMatrix
+    from oopao_gb300.autodiff import jvp_interaction_matrix
+    n_modes = m2c.shape[1]
+    InteractionMatrix(ngs, tel, dm, wfs, m2c[:, :2], STROKE, single_pass=False, method='per_mode', invert=False)
+    _, t_pm = _timed(lambda: InteractionMatrix(ngs, tel, dm, wfs, m2c[:, :n_per_mode], STROKE, single_pass=False,
+                                               method='per_mode', invert=False))
+    InteractionMatrix(ngs, tel, dm, wfs, m2c[:, :8], STROKE, single_pass=False, method='batched', invert=False)
+    _, t_b = _timed(lambda: InteractionMatrix(ngs, tel, dm, wfs, m2c, STROKE, single_pass=False,
+                                              method='batched', invert=False))
+    jvp_interaction_matrix(ngs, tel, dm, wfs, m2c[:, :8])
+    D, t_j = _timed(lambda: jvp_interaction_matrix(ngs, tel, dm, wfs, m2c))
+    out = {'modes': n_modes, 'per_mode_push_pull_ms': t_pm / n_per_mode * n_modes * 1000.0,
+           'per_mode_timed_modes': n_per_mode, 'batched_push_pull_ms': t_b * 1000.0, 'jvp_ms': t_j * 1000.0}
+    out['jvp_speedup_vs_per_mode_push_pull'] = out['per_mode_push_pull_ms'] / out['jvp_ms']
+    out['batched_speedup_vs_per_mode_push_pull'] = out['per_mode_push_pull_ms'] / out['batched_push_pull_ms']
+    if with_error:
+        from oracle import pwfs_oracle as O
+        res, nsub = tel.resolution, dm.nActAlongDiameter
+        inten = O.source_intensity(O.telescope_pupil(res), O.n_photon('V0', 8), 1e-3, 8.0)
+        ow = O.build_pyramid(res, nsub, wfs.modulation, 0.5, inten, n_theta_user=wfs.nTheta,
+                             workers=os.cpu_count())
+        Dref = O.interaction_matrix(ow, O.dm_modes(res, 8.0, nsub), m2c[:, :2], 1e-12, ngs.wavelength,
+                                    O.telescope_pupil(res), single_pass=False, workers=os.cpu_count())
+        out['jvp_rel_fro_err_vs_fp64_2cols'] = O.rel_l2(D[:, :2].double().cpu().numpy(), Dref)
+    return out
+
+
+def cl_rate(n_steps=2000):
+    """Graph-replayed closed-loop steps/s on the 40x40 configuration: 240 px,
+    N=504, modulation 5 l/D x 96 points, 41x41 DM, 3 frozen-flow layers
+    (r0 0.12 m, L0 30 m, 10/15/20 m/s), gain 0.4, delay 1."""
+    import torch
+    from oopao_gb300.closed_loop import ClosedLoop, VonKarmanLayers
+    from oopao_gb300 import autotune
+    tel, ngs, dm, wfs = build_system(0, 240, 40, 5, 96, max_batch=16)
+    autotune.tune_pyramid(wfs, batch=1)
+    layers = VonKarmanLayers(tel, r0=0.12, L0=30, fractionalR0=(1 / 3, 1 / 3, 1 / 3), windSpeed=(10., 15., 20.),
+                             windDirection=(0., 72., 144.), seed=0)
+    R = np.zeros((dm.nValidAct, wfs.nSignal), np.float32)
+    cl = ClosedLoop(tel, ngs, dm, wfs, R, gain=0.4, layers=layers, max_steps=n_steps + 10)
+    cl.capture()
+    cl.run(20)
+    torch.cuda.synchronize()
+    cl.reset()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    cl.run(n_steps)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / n_steps
+    return {'config': '40x40 PWFS, 240 px, N=504, 96 points, 41x41 DM (%d act), 3 layers' % dm.nValidAct,
+            'steps': n_steps, 'us_per_step': ms * 1000.0, 'khz': 1.0 / ms,
+            'graph': True, 'variant': int(N_variant(wfs))}
+
+
+def N_variant(wfs):
+    from oopao_gb300 import _native as N
+    return N.load().oopao_pwfs_get_variant(wfs.plan.h)
 
 
 class ClockSampler:
@@ -269,6 +347,8 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
+    from oopao_gb300 import autotune
+    tune = autotune.tune_pyramid(wfs, batch=wfs.max_batch)
     for _ in range(args.warmup):
         device_step()
     barrier()
@@ -351,6 +431,16 @@ def run_ours(args):
                                     workers=os.cpu_count())
         err = O.rel_l2(D[:, :2].double().cpu().numpy(), Dref)
 
+    extra = {}
+    if rank == 0 and world == 1 and not args.no_extra:
+        extra['im_c1_300'] = im_comparison(tel, ngs, dm, wfs, m2c, n_per_mode=30)
+        tel3, ngs3, dm3, wfs3 = build_system(0, 240, 40, 5, 96, max_batch=16)
+        autotune.tune_pyramid(wfs3, batch=16)
+        m2c3 = kl_like_basis(dm3.modes, tel3.pupil, 1000)
+        extra['im_c3_1000'] = im_comparison(tel3, ngs3, dm3, wfs3, m2c3, n_per_mode=10)
+        del tel3, ngs3, dm3, wfs3
+        extra['cl_step'] = cl_rate()
+
     if rank == 0:
         line = {
             'metric': 'PWFS frames/s (batched IM build)', 'value': value, 'unit': 'frames/s',
@@ -370,7 +460,9 @@ def run_ours(args):
             'gpu_launches': int(launches),
             'clocks': clocks,
             'cpu_baseline': cpu,
+            'autotune': {'variant': tune['variant'], 'ms_per_variant': tune['ms']},
         }
+        line.update(extra)
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
@@ -383,6 +475,8 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline and accuracy legs')
+    ap.add_argument('--no-extra', action='store_true',
+                    help='skip the interaction-matrix comparisons and the closed-loop rate')
     args = ap.parse_args()
     if args.impl == 'reference':
         run_reference(args)
