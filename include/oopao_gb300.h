@@ -168,6 +168,19 @@ int oopao_pwfs_signal(const oopao_pwfs_plan* plan, const float* frame, int batch
  * ------------------------------------------------------------------------ */
 int oopao_dm_opd_f32(const float* modes_t, const float* coefs, int n_act, int n_pix, int batch,
                      float scale, float* opd, void* stream);
+/* BF16 tensor-core projection (tcgen05 MMA, TMA-fed tiles, FP32
+ * accumulation), same result layout as oopao_dm_opd_f32 (plus an optional
+ * base).  modes: device [n_pix][n_act_pad] BF16 (K-major, zero padded,
+ * n_act_pad a multiple of 64), built once by oopao_dm_modes_bf16 from the
+ * FP32 modes_t.  workspace: device, 256-byte aligned,
+ * oopao_dm_bf16_workspace_bytes(n_act_pad, batch) bytes; its first int
+ * holds 0 after the call, or the code of a pipeline wait that timed out. */
+int oopao_dm_modes_bf16(const float* modes_t, int n_act, int n_pix, int n_act_pad, void* modes_out, void* stream);
+size_t oopao_dm_bf16_workspace_bytes(int n_act_pad, int batch);
+int oopao_dm_opd_bf16(const void* modes, int n_act_pad, const float* coefs, int n_act, int n_pix, int batch,
+                      float scale, const float* base, float* opd, void* workspace, size_t workspace_bytes,
+                      void* stream);
+
 /* opd = (modes @ coefs)^T * scale + base: the DM shape added to an incoming
  * OPD in one pass (DeformableMirror.relay, OOPAO/DeformableMirror.py:441-447:
  * src.OPD_no_pupil += dm.OPD).  base: device [batch][n_pix] or NULL. */

@@ -1,0 +1,338 @@
+// BF16 tensor-core influence-function projection on sm_103a (tcgen05 + TMA).
+//
+// opd[b][p] = scale * sum_a modes[p][a] * coefs[a][b] (+ base[b][p])
+// (dm.coefs setter, OOPAO/DeformableMirror.py:651-686), as a GEMM
+//   D[M = pixels][N = batch] = A[M][K = actuators] * B[N][K]^T
+// with A = the IF matrix in BF16, K-major ([n_pix][n_act_pad]), B = the
+// coefficients transposed to BF16 K-major ([batch_pad][n_act_pad]).
+//
+// One CTA computes a 128 x BN tile: a TMA producer thread streams 128x64 A
+// and BNx64 B tiles (128-byte swizzle) through a 4-stage mbarrier ring, one
+// thread issues tcgen05.mma (kind::f16, M=128, N=BN, K=16) into a TMEM
+// accumulator, and the four warps read the accumulator back with
+// tcgen05.ld (32 lanes x 16 columns per load) and store FP32, coalesced
+// along pixels.  Every mbarrier wait is bounded: on time-out the CTA records
+// a code in the error word, stops issuing work and still frees its TMEM.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
+#include <mutex>
+
+#include "common.cuh"
+
+namespace {
+
+constexpr int kBM = 128;     // pixels per tile = TMEM lanes
+constexpr int kBK = 64;      // actuators per stage: one 128-byte swizzle row of BF16
+constexpr int kUK = 16;      // K of one tcgen05.mma kind::f16
+constexpr int kStages = 4;
+constexpr int kThreads = 128;
+constexpr long long kWaitCycles = 1ll << 31;  // ~1 s at 2 GHz
+
+struct TcParams {
+  int n_pix, batch;
+  int nk;  // K tiles
+  float scale;
+  const float* base;
+  float* out;
+  int* err;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred P1;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
+      "selp.b32 %0, 1, 0, P1;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: false (and an error code) after ~1 s.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (clock64() - t0 > kWaitCycles) {
+      atomicExch(err, code);
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (stride byte offset), descriptor version 1.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;             // leading byte offset (16 B; unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
+  d |= (uint64_t)1 << 46;             // version
+  d |= (uint64_t)2 << 61;             // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor, kind::f16: F32 accumulator, BF16 A and B, both
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t make_idesc(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+      ::"r"(tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+template <int BN>
+constexpr size_t tc_smem_bytes() {
+  return 1024 + (size_t)kStages * (kBM + BN) * kBK * 2 + 256;
+}
+
+template <int BN>
+__global__ void __launch_bounds__(kThreads, 1)
+    dm_tc_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_b, TcParams p) {
+  constexpr int A_BYTES = kBM * kBK * 2;
+  constexpr int B_BYTES = BN * kBK * 2;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* sa = smem;
+  unsigned char* sb = smem + kStages * A_BYTES;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sb + kStages * B_BYTES);
+  uint64_t* empty = full + kStages;
+  uint64_t* done = empty + kStages;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"((uint32_t)BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // TMA producer
+    for (int kb = 0; kb < p.nk; kb++) {
+      const int s = kb % kStages;
+      if (!mbar_wait(&empty[s], ((kb / kStages) & 1) ^ 1, p.err, 1)) break;
+      mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
+      tma_load_2d(sa + s * A_BYTES, &tma_a, &full[s], kb * kBK, m0);
+      tma_load_2d(sb + s * B_BYTES, &tma_b, &full[s], kb * kBK, n0);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    constexpr uint32_t idesc = make_idesc(kBM, BN);
+    for (int kb = 0; kb < p.nk; kb++) {
+      const int s = kb % kStages;
+      if (!mbar_wait(&full[s], (kb / kStages) & 1, p.err, 2)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a0 = smem_u32(sa + s * A_BYTES), b0 = smem_u32(sb + s * B_BYTES);
+#pragma unroll
+      for (int k = 0; k < kBK / kUK; k++)
+        mma_bf16(tmem, sw128_desc(a0 + k * kUK * 2), sw128_desc(b0 + k * kUK * 2), idesc, (kb | k) ? 1u : 0u);
+      mma_commit(&empty[s]);
+    }
+    mma_commit(done);
+  }
+  __syncwarp();
+
+  // epilogue: warp w owns TMEM lanes (pixels) 32w .. 32w+31
+  const bool ok = mbar_wait(done, 0, p.err, 3);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (__all_sync(0xffffffffu, ok)) {
+    const int pix = m0 + warp * 32 + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+      uint32_t r[16];
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
+      if (pix < p.n_pix) {
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          const int b = n0 + c0 + j;
+          if (b < p.batch) {
+            const size_t o = (size_t)b * p.n_pix + pix;
+            p.out[o] = __uint_as_float(r[j]) * p.scale + (p.base ? p.base[o] : 0.f);
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)BN) : "memory");
+  }
+}
+
+// coefs [n_act][batch] f32 -> coefsT [batch_pad][n_act_pad] bf16, zero padded
+__global__ void dm_coefs_to_bf16(const float* __restrict__ coefs, int n_act, int batch, int n_act_pad,
+                                 int batch_pad, __nv_bfloat16* __restrict__ out) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)batch_pad * n_act_pad) return;
+  const int b = (int)(i / n_act_pad), a = (int)(i % n_act_pad);
+  out[i] = __float2bfloat16_rn((a < n_act && b < batch) ? coefs[(size_t)a * batch + b] : 0.f);
+}
+
+// modes_t [n_act][n_pix] f32 -> modes [n_pix][n_act_pad] bf16, zero padded
+__global__ void dm_modes_to_bf16(const float* __restrict__ modes_t, int n_act, int n_pix, int n_act_pad,
+                                 __nv_bfloat16* __restrict__ out) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)n_pix * n_act_pad) return;
+  const int p = (int)(i / n_act_pad), a = (int)(i % n_act_pad);
+  out[i] = __float2bfloat16_rn(a < n_act ? modes_t[(size_t)a * n_pix + p] : 0.f);
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* ptr = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+  });
+  return fn;
+}
+
+int encode_2d(CUtensorMap* map, const void* base, uint64_t inner, uint64_t rows, uint32_t box_inner,
+              uint32_t box_rows) {
+  PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+  if (!fn) {
+    oopao_set_last_error("cuTensorMapEncodeTiled is not available from the driver", __FILE__, __LINE__);
+    return OOPAO_ERR_CUDA;
+  }
+  const cuuint64_t dims[2] = {inner, rows};
+  const cuuint64_t strides[1] = {inner * 2};
+  const cuuint32_t box[2] = {box_inner, box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    oopao_set_last_error("cuTensorMapEncodeTiled rejected the tensor map", __FILE__, __LINE__);
+    return OOPAO_ERR_INVALID;
+  }
+  return OOPAO_OK;
+}
+
+template <int BN>
+int launch_tc(const void* modes, const void* coefs_t, int n_pix, int n_act_pad, int batch, int batch_pad,
+              float scale, const float* base, float* out, int* err, cudaStream_t st) {
+  CUtensorMap ta, tb;
+  int s = encode_2d(&ta, modes, (uint64_t)n_act_pad, (uint64_t)n_pix, kBK, kBM);
+  if (s) return s;
+  s = encode_2d(&tb, coefs_t, (uint64_t)n_act_pad, (uint64_t)batch_pad, kBK, BN);
+  if (s) return s;
+  const size_t smem = tc_smem_bytes<BN>();
+  OOPAO_CUDA_TRY(cudaFuncSetAttribute(dm_tc_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  TcParams p{n_pix, batch, n_act_pad / kBK, scale, base, out, err};
+  dim3 grid(ceil_div(n_pix, kBM), batch_pad / BN);
+  dm_tc_kernel<BN><<<grid, kThreads, smem, st>>>(ta, tb, p);
+  return OOPAO_OK;
+}
+
+}  // namespace
+
+extern "C" int oopao_dm_modes_bf16(const float* modes_t, int n_act, int n_pix, int n_act_pad, void* out,
+                                   void* stream) {
+  OOPAO_CHECK_ARG(modes_t && out, "NULL argument");
+  OOPAO_CHECK_ARG(n_act > 0 && n_pix > 0 && n_act_pad >= n_act && n_act_pad % kBK == 0,
+                  "n_act_pad must be a multiple of 64 and >= n_act");
+  const size_t total = (size_t)n_pix * n_act_pad;
+  dm_modes_to_bf16<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      modes_t, n_act, n_pix, n_act_pad, reinterpret_cast<__nv_bfloat16*>(out));
+  oopao_count_launches(1);
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}
+
+extern "C" size_t oopao_dm_bf16_workspace_bytes(int n_act_pad, int batch) {
+  if (n_act_pad <= 0 || batch <= 0) return 0;
+  const int bn = batch <= 64 ? 64 : 128;
+  const size_t batch_pad = (size_t)ceil_div(batch, bn) * bn;
+  return 256 + batch_pad * n_act_pad * 2;
+}
+
+extern "C" int oopao_dm_opd_bf16(const void* modes, int n_act_pad, const float* coefs, int n_act, int n_pix,
+                                 int batch, float scale, const float* base, float* opd, void* workspace,
+                                 size_t workspace_bytes, void* stream) {
+  OOPAO_CHECK_ARG(modes && coefs && opd && workspace, "NULL argument");
+  OOPAO_CHECK_ARG(n_act > 0 && n_pix > 0 && batch > 0, "sizes must be positive");
+  OOPAO_CHECK_ARG(n_act_pad >= n_act && n_act_pad % kBK == 0, "n_act_pad must be a multiple of 64 and >= n_act");
+  OOPAO_CHECK_ARG(((uintptr_t)modes & 15) == 0 && ((uintptr_t)workspace & 255) == 0,
+                  "modes must be 16-byte and the workspace 256-byte aligned");
+  OOPAO_CHECK_ARG(workspace_bytes >= oopao_dm_bf16_workspace_bytes(n_act_pad, batch), "workspace too small");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int bn = batch <= 64 ? 64 : 128;
+  const int batch_pad = ceil_div(batch, bn) * bn;
+  int* err = reinterpret_cast<int*>(workspace);
+  __nv_bfloat16* ct = reinterpret_cast<__nv_bfloat16*>((char*)workspace + 256);
+  OOPAO_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
+  const size_t total = (size_t)batch_pad * n_act_pad;
+  dm_coefs_to_bf16<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(coefs, n_act, batch, n_act_pad, batch_pad, ct);
+  const int s = bn == 64 ? launch_tc<64>(modes, ct, n_pix, n_act_pad, batch, batch_pad, scale, base, opd, err, st)
+                         : launch_tc<128>(modes, ct, n_pix, n_act_pad, batch, batch_pad, scale, base, opd, err, st);
+  if (s) return s;
+  oopao_count_launches(2);
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}

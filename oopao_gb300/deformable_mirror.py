@@ -140,20 +140,43 @@ class DeformableMirror:
         mt = np.ascontiguousarray(np.asarray(self.modes, dtype=np.float32).T)
         self._modes_t = torch.as_tensor(mt, device=self._dev)
         self._modes_bf16 = None
+        if self.if_dtype == 'bf16':
+            self._n_act_pad = (self.nValidAct + 63) // 64 * 64
+            npix = self.resolution ** 2
+            self._modes_bf16 = torch.empty((npix, self._n_act_pad), dtype=torch.bfloat16, device=self._dev)
+            N.call('oopao_dm_modes_bf16', self._modes_t, self.nValidAct, npix, self._n_act_pad, self._modes_bf16,
+                   N.stream_handle())
+            self._tc_ws = None
+        elif self.if_dtype != 'fp32':
+            raise OopaoError("if_dtype must be 'fp32' or 'bf16'")
 
     # ------------------------------------------------------------ projection
-    def opd_device(self, coefs_dev, scale=1.0, out=None):
+    def opd_device(self, coefs_dev, scale=1.0, out=None, base=None):
         """Device projection: coefs [n_act] or [n_act, B] float32 -> opd
-        [B, res, res] float32 (= (modes @ coefs)^T * scale)."""
+        [B, res, res] float32 (= (modes @ coefs)^T * scale [+ base]); FP32
+        CUDA-core path, or the BF16 tensor-core path for if_dtype='bf16'."""
         c = coefs_dev if coefs_dev.ndim == 2 else coefs_dev[:, None]
         c = c.contiguous()
         B = c.shape[1]
         res = self.resolution
         if out is None:
             out = torch.empty((B, res, res), dtype=torch.float32, device=self._dev)
-        N.call('oopao_dm_opd_f32', N.ptr(self._modes_t), N.ptr(c), self.nValidAct, res * res, B,
-               float(scale), N.ptr(out), N.stream_handle())
+        if self._modes_bf16 is not None:
+            nb = N.load().oopao_dm_bf16_workspace_bytes(self._n_act_pad, B)
+            if self._tc_ws is None or self._tc_ws.numel() < nb:
+                self._tc_ws = torch.empty(nb, dtype=torch.uint8, device=self._dev)
+            N.call('oopao_dm_opd_bf16', self._modes_bf16, self._n_act_pad, c, self.nValidAct, res * res, B,
+                   float(scale), base, out, self._tc_ws, nb, N.stream_handle())
+        else:
+            N.call('oopao_dm_opd_acc_f32', self._modes_t, c, self.nValidAct, res * res, B, float(scale), base, out,
+                   N.stream_handle())
         return out
+
+    def tensor_core_status(self):
+        """0, or the code of a timed-out pipeline wait of the last BF16 projection."""
+        if self._modes_bf16 is None or self._tc_ws is None:
+            return 0
+        return int(self._tc_ws[:4].view(torch.int32).item())
 
     @property
     def coefs(self):

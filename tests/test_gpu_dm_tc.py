@@ -1,0 +1,95 @@
+"""BF16 tensor-core (tcgen05) influence-function projection.
+
+Exactness of the MMA pipeline is checked against a float64 product of the
+same BF16-rounded operands (only FP32 accumulation differs: <= 1e-5); the
+BF16 path as a whole against the float64 projection (<= 2e-3), and the
+pyramid signal of a BF16 DM against the FP32 one (<= 2e-3, the BF16 IF
+path tolerance)."""
+import numpy as np
+import pytest
+
+from oracle import pwfs_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def bf16_round(a):
+    import torch
+    return torch.as_tensor(np.asarray(a, dtype=np.float32)).to(torch.bfloat16).to(torch.float64).numpy()
+
+
+@pytest.fixture(scope='module')
+def modes():
+    return O.dm_modes(120, 8.0, 20)
+
+
+@pytest.mark.parametrize('batch', [1, 3, 64, 65, 300])
+def test_tc_projection(modes, batch):
+    import torch
+    from oopao_gb300 import _native as N
+    n_pix, n_act = modes.shape
+    n_pad = (n_act + 63) // 64 * 64
+    mt = torch.as_tensor(np.ascontiguousarray(modes.T, dtype=np.float32), device='cuda')
+    mb = torch.empty((n_pix, n_pad), dtype=torch.bfloat16, device='cuda')
+    N.call('oopao_dm_modes_bf16', mt, n_act, n_pix, n_pad, mb, N.stream_handle())
+    rng = np.random.default_rng(batch)
+    coefs = rng.standard_normal((n_act, batch)).astype(np.float32)
+    c = torch.as_tensor(coefs, device='cuda')
+    out = torch.full((batch, n_pix), float('nan'), device='cuda')
+    nb = N.load().oopao_dm_bf16_workspace_bytes(n_pad, batch)
+    ws = torch.zeros(nb, dtype=torch.uint8, device='cuda')
+    N.call('oopao_dm_opd_bf16', mb, n_pad, c, n_act, n_pix, batch, 0.5, None, out, ws, nb, N.stream_handle())
+    torch.cuda.synchronize()
+    assert int(ws[:4].view(torch.int32).item()) == 0
+    got = out.double().cpu().numpy()
+    assert np.isfinite(got).all()
+    exact_bf16 = (bf16_round(modes) @ bf16_round(coefs)).T * 0.5
+    assert O.rel_l2(got, exact_bf16) < 1e-5
+    full = (modes @ coefs.astype(np.float64)).T * 0.5
+    assert O.rel_l2(got, full) < 2e-3
+
+
+def test_tc_projection_with_base(modes):
+    import torch
+    from oopao_gb300 import _native as N
+    n_pix, n_act = modes.shape
+    n_pad = (n_act + 63) // 64 * 64
+    mt = torch.as_tensor(np.ascontiguousarray(modes.T, dtype=np.float32), device='cuda')
+    mb = torch.empty((n_pix, n_pad), dtype=torch.bfloat16, device='cuda')
+    N.call('oopao_dm_modes_bf16', mt, n_act, n_pix, n_pad, mb, N.stream_handle())
+    coefs = np.random.default_rng(9).standard_normal((n_act, 2)).astype(np.float32)
+    base = np.random.default_rng(10).standard_normal((2, n_pix)).astype(np.float32)
+    c = torch.as_tensor(coefs, device='cuda')
+    b = torch.as_tensor(base, device='cuda')
+    out = torch.empty((2, n_pix), device='cuda')
+    nb = N.load().oopao_dm_bf16_workspace_bytes(n_pad, 2)
+    ws = torch.zeros(nb, dtype=torch.uint8, device='cuda')
+    N.call('oopao_dm_opd_bf16', mb, n_pad, c, n_act, n_pix, 2, 1.0, b, out, ws, nb, N.stream_handle())
+    torch.cuda.synchronize()
+    ref = (bf16_round(modes) @ bf16_round(coefs)).T + base
+    assert O.rel_l2(out.double().cpu().numpy(), ref) < 1e-5
+
+
+def test_bf16_dm_signal_within_tolerance():
+    import contextlib
+    import io
+    import oopao_gb300 as og
+    with contextlib.redirect_stdout(io.StringIO()):
+        tel = og.Telescope(resolution=120, diameter=8.0, samplingTime=1e-3)
+        ngs = og.Source(optBand='V0', magnitude=8)
+        ngs * tel
+        dm32 = og.DeformableMirror(tel, nSubap=20)
+        dm16 = og.DeformableMirror(tel, nSubap=20, if_dtype='bf16')
+        wfs = og.Pyramid(nSubap=20, telescope=tel, modulation=3, lightRatio=0.5, nTheta_user_defined=48)
+    c = np.random.default_rng(2).standard_normal(dm32.nValidAct) * 50e-9
+    dm32.coefs = c
+    ngs ** tel * dm32 * wfs
+    s32 = wfs.signal.copy()
+    dm16.coefs = c
+    ngs ** tel * dm16 * wfs
+    assert dm16.tensor_core_status() == 0
+    assert O.rel_l2(wfs.signal, s32) < 2e-3
+    m2c = np.eye(dm32.nValidAct)[:, :40]
+    D32 = og.InteractionMatrix(ngs, tel, dm32, wfs, m2c, 1e-8, single_pass=False, invert=False).D
+    D16 = og.InteractionMatrix(ngs, tel, dm16, wfs, m2c, 1e-8, single_pass=False, invert=False).D
+    assert O.rel_l2(D16, D32) < 2e-3
