@@ -172,7 +172,9 @@ int oopao_dm_opd_f32(const float* modes_t, const float* coefs, int n_act, int n_
  * accumulation), same result layout as oopao_dm_opd_f32 (plus an optional
  * base).  modes: device [n_pix][n_act_pad] BF16 (K-major, zero padded,
  * n_act_pad a multiple of 64), built once by oopao_dm_modes_bf16 from the
- * FP32 modes_t.  workspace: device, 256-byte aligned,
+ * FP32 modes_t.  The coefficients enter as two BF16 terms (hi = bf16(c),
+ * lo = bf16(c - hi)) summed in the FP32 accumulator, so only the IF matrix
+ * is rounded to BF16.  workspace: device, 256-byte aligned,
  * oopao_dm_bf16_workspace_bytes(n_act_pad, batch) bytes; its first int
  * holds 0 after the call, or the code of a pipeline wait that timed out. */
 int oopao_dm_modes_bf16(const float* modes_t, int n_act, int n_pix, int n_act_pad, void* modes_out, void* stream);

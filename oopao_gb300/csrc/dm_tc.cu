@@ -4,11 +4,14 @@
 // (dm.coefs setter, OOPAO/DeformableMirror.py:651-686), as a GEMM
 //   D[M = pixels][N = batch] = A[M][K = actuators] * B[N][K]^T
 // with A = the IF matrix in BF16, K-major ([n_pix][n_act_pad]), B = the
-// coefficients transposed to BF16 K-major ([batch_pad][n_act_pad]).
+// coefficients transposed to BF16 K-major and split into two BF16 terms,
+// hi = bf16(c) and lo = bf16(c - hi) ([2][batch_pad][n_act_pad]).  Both terms
+// accumulate into the same FP32 tile, so the coefficients keep ~16
+// significant bits and the only BF16 rounding left is the IF storage.
 //
 // One CTA computes a 128 x BN tile: a TMA producer thread streams 128x64 A
-// and BNx64 B tiles (128-byte swizzle) through a 4-stage mbarrier ring, one
-// thread issues tcgen05.mma (kind::f16, M=128, N=BN, K=16) into a TMEM
+// and two BNx64 B tiles (128-byte swizzle) through a 4-stage mbarrier ring,
+// one thread issues tcgen05.mma (kind::f16, M=128, N=BN, K=16) into a TMEM
 // accumulator, and the four warps read the accumulator back with
 // tcgen05.ld (32 lanes x 16 columns per load) and store FP32, coalesced
 // along pixels.  Every mbarrier wait is bounded: on time-out the CTA records
@@ -32,7 +35,8 @@ constexpr long long kWaitCycles = 1ll << 31;  // ~1 s at 2 GHz
 
 struct TcParams {
   int n_pix, batch;
-  int nk;  // K tiles
+  int nk;         // K tiles
+  int batch_pad;  // row offset of the lo coefficients
   float scale;
   const float* base;
   float* out;
@@ -128,14 +132,15 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r) {
 
 template <int BN>
 constexpr size_t tc_smem_bytes() {
-  return 1024 + (size_t)kStages * (kBM + BN) * kBK * 2 + 256;
+  return 1024 + (size_t)kStages * (kBM + 2 * BN) * kBK * 2 + 256;
 }
 
 template <int BN>
 __global__ void __launch_bounds__(kThreads, 1)
     dm_tc_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_b, TcParams p) {
   constexpr int A_BYTES = kBM * kBK * 2;
-  constexpr int B_BYTES = BN * kBK * 2;
+  constexpr int B_BYTES = 2 * BN * kBK * 2;  // hi tile, then lo tile
+  constexpr int B_HALF = BN * kBK * 2;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   unsigned char* sa = smem;
@@ -174,6 +179,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
       tma_load_2d(sa + s * A_BYTES, &tma_a, &full[s], kb * kBK, m0);
       tma_load_2d(sb + s * B_BYTES, &tma_b, &full[s], kb * kBK, n0);
+      tma_load_2d(sb + s * B_BYTES + B_HALF, &tma_b, &full[s], kb * kBK, p.batch_pad + n0);
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
@@ -184,8 +190,11 @@ __global__ void __launch_bounds__(kThreads, 1)
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t a0 = smem_u32(sa + s * A_BYTES), b0 = smem_u32(sb + s * B_BYTES);
 #pragma unroll
-      for (int k = 0; k < kBK / kUK; k++)
-        mma_bf16(tmem, sw128_desc(a0 + k * kUK * 2), sw128_desc(b0 + k * kUK * 2), idesc, (kb | k) ? 1u : 0u);
+      for (int k = 0; k < kBK / kUK; k++) {
+        const uint64_t ad = sw128_desc(a0 + k * kUK * 2);
+        mma_bf16(tmem, ad, sw128_desc(b0 + k * kUK * 2), idesc, (kb | k) ? 1u : 0u);
+        mma_bf16(tmem, ad, sw128_desc(b0 + B_HALF + k * kUK * 2), idesc, 1u);
+      }
       mma_commit(&empty[s]);
     }
     mma_commit(done);
@@ -221,13 +230,17 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
-// coefs [n_act][batch] f32 -> coefsT [batch_pad][n_act_pad] bf16, zero padded
+// coefs [n_act][batch] f32 -> [2][batch_pad][n_act_pad] bf16 (hi, lo), zero padded
 __global__ void dm_coefs_to_bf16(const float* __restrict__ coefs, int n_act, int batch, int n_act_pad,
                                  int batch_pad, __nv_bfloat16* __restrict__ out) {
+  const size_t plane = (size_t)batch_pad * n_act_pad;
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (size_t)batch_pad * n_act_pad) return;
+  if (i >= plane) return;
   const int b = (int)(i / n_act_pad), a = (int)(i % n_act_pad);
-  out[i] = __float2bfloat16_rn((a < n_act && b < batch) ? coefs[(size_t)a * batch + b] : 0.f);
+  const float c = (a < n_act && b < batch) ? coefs[(size_t)a * batch + b] : 0.f;
+  const __nv_bfloat16 hi = __float2bfloat16_rn(c);
+  out[i] = hi;
+  out[plane + i] = __float2bfloat16_rn(c - __bfloat162float(hi));
 }
 
 // modes_t [n_act][n_pix] f32 -> modes [n_pix][n_act_pad] bf16, zero padded
@@ -280,11 +293,11 @@ int launch_tc(const void* modes, const void* coefs_t, int n_pix, int n_act_pad, 
   CUtensorMap ta, tb;
   int s = encode_2d(&ta, modes, (uint64_t)n_act_pad, (uint64_t)n_pix, kBK, kBM);
   if (s) return s;
-  s = encode_2d(&tb, coefs_t, (uint64_t)n_act_pad, (uint64_t)batch_pad, kBK, BN);
+  s = encode_2d(&tb, coefs_t, (uint64_t)n_act_pad, (uint64_t)(2 * batch_pad), kBK, BN);
   if (s) return s;
   const size_t smem = tc_smem_bytes<BN>();
   OOPAO_CUDA_TRY(cudaFuncSetAttribute(dm_tc_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  TcParams p{n_pix, batch, n_act_pad / kBK, scale, base, out, err};
+  TcParams p{n_pix, batch, n_act_pad / kBK, batch_pad, scale, base, out, err};
   dim3 grid(ceil_div(n_pix, kBM), batch_pad / BN);
   dm_tc_kernel<BN><<<grid, kThreads, smem, st>>>(ta, tb, p);
   return OOPAO_OK;
@@ -309,7 +322,7 @@ extern "C" size_t oopao_dm_bf16_workspace_bytes(int n_act_pad, int batch) {
   if (n_act_pad <= 0 || batch <= 0) return 0;
   const int bn = batch <= 64 ? 64 : 128;
   const size_t batch_pad = (size_t)ceil_div(batch, bn) * bn;
-  return 256 + batch_pad * n_act_pad * 2;
+  return 256 + 2 * batch_pad * n_act_pad * 2;
 }
 
 extern "C" int oopao_dm_opd_bf16(const void* modes, int n_act_pad, const float* coefs, int n_act, int n_pix,

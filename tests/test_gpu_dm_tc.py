@@ -1,10 +1,10 @@
 """BF16 tensor-core (tcgen05) influence-function projection.
 
 Exactness of the MMA pipeline is checked against a float64 product of the
-same BF16-rounded operands (only FP32 accumulation differs: <= 1e-5); the
-BF16 path as a whole against the float64 projection (<= 2e-3), and the
-pyramid signal of a BF16 DM against the FP32 one (<= 2e-3, the BF16 IF
-path tolerance)."""
+same BF16 operands (BF16 IFs, coefficients as hi + lo BF16 terms; only the
+FP32 accumulation differs: <= 1e-5); the BF16 path as a whole against the
+float64 projection (<= 2e-3), and the pyramid signal of a BF16 DM against
+the FP32 one (<= 2e-3, the BF16 IF path tolerance)."""
 import numpy as np
 import pytest
 
@@ -16,6 +16,14 @@ pytestmark = pytest.mark.gpu
 def bf16_round(a):
     import torch
     return torch.as_tensor(np.asarray(a, dtype=np.float32)).to(torch.bfloat16).to(torch.float64).numpy()
+
+
+def bf16_split(c):
+    """hi + lo with hi = bf16(c), lo = bf16(c - hi), as the kernel stores them."""
+    c = np.asarray(c, dtype=np.float32)
+    hi = bf16_round(c)
+    lo = bf16_round(c - hi.astype(np.float32))
+    return hi + lo
 
 
 @pytest.fixture(scope='module')
@@ -43,7 +51,7 @@ def test_tc_projection(modes, batch):
     assert int(ws[:4].view(torch.int32).item()) == 0
     got = out.double().cpu().numpy()
     assert np.isfinite(got).all()
-    exact_bf16 = (bf16_round(modes) @ bf16_round(coefs)).T * 0.5
+    exact_bf16 = (bf16_round(modes) @ bf16_split(coefs)).T * 0.5
     assert O.rel_l2(got, exact_bf16) < 1e-5
     full = (modes @ coefs.astype(np.float64)).T * 0.5
     assert O.rel_l2(got, full) < 2e-3
@@ -66,7 +74,7 @@ def test_tc_projection_with_base(modes):
     ws = torch.zeros(nb, dtype=torch.uint8, device='cuda')
     N.call('oopao_dm_opd_bf16', mb, n_pad, c, n_act, n_pix, 2, 1.0, b, out, ws, nb, N.stream_handle())
     torch.cuda.synchronize()
-    ref = (bf16_round(modes) @ bf16_round(coefs)).T + base
+    ref = (bf16_round(modes) @ bf16_split(coefs)).T + base
     assert O.rel_l2(out.double().cpu().numpy(), ref) < 1e-5
 
 
