@@ -79,13 +79,13 @@ def kl_like_basis(modes, pupil, n_modes, diameter=8.0, r0=0.15, L0=25.0):
     return np.ascontiguousarray(vec)
 
 
-def build_system(dev_index, res=RES, nsub=NSUB, mod=MOD, ntheta=NTHETA, max_batch=100):
+def build_system(dev_index, res=RES, nsub=NSUB, mod=MOD, ntheta=NTHETA, max_batch=100, if_dtype='fp32'):
     import oopao_gb300 as og
     with _quiet():
         tel = og.Telescope(resolution=res, diameter=8.0, samplingTime=1e-3)
         ngs = og.Source(optBand='V0', magnitude=8)
         ngs * tel
-        dm = og.DeformableMirror(tel, nSubap=nsub, mechCoupling=0.35)
+        dm = og.DeformableMirror(tel, nSubap=nsub, mechCoupling=0.35, if_dtype=if_dtype)
         wfs = og.Pyramid(nSubap=nsub, telescope=tel, modulation=mod, lightRatio=0.5,
                          nTheta_user_defined=ntheta, max_batch=max_batch)
     return tel, ngs, dm, wfs
@@ -135,11 +135,12 @@ def im_comparison(tel, ngs, dm, wfs, m2c, n_per_mode, with_error=True):
 def cl_rate(n_steps=2000):
     """Graph-replayed closed-loop steps/s on the 40x40 configuration: 240 px,
     N=504, modulation 5 l/D x 96 points, 41x41 DM, 3 frozen-flow layers
-    (r0 0.12 m, L0 30 m, 10/15/20 m/s), gain 0.4, delay 1."""
+    (r0 0.12 m, L0 30 m, 10/15/20 m/s), gain 0.4, delay 1; BF16 tensor-core
+    IF projection with FP32 accumulation."""
     import torch
     from oopao_gb300.closed_loop import ClosedLoop, VonKarmanLayers
     from oopao_gb300 import autotune
-    tel, ngs, dm, wfs = build_system(0, 240, 40, 5, 96, max_batch=16)
+    tel, ngs, dm, wfs = build_system(0, 240, 40, 5, 96, max_batch=16, if_dtype='bf16')
     autotune.tune_pyramid(wfs, batch=1)
     layers = VonKarmanLayers(tel, r0=0.12, L0=30, fractionalR0=(1 / 3, 1 / 3, 1 / 3), windSpeed=(10., 15., 20.),
                              windDirection=(0., 72., 144.), seed=0)
@@ -157,7 +158,63 @@ def cl_rate(n_steps=2000):
     ms = e0.elapsed_time(e1) / n_steps
     return {'config': '40x40 PWFS, 240 px, N=504, 96 points, 41x41 DM (%d act), 3 layers' % dm.nValidAct,
             'steps': n_steps, 'us_per_step': ms * 1000.0, 'khz': 1.0 / ms,
-            'graph': True, 'variant': int(N_variant(wfs))}
+            'graph': True, 'variant': int(N_variant(wfs)), 'dm': 'bf16 tcgen05',
+            'tc_status': dm.tensor_core_status()}
+
+
+def dm_projection(peaks):
+    """DM influence-function projection OPD = modes @ coefs at the 20x20,
+    40x40 and 80x80 sizes: FP32 CUDA-core path vs BF16 tcgen05 path, per
+    batch.  Modes are seeded device-random (timing does not depend on the
+    values).  Dense FLOPs 2*n_pix*n_act*B; IF bytes are the bytes of the IF
+    matrix one call streams (FP32 [n_act][n_pix] or BF16 [n_pix][n_act_pad])."""
+    import torch
+    from oopao_gb300 import _native as N
+    lib = N.load()
+    st = N.stream_handle()
+    out = {}
+    for name, n_side, n_act in (('20x20', 120, 357), ('40x40', 240, 1353), ('80x80', 480, 5209)):
+        n_pix = n_side * n_side
+        n_pad = (n_act + 63) // 64 * 64
+        g = torch.Generator(device='cuda').manual_seed(0)
+        mt = torch.randn((n_act, n_pix), device='cuda', generator=g)
+        mb = torch.empty((n_pix, n_pad), dtype=torch.bfloat16, device='cuda')
+        N.call('oopao_dm_modes_bf16', mt, n_act, n_pix, n_pad, mb, st)
+        rows = []
+        for B in (1, 16, 64, 300):
+            c = torch.randn((n_act, B), device='cuda', generator=g)
+            o = torch.empty((B, n_pix), device='cuda')
+            nb = lib.oopao_dm_bf16_workspace_bytes(n_pad, B)
+            ws = torch.zeros(nb, dtype=torch.uint8, device='cuda')
+            runs = {'fp32': lambda: N.call('oopao_dm_opd_acc_f32', mt, c, n_act, n_pix, B, 1.0, None, o, st),
+                    'bf16_tc': lambda: N.call('oopao_dm_opd_bf16', mb, n_pad, c, n_act, n_pix, B, 1.0, None, o, ws,
+                                              nb, st)}
+            row = {'batch': B}
+            for key, fn in runs.items():
+                reps = 20
+                for _ in range(3):
+                    fn()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(reps):
+                    fn()
+                e1.record()
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1) / reps
+                if_bytes = n_pix * n_act * 4 if key == 'fp32' else n_pix * n_pad * 2
+                row[key] = {'ms': ms, 'tflops': 2.0 * n_pix * n_act * B / ms / 1e9,
+                            'if_gbs': if_bytes / ms / 1e6}
+                if key == 'bf16_tc' and peaks.get('bf16_tflops'):
+                    row[key]['tensor_frac_of_measured_bf16'] = row[key]['tflops'] / peaks['bf16_tflops']
+                if peaks.get('hbm_gbs'):
+                    row[key]['hbm_frac_of_measured'] = row[key]['if_gbs'] / peaks['hbm_gbs']
+            row['tc_error_word'] = int(ws[:4].view(torch.int32).item())
+            rows.append(row)
+        out[name] = {'n_pix': n_pix, 'n_act': n_act, 'if_bf16_mb': n_pix * n_pad * 2 / 1e6,
+                     'l2_resident': n_pix * n_pad * 2 < 120e6, 'rows': rows}
+        del mt, mb
+        torch.cuda.empty_cache()
+    return out
 
 
 def N_variant(wfs):
@@ -440,6 +497,11 @@ def run_ours(args):
         extra['im_c3_1000'] = im_comparison(tel3, ngs3, dm3, wfs3, m2c3, n_per_mode=10)
         del tel3, ngs3, dm3, wfs3
         extra['cl_step'] = cl_rate()
+        try:
+            pk = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
+        except Exception:
+            pk = {'hbm_gbs': 6800.0, 'bf16_tflops': 1900.0}
+        extra['dm_projection'] = dm_projection(pk)
 
     if rank == 0:
         line = {
@@ -468,6 +530,64 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+CASES = {'pwfs20': (120, 20, 3, 48), 'pwfs40': (240, 40, 5, 96)}
+
+
+def run_case(args):
+    """Small fixed workload for profiler captures (prints one JSON line, not a
+    bench line).  pwfs20 / pwfs40: `--reps` batched PWFS measurements of
+    `--batch` seeded random OPDs on the 20x20 / 40x40 configuration with the
+    autotuned kernel variant; dm40: `--reps` BF16 tensor-core and FP32 IF
+    projections of `--batch` coefficient vectors on the 40x40 DM.  The
+    measured loop is the NVTX range 'case' (ncu --nvtx --nvtx-include case/)."""
+    import torch
+    from oopao_gb300 import _native as N
+    from oopao_gb300 import autotune
+    torch.cuda.set_device(0)
+    g = torch.Generator(device='cuda').manual_seed(0)
+    t0 = time.perf_counter()
+    if args.case in CASES:
+        res, nsub, mod, nth = CASES[args.case]
+        tel, ngs, dm, wfs = build_system(0, res, nsub, mod, nth, max_batch=args.batch)
+        if args.variant >= 0:
+            N.call('oopao_pwfs_set_variant', wfs.plan.h, args.variant)
+            tune = {'variant': args.variant}
+        else:
+            tune = autotune.tune_pyramid(wfs, batch=args.batch)
+        ngs ** tel
+        wfs.plan.set_amplitude(ngs.intensity, wfs._amplitude_key())
+        opd = torch.randn((args.batch, res, res), device='cuda', generator=g) * 50e-9
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push('case')
+        for _ in range(args.reps):
+            frame, _ = wfs._measure_frames(opd, 2 * np.pi / ngs.wavelength)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        out = {'case': args.case, 'batch': args.batch, 'reps': args.reps, 'variant': tune['variant'],
+               'frame_sum': float(frame.double().sum().item())}
+    elif args.case == 'dm40':
+        tel, ngs, dm, wfs = None, None, None, None
+        with _quiet():
+            import oopao_gb300 as og
+            tel = og.Telescope(resolution=240, diameter=8.0, samplingTime=1e-3)
+            dm = og.DeformableMirror(tel, nSubap=40, if_dtype='bf16')
+        c = torch.randn((dm.nValidAct, args.batch), device='cuda', generator=g) * 50e-9
+        o = torch.empty((args.batch, 240, 240), device='cuda')
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push('case')
+        for _ in range(args.reps):
+            dm.opd_device(c, out=o)
+            N.call('oopao_dm_opd_acc_f32', dm._modes_t, c, dm.nValidAct, 240 * 240, args.batch, 1.0, None, o,
+                   N.stream_handle())
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        out = {'case': args.case, 'batch': args.batch, 'reps': args.reps, 'tc_status': dm.tensor_core_status()}
+    else:
+        raise SystemExit('unknown case %s' % args.case)
+    out['seconds'] = time.perf_counter() - t0
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -477,8 +597,17 @@ def main():
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline and accuracy legs')
     ap.add_argument('--no-extra', action='store_true',
                     help='skip the interaction-matrix comparisons and the closed-loop rate')
+    ap.add_argument('--case', default=None, help='run a small profiling workload (%s, dm40) instead'
+                    % ', '.join(CASES))
+    ap.add_argument('--batch', type=int, default=16)
+    ap.add_argument('--reps', type=int, default=3)
+    ap.add_argument('--variant', type=int, default=-1, help='kernel variant for --case (-1: autotune)')
     args = ap.parse_args()
-    if args.impl == 'reference':
+    if args.case:
+        import __graft_entry__
+        __graft_entry__.build()
+        run_case(args)
+    elif args.impl == 'reference':
         run_reference(args)
     else:
         import __graft_entry__

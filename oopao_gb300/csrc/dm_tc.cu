@@ -150,7 +150,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint64_t* done = empty + kStages;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
+  // x = batch tile, so the CTAs that share one 128-pixel IF tile run
+  // together and the tile is read from HBM once, then from L2
+  const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * BN;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; s++) {
@@ -298,7 +300,7 @@ int launch_tc(const void* modes, const void* coefs_t, int n_pix, int n_act_pad, 
   const size_t smem = tc_smem_bytes<BN>();
   OOPAO_CUDA_TRY(cudaFuncSetAttribute(dm_tc_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   TcParams p{n_pix, batch, n_act_pad / kBK, batch_pad, scale, base, out, err};
-  dim3 grid(ceil_div(n_pix, kBM), batch_pad / BN);
+  dim3 grid(batch_pad / BN, ceil_div(n_pix, kBM));
   dm_tc_kernel<BN><<<grid, kThreads, smem, st>>>(ta, tb, p);
   return OOPAO_OK;
 }
@@ -334,6 +336,7 @@ extern "C" int oopao_dm_opd_bf16(const void* modes, int n_act_pad, const float* 
   OOPAO_CHECK_ARG(((uintptr_t)modes & 15) == 0 && ((uintptr_t)workspace & 255) == 0,
                   "modes must be 16-byte and the workspace 256-byte aligned");
   OOPAO_CHECK_ARG(workspace_bytes >= oopao_dm_bf16_workspace_bytes(n_act_pad, batch), "workspace too small");
+  OOPAO_CHECK_ARG(ceil_div(n_pix, kBM) <= 65535, "n_pix above 65535 * 128");
   cudaStream_t st = (cudaStream_t)stream;
   const int bn = batch <= 64 ? 64 : 128;
   const int batch_pad = ceil_div(batch, bn) * bn;

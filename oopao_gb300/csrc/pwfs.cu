@@ -98,6 +98,7 @@ struct oopao_pwfs_plan {
   size_t l2_budget;  // bytes of FFT intermediates per pass (kept L2-resident)
   const struct FastPasses* fast;  // compile-time plan for n, or null (generic kernels)
   int variant;                    // 1 = use `fast` when available, 0 = generic
+  int inv_target_ctas;            // row-inverse CTAs wanted per launch (2 resident waves)
   // signal processing
   int sp_mode, nq, n2d, n_signal, cam2;
   int q_r0[4], q_c0[4];
@@ -289,16 +290,25 @@ int fast_candidates(int n, const FastPasses** out) {
 #undef OOPAO_CANDS
 }
 
+constexpr int kTargetCtas = 2 * 152;  // row-inverse CTAs wanted by the generic kernels
+
 const FastPasses* fast_passes(int n, int idx = 0) {
   const FastPasses* c = nullptr;
   const int cnt = fast_candidates(n, &c);
   return (idx >= 0 && idx < cnt) ? c + idx : nullptr;
 }
 
-cudaError_t fast_attrs(const FastPasses* f) {
+// Opt the variant's kernels into their shared memory and return, in
+// *inv_target, two resident waves of row-inverse CTAs on this device.
+cudaError_t fast_attrs(const FastPasses* f, int* inv_target) {
   cudaError_t e = cudaFuncSetAttribute(f->rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->smem_rows);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(f->cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->smem_cols);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(f->inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->smem_inv);
+  int dev = 0, sms = 0, occ = 0;
+  if (e == cudaSuccess) e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, f->inv, f->t * f->l_inv, f->smem_inv);
+  if (e == cudaSuccess) *inv_target = 2 * sms * std::max(occ, 1);
   return e;
 }
 }  // namespace
@@ -588,7 +598,8 @@ extern "C" int oopao_pwfs_plan_create(oopao_pwfs_plan** out, int res, int n, int
   if (e == cudaSuccess) e = cudaFuncSetAttribute(pwfs_rows_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
   p->fast = fast_passes(n, 0);
   p->variant = p->fast ? 1 : 0;
-  if (p->fast && e == cudaSuccess) e = fast_attrs(p->fast);
+  p->inv_target_ctas = kTargetCtas;
+  if (p->fast && e == cudaSuccess) e = fast_attrs(p->fast, &p->inv_target_ctas);
   if (e != cudaSuccess) {
     oopao_set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
     free_plan(p);
@@ -653,7 +664,6 @@ namespace {
 
 constexpr int kMaxSlotsBinned = 64;  // partial sums over modulation points, fused binning
 constexpr int kMaxSlotsRaw = 8;      // partial sums kept un-binned (raw_data requested)
-constexpr int kTargetCtas = 2 * 152;
 
 // How one oopao_pwfs_measure call is cut into passes: each pass holds the
 // row/column intermediates of `bc` items x `kp` points, sized to stay
@@ -685,7 +695,7 @@ PassPlan plan_passes(const oopao_pwfs_plan* p, int batch, bool want_raw, size_t 
     pp.ksplit = p->ksplit;
   } else {
     const int row_blocks = ceil_div(p->n, pp.fast ? f->l_inv : p->inv_rows_per_cta);
-    const int want = ceil_div(kTargetCtas, row_blocks * pp.bc);
+    const int want = ceil_div(pp.fast ? p->inv_target_ctas : kTargetCtas, row_blocks * pp.bc);
     int best = 1;
     for (int d = 1; d <= k && d <= cap; d++) {
       if (k % d) continue;
@@ -1334,8 +1344,10 @@ extern "C" int oopao_pwfs_set_variant(oopao_pwfs_plan* p, int variant) {
   }
   if (variant >= 1) {
     const FastPasses* f = c + (variant - 1);
-    OOPAO_CUDA_TRY(fast_attrs(f));
+    int target = kTargetCtas;
+    OOPAO_CUDA_TRY(fast_attrs(f, &target));
     p->fast = f;
+    p->inv_target_ctas = target;
   }
   p->variant = variant;
   return OOPAO_OK;

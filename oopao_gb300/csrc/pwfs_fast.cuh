@@ -44,6 +44,46 @@ __host__ __device__ constexpr int xchg_stride(int min_ls, int T, int L, int RP, 
   return best;
 }
 
+// Same count for an l-fastest pass (thread tid -> line tid % L, butterfly
+// tid / L), as the column pass maps its threads.
+__host__ __device__ constexpr int xchg_conflicts_lf(int LS, int T, int L, int RP, int nw, int nr) {
+  int total = 0;
+  for (int pat = 0; pat < 2; pat++) {
+    const int nj = pat == 0 ? nw : nr, stride = pat == 0 ? RP : 1;
+    for (int base = 0; base < T * L; base += 16) {
+      int cnt[16] = {};
+      for (int u = 0; u < 16 && base + u < T * L; u++) {
+        const int tid = base + u, l = tid % L, t = tid / L;
+        if (t >= nj) continue;
+        cnt[(l * LS + t * stride) % 16]++;
+      }
+      int mx = 0;
+      for (int i = 0; i < 16; i++) mx = cnt[i] > mx ? cnt[i] : mx;
+      total += mx > 0 ? mx - 1 : 0;
+    }
+  }
+  return total;
+}
+
+// Exchange layout of one column-pass buffer: radix-R butterflies write
+// R values at j*RP (j < NW) and are read back at m*RP + j (j < R); RP >= R
+// and the line stride LS >= NW*RP are searched for the fewest conflicts
+// (ties: least shared memory).  Returns RP * 65536 + LS.
+__host__ __device__ constexpr int cols_layout(int R, int NW, int T, int L) {
+  int best = 0, best_c = 1 << 30, best_sz = 1 << 30;
+  for (int rp = R; rp < R + 4; rp++) {
+    for (int ls = NW * rp; ls < NW * rp + 16; ls++) {
+      const int c = xchg_conflicts_lf(ls, T, L, rp, NW, R);
+      if (c < best_c || (c == best_c && ls < best_sz)) {
+        best_c = c;
+        best_sz = ls;
+        best = rp * 65536 + ls;
+      }
+    }
+  }
+  return best;
+}
+
 // ---- pass 1: forward row FFT of field * row phasor (j-fastest mapping) ----
 template <int N, int R1, int R2, int T, int L>
 __global__ void __launch_bounds__(T* L) pwfs_rows_fwd2(RowsFwdArgs a) {
@@ -99,15 +139,16 @@ __global__ void __launch_bounds__(T* L) pwfs_rows_fwd2(RowsFwdArgs a) {
 // ---- pass 2: column phasor, forward FFT, mask, inverse FFT (l-fastest) ----
 template <int N, int R1, int R2, int T, int L>
 __global__ void __launch_bounds__(T* L) pwfs_cols2(ColsArgs a) {
-  constexpr int R1P = pad_odd(R1), R2P = pad_odd(R2);
-  constexpr int LS = odd_up(imax(R2 * R1P, R1 * R2P));
+  constexpr int LAY1 = cols_layout(R1, R2, T, L), LAY2 = cols_layout(R2, R1, T, L);
+  constexpr int R1P = LAY1 >> 16, LS1 = LAY1 & 0xFFFF;
+  constexpr int R2P = LAY2 >> 16, LS2 = LAY2 & 0xFFFF;
   constexpr int PBA = (R2 + T - 1) / T;   // forward stage A / inverse stage B' butterflies
   constexpr int PBB = (R1 + T - 1) / T;   // forward stage B / inverse stage A' butterflies
   extern __shared__ float2 sm[];
-  float2* tw = sm;           // tw[m*R1 + j]  = W_N^{j m},  j < R1, m < R2
-  float2* twi = sm + N;      // twi[m*R2 + j] = W_N^{-j m}, j < R2, m < R1
-  float2* b1 = sm + 2 * N;   // [L][LS] forward exchange
-  float2* b2 = b1 + L * LS;  // [L][LS] inverse exchange
+  float2* tw = sm;            // tw[m*R1 + j]  = W_N^{j m},  j < R1, m < R2
+  float2* twi = sm + N;       // twi[m*R2 + j] = W_N^{-j m}, j < R2, m < R1
+  float2* b1 = sm + 2 * N;    // [L][LS1] forward exchange
+  float2* b2 = b1 + L * LS1;  // [L][LS2] inverse exchange
   const int tid = threadIdx.x;
   const int l = tid % L, t = tid / L;
   for (int i = tid; i < N; i += T * L) {
@@ -122,8 +163,8 @@ __global__ void __launch_bounds__(T* L) pwfs_cols2(ColsArgs a) {
   const int res = a.res, off = a.off;
   const float2* y = a.y + ((size_t)b * a.ng + g) * res * N + c;
   const float2* cf = a.colfac + (size_t)kabs * res;
-  float2* x1 = b1 + l * LS;
-  float2* x2 = b2 + l * LS;
+  float2* x1 = b1 + l * LS1;
+  float2* x2 = b2 + l * LS2;
   // forward stage A: rows e = j + m*R2, non-zero for off <= e < off + res
 #pragma unroll
   for (int p = 0; p < PBA; p++) {
@@ -300,7 +341,7 @@ template <int N, int R1, int R2, int T, int LR, int LC, int LI>
 FastPasses make_fast() {
   constexpr int R1P = pad_odd(R1), R2P = pad_odd(R2);
   constexpr int LSR = xchg_stride(R2 * R1P, T, LR, R1P, R2, R1);
-  constexpr int LSC = odd_up(imax(R2 * R1P, R1 * R2P));
+  constexpr int LSC = (cols_layout(R1, R2, T, LC) & 0xFFFF) + (cols_layout(R2, R1, T, LC) & 0xFFFF);
   constexpr int LSI = xchg_stride(R1 * R2P, T, LI, R2P, R1, R2);
   FastPasses f;
   f.n = N; f.r1 = R1; f.r2 = R2; f.t = T; f.l_rows = LR; f.l_cols = LC; f.l_inv = LI;
@@ -308,7 +349,7 @@ FastPasses make_fast() {
   f.cols = pwfs_cols2<N, R1, R2, T, LC>;
   f.inv = pwfs_rows_inv2<N, R1, R2, T, LI>;
   f.smem_rows = sizeof(float2) * (N + (size_t)LR * LSR);
-  f.smem_cols = sizeof(float2) * (2 * N + 2 * (size_t)LC * LSC);
+  f.smem_cols = sizeof(float2) * (2 * N + (size_t)LC * LSC);
   f.smem_inv = sizeof(float2) * (N + 2 * (size_t)LI * LSI);
   return f;
 }
