@@ -249,10 +249,15 @@ class Pyramid:
         return out
 
     def _effective_mask(self):
+        """Focal-plane multiplier of one modulation point.  The mask carries the
+        spatial filter; the 1-pixel-centred branch multiplies the shifted
+        focal field by the filter once more (OOPAO/Pyramid.py:634-637)."""
         m = self.mask
-        if self.spatialFilter is not None:
-            m = (m * self.spatialFilter).astype(np.complex64)
-        return m
+        if not self.psfCentering and self.spatialFilter is not None:
+            if np.shape(self.spatialFilter) != np.shape(m):
+                raise OopaoError('spatialFilter must have the shape of the mask %s' % (np.shape(m),))
+            m = m * self.spatialFilter
+        return np.asarray(m).astype(np.complex64)
 
     def _make_plan(self, path):
         tel = self.telescope
@@ -294,6 +299,36 @@ class Pyramid:
             self.referenceSignal = 0
             self.referenceSignal_2D = 0
             self.wfs_calibration()
+
+    @property
+    def spatialFilter(self):
+        return self._spatialFilter
+
+    @spatialFilter.setter
+    def spatialFilter(self, val):
+        """``spatialFilter`` setter (OOPAO/Pyramid.py:1051-1085): the mask becomes
+        initial_mask * val (or initial_mask again for None / a wrong shape) and
+        a calibrated sensor is recalibrated."""
+        self._spatialFilter = val
+        if not getattr(self, 'isInitialized', False):
+            return
+        if val is None:
+            print('No spatial filter considered')
+            self.mask = self.initial_mask
+        elif np.shape(val) == self.mask.shape:
+            print('A spatial filter is now considered')
+            self.mask = self.initial_mask * val
+        else:
+            warning('Wrong shape for the spatial filter. No spatial filter attached to the mask')
+            self.mask = self.initial_mask
+        self._plan = None
+        if self.isCalibrated:
+            print('Updating the reference slopes and Wavelength Calibration for the new modulation...')
+            self.slopesUnits = 1
+            self.referenceSignal = 0
+            self.referenceSignal_2D = 0
+            self.wfs_calibration()
+            print('Done!')
 
     @property
     def delta_Tip(self):

@@ -155,6 +155,19 @@ class PyramidGeometry:
     tilt: np.ndarray            # float64 [res,res]
     binning: int = 1
     extra: dict = field(default_factory=dict)
+    spatial_filter: object = None  # [N,N] or None; mask already includes it
+
+
+def with_spatial_filter(geom: PyramidGeometry, filt, initial_mask=None) -> PyramidGeometry:
+    """``spatialFilter`` setter, ``OOPAO/Pyramid.py:1051-1085``: mask =
+    initial_mask * filter (initial_mask again for None or a wrong shape)."""
+    import dataclasses
+    m0 = geom.mask if initial_mask is None else initial_mask
+    if filt is not None and np.shape(filt) == m0.shape:
+        mask = m0 * filt
+    else:
+        mask = m0
+    return dataclasses.replace(geom, mask=mask, spatial_filter=filt)
 
 
 def phase_mask(res: int, n_subap: int, n_pix_separation: float, n_pix_edge: float,
@@ -257,6 +270,8 @@ def pyramid_transform_stack(phase_pts: np.ndarray, amplitude: np.ndarray,
     N, res, c = geom.N, geom.res, geom.center
     lo = c - res // 2
     P = phase_pts.shape[0]
+    if spatial_filter is None:
+        spatial_filter = geom.spatial_filter
     support = np.zeros((P, N, N), dtype=np.complex128)
     support[:, lo:lo + res, lo:lo + res] = amplitude[None] * np.exp(1j * phase_pts)
     if geom.psf_centering:
@@ -422,11 +437,15 @@ def build_pyramid(res: int, n_subap: int, modulation: float, light_ratio: float,
                   n_pix_edge=None, psf_centering: bool = True, calib_modulation: float = 50.,
                   n_theta_user: int | None = None, extra: int = 0, delta_theta: float = 0.,
                   rooftop: float = 0., theta_rotation: float = 0., user_path=None,
-                  workers: int = 1) -> OraclePyramid:
+                  workers: int = 1, spatial_filter=None) -> OraclePyramid:
     """Construction sequence of ``Pyramid.__init__`` (``OOPAO/Pyramid.py:26-366``):
     geometry, calibration modulation clamp (``:292-296``), valid pixels at
     ``calibModulation`` (``initialization`` ``:541-589``), flat-wavefront
-    reference slopes (``wfs_calibration`` ``:591-610``)."""
+    reference slopes (``wfs_calibration`` ``:591-610``).  With
+    ``spatial_filter``, the filter is then attached as the ``spatialFilter``
+    setter does (``:1051-1085``): the mask is filtered and the reference
+    slopes are measured again; the valid pixels stay those of the
+    unfiltered initialization."""
     geom = pyramid_geometry(res, n_subap, n_pix_separation, n_pix_edge, psf_centering,
                             rooftop, theta_rotation)
     if calib_modulation >= res / 2:
@@ -442,6 +461,8 @@ def build_pyramid(res: int, n_subap: int, modulation: float, light_ratio: float,
     valid, _ = valid_pixels(frame0, geom, light_ratio)
     path, n_theta = modulation_path(modulation, n_theta_user, extra, delta_theta, user_path=user_path)
     tt = tt_buffers(path, geom)
+    if spatial_filter is not None:
+        geom = with_spatial_filter(geom, spatial_filter)
     raw1 = wfs_raw(flat, intensity, tt, geom, workers=workers)
     frame1 = camera_frame(raw1, geom)
     ref2d, _, _ = slopes_maps(frame1, geom, valid, 0)

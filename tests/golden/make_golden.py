@@ -84,13 +84,31 @@ def geometry_record(tel, ngs, dm, wfs):
     )
 
 
+def circular_filter(n, radius, centred_on_pixel):
+    """Top-hat focal-plane filter of `radius` pixels around the PSF centre
+    (pixel n/2 for the 1-pixel-centred mask, the 4-pixel corner otherwise)."""
+    c = n / 2 if centred_on_pixel else (n - 1) / 2
+    yy, xx = np.mgrid[:n, :n]
+    return (np.hypot(xx - c, yy - c) <= radius).astype(np.float64)
+
+
 def case_small(OOPAO, name, res, n_subap, modulation, light_ratio, co=0.0, full=True, n_im=6,
-               seeds=(1, 2), **kw):
+               seeds=(1, 2), sf_radius=None, **kw):
     tel, ngs, dm, wfs = build(OOPAO, res, n_subap, modulation, light_ratio, co=co, **kw)
-    rec = geometry_record(tel, ngs, dm, wfs)
     import json
-    rec['params'] = json.dumps(dict(res=res, n_subap=n_subap, modulation=modulation,
-                                    light_ratio=light_ratio, co=co, **kw))
+    params = dict(res=res, n_subap=n_subap, modulation=modulation, light_ratio=light_ratio, co=co, **kw)
+    filt = None
+    if sf_radius is not None:
+        # attached after construction through the reference's own setter,
+        # which filters the mask and re-measures the reference slopes
+        filt = circular_filter(wfs.mask.shape[0], sf_radius, not kw.get('psfCentering', True))
+        with _quiet():
+            wfs.spatialFilter = filt
+        params['sf_radius'] = sf_radius
+    rec = geometry_record(tel, ngs, dm, wfs)
+    if filt is not None:
+        rec['spatial_filter'] = filt
+    rec['params'] = json.dumps(params)
     if full and res <= 32:
         rec['mask'] = np.array(wfs.mask)
         rec['tt'] = np.array(wfs.phaseBuffModulationLowres) if wfs.modulation != 0 else np.zeros((1, res, res), np.float32)
@@ -137,18 +155,27 @@ def case_small(OOPAO, name, res, n_subap, modulation, light_ratio, co=0.0, full=
           'nAct', rec['n_act'])
 
 
+CASES = [
+    ('tiny', (24, 4, 3, 0.5), {}),
+    ('tiny_nocenter', (24, 4, 2, 0.5), dict(psfCentering=False, n_im=0)),
+    ('tiny_rooftop', (24, 4, 2, 0.3), dict(rooftop=0.5, theta_rotation=0.1, nTheta_user_defined=8, n_im=0)),
+    ('tiny_nomod', (32, 4, 0, 0.2), dict(co=0.25, n_im=0, n_pix_separation=4)),
+    ('small_sep', (40, 10, 2, 0.5), dict(n_pix_separation=4, n_pix_edge=2, nTheta_user_defined=12, n_im=4)),
+    ('c1', (120, 20, 3, 0.5), dict(full=False, n_im=3, nTheta_user_defined=48)),
+    ('tiny_sf', (24, 4, 3, 0.5), dict(n_im=4, sf_radius=14)),
+    ('tiny_nocenter_sf', (24, 4, 2, 0.5), dict(psfCentering=False, n_im=4, sf_radius=12)),
+]
+
+
 def main():
+    """argv: [reference project root] [case names...] (default: every case)."""
     from refimport import import_reference
     ref_root = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+    only = set(sys.argv[2:])
     OOPAO = import_reference(ref_root)
-    case_small(OOPAO, 'tiny', 24, 4, 3, 0.5)
-    case_small(OOPAO, 'tiny_nocenter', 24, 4, 2, 0.5, psfCentering=False, n_im=0)
-    case_small(OOPAO, 'tiny_rooftop', 24, 4, 2, 0.3, rooftop=0.5, theta_rotation=0.1,
-               nTheta_user_defined=8, n_im=0)
-    case_small(OOPAO, 'tiny_nomod', 32, 4, 0, 0.2, co=0.25, n_im=0, n_pix_separation=4)
-    case_small(OOPAO, 'small_sep', 40, 10, 2, 0.5, n_pix_separation=4, n_pix_edge=2,
-               nTheta_user_defined=12, n_im=4)
-    case_small(OOPAO, 'c1', 120, 20, 3, 0.5, full=False, n_im=3, nTheta_user_defined=48)
+    for name, args, kw in CASES:
+        if not only or name in only:
+            case_small(OOPAO, name, *args, **kw)
 
 
 if __name__ == '__main__':

@@ -5,7 +5,7 @@ import os
 import numpy as np
 
 GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden')
-CASES = ['tiny', 'tiny_nocenter', 'tiny_rooftop', 'tiny_nomod', 'small_sep', 'c1']
+CASES = ['tiny', 'tiny_nocenter', 'tiny_rooftop', 'tiny_nomod', 'small_sep', 'c1', 'tiny_sf', 'tiny_nocenter_sf']
 
 
 def load(name):
@@ -23,4 +23,5 @@ def oracle_pyramid(d):
         p['res'], p['n_subap'], p['modulation'], p['light_ratio'], d['intensity'],
         n_pix_separation=p.get('n_pix_separation', 2), n_pix_edge=p.get('n_pix_edge'),
         psf_centering=p.get('psfCentering', True), n_theta_user=p.get('nTheta_user_defined'),
-        rooftop=p.get('rooftop', 0.0), theta_rotation=p.get('theta_rotation', 0.0))
+        rooftop=p.get('rooftop', 0.0), theta_rotation=p.get('theta_rotation', 0.0),
+        spatial_filter=d.get('spatial_filter'))

@@ -25,7 +25,7 @@ def _quiet():
 def build_system(d):
     import oopao_gb300 as og
     p = d['params']
-    kw = {k: v for k, v in p.items() if k not in ('res', 'n_subap', 'modulation', 'light_ratio', 'co')}
+    kw = {k: v for k, v in p.items() if k not in ('res', 'n_subap', 'modulation', 'light_ratio', 'co', 'sf_radius')}
     with _quiet():
         tel = og.Telescope(resolution=p['res'], diameter=8.0, samplingTime=1e-3, centralObstruction=p['co'])
         ngs = og.Source(optBand='V0', magnitude=8)
@@ -33,6 +33,8 @@ def build_system(d):
         dm = og.DeformableMirror(tel, nSubap=p['n_subap'], mechCoupling=0.35)
         wfs = og.Pyramid(nSubap=p['n_subap'], telescope=tel, modulation=p['modulation'],
                          lightRatio=p['light_ratio'], **kw)
+        if 'spatial_filter' in d:
+            wfs.spatialFilter = d['spatial_filter']
     return tel, ngs, dm, wfs
 
 
