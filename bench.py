@@ -162,6 +162,57 @@ def cl_rate(n_steps=2000):
             'tc_status': dm.tensor_core_status()}
 
 
+def cl_strehl(n_steps=500, n_oracle=100):
+    """Plain closed loop on the 20x20 configuration: 8 m, 120 px, modulation
+    3 l/D x 48 points, 21x21 DM, one frozen-flow von Karman layer (r0 0.15 m
+    at 500 nm, L0 25 m, 10 m/s), 300-mode KL-like integrator (gain 0.4,
+    delay 1, reconstructor from the batched IM and the FP64 SVD keeping 280
+    modes), `n_steps` frames at 1 kHz with the science PSF summed on the GPU.
+    The float64 oracle runs the first `n_oracle` frames of the same loop with
+    the same reconstructor; the error of the residual WFE trajectory, of the
+    long-exposure PSF and of its Strehl ratio over those frames is reported."""
+    import torch
+    from oopao_gb300.calibration import InteractionMatrix
+    from oopao_gb300.closed_loop import ClosedLoop, VonKarmanLayers
+    from oracle import pwfs_oracle as O
+    tel, ngs, dm, wfs = build_system(0)
+    m2c = kl_like_basis(dm.modes, tel.pupil, NMODES)
+    with _quiet():
+        calib = InteractionMatrix(ngs, tel, dm, wfs, m2c, STROKE, single_pass=False, nTrunc=NTRUNC)
+    R = m2c @ np.asarray(calib.Mtrunc)
+    layers = VonKarmanLayers(tel, r0=0.15, L0=25, windSpeed=(10.,), seed=0)
+    out = {'config': '20x20 PWFS, 120 px, N=264, 48 points, 21x21 DM, 1 layer r0 0.15 m, 300-mode integrator '
+                     'gain 0.4, %d frames' % n_steps}
+    for science in (False, True):
+        cl = ClosedLoop(tel, ngs, dm, wfs, R, gain=0.4, layers=layers, max_steps=n_steps + 10, science=science)
+        cl.capture()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        cl.run(n_oracle)
+        e1.record()
+        torch.cuda.synchronize()
+        key = 'with_science_psf' if science else 'wfs_only'
+        out['us_per_step_' + key] = e0.elapsed_time(e1) / n_oracle * 1000.0
+    wfe100, psf100, sr100 = cl.residual_wfe, cl.long_exposure_psf(), cl.long_exposure_strehl()
+    cl.run(n_steps - n_oracle)
+    torch.cuda.synchronize()
+    wfe = cl.residual_wfe
+    out.update({'strehl_le_pct': cl.long_exposure_strehl(), 'wfe_first_nm': float(wfe[0] * 1e9),
+                'wfe_mean_last_100_nm': float(wfe[-100:].mean() * 1e9)})
+    pup = O.telescope_pupil(RES)
+    inten = O.source_intensity(pup, O.n_photon('V0', 8), 1e-3, 8.0)
+    ow = O.build_pyramid(RES, NSUB, MOD, 0.5, inten, n_theta_user=NTHETA, workers=os.cpu_count())
+    t0 = time.perf_counter()
+    ref = O.closed_loop(ow, O.dm_modes(RES, 8.0, NSUB), R.astype(np.float64), lambda t: layers.opd(t, RES), pup,
+                        ngs.wavelength, 0.4, n_oracle, workers=os.cpu_count())
+    out['oracle'] = {'frames': n_oracle, 'seconds': time.perf_counter() - t0,
+                     'strehl_le_pct': ref['strehl_le'], 'gpu_strehl_le_pct': sr100,
+                     'strehl_rel_err': abs(sr100 - ref['strehl_le']) / ref['strehl_le'],
+                     'psf_le_rel_l2': O.rel_l2(psf100, ref['psf_le']),
+                     'wfe_rel_l2': O.rel_l2(wfe100, ref['wfe'])}
+    return out
+
+
 def dm_projection(peaks):
     """DM influence-function projection OPD = modes @ coefs at the 20x20,
     40x40 and 80x80 sizes: FP32 CUDA-core path vs BF16 tcgen05 path, per
@@ -497,6 +548,7 @@ def run_ours(args):
         extra['im_c3_1000'] = im_comparison(tel3, ngs3, dm3, wfs3, m2c3, n_per_mode=10)
         del tel3, ngs3, dm3, wfs3
         extra['cl_step'] = cl_rate()
+        extra['cl_strehl_20x20'] = cl_strehl()
         try:
             pk = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
         except Exception:

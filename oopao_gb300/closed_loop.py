@@ -7,6 +7,11 @@ One step follows ``tutorials/AO_closed_loop_Pyramid_WFS.py:601-639`` and
     ->  modulated pyramid frame  ->  slopes
     ->  coefs -= gain * reconstructor @ slopes       (frame delay 1 or 2)
     + residual wavefront RMS over the pupil (logged on the device)
+    + optionally the science PSF of the residual, summed into a long-exposure
+      image (``Telescope.computePSF`` with zero padding 2,
+      ``OOPAO/Telescope.py:251-420``; FFT by cuFFT through torch, a
+      diagnostic outside the WFS path), and its Strehl ratio by the OTF ratio
+      of ``strehlMeter`` (``OOPAO/tools/tools.py:102-157``)
 
 Every operation is a launch of ``liboopao_gb300`` on preallocated buffers; a
 device step counter carries the time index, so the captured graph is
@@ -78,9 +83,22 @@ class VonKarmanLayers:
         return out
 
 
+def strehl_meter(psf, psf_ref):
+    """Strehl ratio in percent from a focal-plane image and the image of a
+    flat wavefront of the same sampling: ratio of the sums of the
+    max-normalised OTF moduli (``strehlMeter``, OOPAO/tools/tools.py:102-157)."""
+    psf = np.asarray(psf, dtype=np.float64)
+    psf_ref = np.asarray(psf_ref, dtype=np.float64)
+    if psf.shape != psf_ref.shape:
+        raise OopaoError('strehl_meter: PSF and reference PSF must have the same shape')
+    otf = np.abs(np.fft.fftshift(np.fft.fft2(psf)))
+    otfa = np.abs(np.fft.fftshift(np.fft.fft2(psf_ref)))
+    return float(np.sum(otf / otf.max()) / np.sum(otfa / otfa.max()) * 100)
+
+
 class ClosedLoop:
     def __init__(self, tel, ngs, dm, wfs, reconstructor, gain=0.4, frame_delay=1, layers=None,
-                 max_steps=100000):
+                 max_steps=100000, science=False):
         if frame_delay not in (1, 2):
             raise OopaoError('frame_delay must be 1 or 2')
         self.tel, self.ngs, self.dm, self.wfs = tel, ngs, dm, wfs
@@ -128,6 +146,28 @@ class ClosedLoop:
             self._x0 = (N.ctypes.c_float * nl)(*c)
             self._vy = (N.ctypes.c_float * nl)(*np.float32(layers.vy))
             self._vx = (N.ctypes.c_float * nl)(*np.float32(layers.vx))
+        self._tc_ws = None
+        if getattr(dm, '_modes_bf16', None) is not None:
+            nb = N.load().oopao_dm_bf16_workspace_bytes(dm._n_act_pad, 1)
+            self._tc_ws = torch.zeros(nb, dtype=torch.uint8, device=d)
+            self._tc_nb = nb
+        self.science = bool(science)
+        if self.science:
+            # science camera of the NGS: zero padding 2 (N = 2 res), centring
+            # phasor exp(-i pi (N+1)/N (x+y)), EMF = fft2(E * phasor) / N
+            n2 = 2 * res
+            lo = (n2 - res) // 2
+            xx, yy = np.meshgrid(np.arange(n2), np.arange(n2))
+            ph = np.exp(-1j * np.pi * (n2 + 1) / n2 * (xx + yy))[lo:lo + res, lo:lo + res]
+            amp = np.sqrt(ngs.intensity) * tel.pupil
+            self._sci_field0 = torch.as_tensor((amp * ph / n2).astype(np.complex64), device=d)
+            self._sci_pad = torch.zeros((n2, n2), dtype=torch.complex64, device=d)
+            self._sci_lo = lo
+            self.psf_le = torch.zeros((n2, n2), dtype=torch.float64, device=d)
+            self._sci_pad[lo:lo + res, lo:lo + res] = self._sci_field0
+            f = torch.fft.fft2(self._sci_pad)
+            self.psf_ref = (f.real.double() ** 2 + f.imag.double() ** 2).cpu().numpy()
+            self._sci_pad.zero_()
         self.graph = None
 
     def reset(self):
@@ -135,6 +175,25 @@ class ClosedLoop:
         self.step_counter.zero_()
         self.s_prev.zero_()
         self.wfe.zero_()
+        if self.science:
+            self.psf_le.zero_()
+
+    def _science(self):
+        lo, res = self._sci_lo, self.res
+        e = self._sci_field0 * torch.exp(1j * (self.scale * self.opd[0]))
+        self._sci_pad[lo:lo + res, lo:lo + res] = e
+        f = torch.fft.fft2(self._sci_pad)
+        self.psf_le += f.real.double() ** 2 + f.imag.double() ** 2
+
+    def long_exposure_psf(self):
+        """Sum of the science PSFs of the steps run since the last reset."""
+        if not self.science:
+            raise OopaoError('ClosedLoop(science=True) is needed for the science PSF')
+        return self.psf_le.cpu().numpy()
+
+    def long_exposure_strehl(self):
+        """Strehl ratio (percent) of the long-exposure PSF."""
+        return strehl_meter(self.long_exposure_psf(), self.psf_ref)
 
     def _launch_step(self):
         st = N.stream_handle()
@@ -144,10 +203,16 @@ class ClosedLoop:
             N.call('oopao_cl_screen', len(self._scr), self._scr_ptr, self._h, self._w, self._y0, self._x0,
                    self._vy, self._vx, self.res, self.step_counter, self.opd_atm, st)
             base = self.opd_atm
-        N.call('oopao_dm_opd_acc_f32', dm._modes_t, self.coefs, dm.nValidAct, self.res * self.res, 1, 1.0, base,
-               self.opd, st)
+        if self._tc_ws is not None:
+            N.call('oopao_dm_opd_bf16', dm._modes_bf16, dm._n_act_pad, self.coefs, dm.nValidAct, self.res * self.res,
+                   1, 1.0, base, self.opd, self._tc_ws, self._tc_nb, st)
+        else:
+            N.call('oopao_dm_opd_acc_f32', dm._modes_t, self.coefs, dm.nValidAct, self.res * self.res, 1, 1.0,
+                   base, self.opd, st)
         N.call('oopao_cl_pupil_rms', self.opd, self.pupil_idx, self.pupil_idx.numel(), self.step_counter,
                self.wfe, self.max_steps, st)
+        if self.science:
+            self._science()
         N.call('oopao_pwfs_measure', self.plan.h, self.opd, self.scale, 1, self.frame, None, self.ws,
                self.ws_bytes, st)
         N.call('oopao_pwfs_signal', self.plan.h, self.frame, 1, self.s2d, self.s, None, st)

@@ -510,3 +510,64 @@ def rel_l2(a, b) -> float:
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+# ---------------------------------------------------------------------------
+# Closed loop and science image (float64)
+# ---------------------------------------------------------------------------
+
+def science_psf(opd: np.ndarray, intensity: np.ndarray, pupil: np.ndarray, wavelength: float) -> np.ndarray:
+    """On-axis ``Telescope.computePSF`` with zero padding 2 and an image of
+    2*res pixels (``OOPAO/Telescope.py:251-420``): the field
+    sqrt(I)*pupil*exp(i*2*pi*opd/lambda) zero-padded to N = 2 res (res/2 on
+    each side), times exp(-i*pi*(N+1)/N*(x+y)), EMF = fft2(.)/N, PSF = |EMF|^2."""
+    res = opd.shape[0]
+    n2 = 2 * res
+    lo = (n2 - res) // 2
+    xx, yy = np.meshgrid(np.arange(n2), np.arange(n2))
+    phasor = np.exp(-1j * np.pi * (n2 + 1) / n2 * (xx + yy))
+    sup = np.zeros((n2, n2), dtype=np.complex128)
+    sup[lo:lo + res, lo:lo + res] = np.sqrt(intensity) * pupil * np.exp(1j * 2 * np.pi / wavelength * opd)
+    emf = np.fft.fft2(sup * phasor) / n2
+    return np.abs(emf) ** 2
+
+
+def strehl_meter(psf: np.ndarray, psf_ref: np.ndarray) -> float:
+    """``strehlMeter`` (``OOPAO/tools/tools.py:102-157``) for images of equal
+    size: sum of the max-normalised |OTF| over that of the reference, in %."""
+    otf = np.abs(np.fft.fftshift(np.fft.fft2(psf)))
+    otfa = np.abs(np.fft.fftshift(np.fft.fft2(psf_ref)))
+    return float(np.sum(otf / np.max(otf)) / np.sum(otfa / np.max(otfa)) * 100)
+
+
+def closed_loop(wfs: OraclePyramid, modes: np.ndarray, reconstructor: np.ndarray, turbulence_opd,
+                pupil: np.ndarray, wavelength: float, gain: float, n_steps: int, frame_delay: int = 1,
+                science: bool = True, workers: int = 1) -> dict:
+    """The loop of ``tutorials/AO_closed_loop_Pyramid_WFS.py:601-639`` in
+    float64: at step t the residual OPD = turbulence_opd(t) + modes @ coefs;
+    its standard deviation over the pupil is logged; the sensor measures it;
+    coefs -= gain * R @ s_t (frame delay 1) or R @ s_{t-1} (delay 2).  With
+    ``science``, the science PSF of every residual is summed and the
+    long-exposure Strehl ratio is returned with the flat-wavefront PSF."""
+    res = pupil.shape[0]
+    coefs = np.zeros(modes.shape[1])
+    s_prev = np.zeros(reconstructor.shape[1])
+    ip = pupil > 0
+    wfe = np.zeros(n_steps)
+    psf_le = 0.0
+    for t in range(n_steps):
+        opd = turbulence_opd(t) + (modes @ coefs).reshape(res, res)
+        wfe[t] = np.std(opd[ip])
+        if science:
+            psf_le = psf_le + science_psf(opd, wfs.intensity, pupil, wavelength)
+        _, _, _, s = wfs.measure(opd * 2 * np.pi / wavelength, workers=workers)
+        if frame_delay == 1:
+            coefs = coefs - gain * reconstructor @ s
+        else:
+            coefs = coefs - gain * reconstructor @ s_prev
+            s_prev = s
+    out = {'wfe': wfe, 'coefs': coefs}
+    if science:
+        ref = science_psf(np.zeros((res, res)), wfs.intensity, pupil, wavelength)
+        out.update(psf_le=psf_le, psf_ref=ref, strehl_le=strehl_meter(psf_le, ref))
+    return out

@@ -90,3 +90,31 @@ def test_loop_converges_on_static_aberration(system):
     w = cl.residual_wfe
     assert len(w) == 30
     assert w[-1] < 0.35 * w[0], (w[0], w[-1])
+
+
+def test_long_exposure_strehl_vs_fp64_oracle(system):
+    """Graph-replayed FP32 loop against the float64 oracle loop (oracle IM,
+    float64 pseudo-inverse, same frozen-flow turbulence): residual WFE per
+    step, long-exposure PSF and its Strehl ratio within 1e-4 relative."""
+    import torch
+    from oopao_gb300.closed_loop import ClosedLoop, VonKarmanLayers
+    tel, ngs, dm, wfs, _ = system
+    res = tel.resolution
+    pup = O.telescope_pupil(res)
+    inten = O.source_intensity(pup, O.n_photon('V0', 8), 1e-3, 8.0)
+    ow = O.build_pyramid(res, 10, 2, 0.5, inten, n_pix_separation=4, n_pix_edge=2, n_theta_user=12, workers=4)
+    modes = O.dm_modes(res, 8.0, 10)
+    D = O.interaction_matrix(ow, modes, np.eye(modes.shape[1]), 1e-8, ngs.wavelength, pup, single_pass=False,
+                             workers=4)
+    R = np.linalg.pinv(D, rcond=1e-6)   # drops the modes the sensor does not see
+    layers = VonKarmanLayers(tel, r0=0.5, L0=25, windSpeed=(10.,), seed=5)
+    n = 60
+    cl = ClosedLoop(tel, ngs, dm, wfs, R, gain=0.4, layers=layers, max_steps=n + 5, science=True)
+    cl.run(n)
+    torch.cuda.synchronize()
+    wfe, psf, sr = cl.residual_wfe, cl.long_exposure_psf(), cl.long_exposure_strehl()
+    ref = O.closed_loop(ow, modes, R, lambda t: layers.opd(t, res), pup, ngs.wavelength, 0.4, n, workers=4)
+    assert ref['wfe'][-1] < 0.5 * ref['wfe'][0]          # the loop closes
+    assert O.rel_l2(wfe, ref['wfe']) < 1e-4
+    assert O.rel_l2(psf, ref['psf_le']) < 1e-4
+    assert abs(sr - ref['strehl_le']) < 1e-4 * ref['strehl_le']

@@ -127,7 +127,9 @@ def test_batched_phase_cube(system):
     for i in range(3):
         ngs ** tel
         wfs.wfs_measure(phase_in=cube[:, :, i])
-        assert rel(s_batch[:, i], wfs.signal) < 1e-6
+        # the slot split over modulation points depends on the batch size, so
+        # the FP32 sums are ordered differently: the FP32-path bound applies
+        assert rel(s_batch[:, i], wfs.signal) < 1e-5
     # and against the oracle
     wo = G.oracle_pyramid(d)
     _, _, _, s_or = wo.measure(cube)
