@@ -47,34 +47,54 @@ def _quiet():
 
 
 def kl_like_basis(modes, pupil, n_modes, diameter=8.0, r0=0.15, L0=25.0):
-    """Synthetic KL-like basis [n_act, n_modes]: eigenvectors of the von
-    Karman phase covariance sampled at the actuator footprints, each column
-    scaled to 1 m RMS OPD over the pupil.  Stands in for the reference's KL
-    basis (its computation is not on the measured path)."""
+    """Synthetic KL modal basis M2C [n_act, n_modes] in the DM space: the
+    von Karman phase covariance projected on the in-pupil influence
+    functions, P = F^T C_phi F, diagonalised in the pupil metric G = F^T F
+    (generalised eigenproblem P c = lambda G c, modes orthonormal over the
+    pupil, decreasing turbulence variance), each mode scaled to 1 m RMS OPD
+    over the pupil.  The construction of the reference's KL basis (covariance
+    diagonalised in the DM's pupil metric, OOPAO/calibration/ao_cockpit_psim.py:
+    649-736, HHt by FFT :847) restated for the bench inputs; the modes are not
+    on the measured path.  F^T C_phi F is computed by FFT convolution of
+    each influence function with the covariance kernel (torch on the GPU)."""
+    import scipy.linalg
+    import torch
     from scipy.special import gamma, kv
     res = pupil.shape[0]
     n_act = modes.shape[1]
     ipup = pupil.reshape(-1) > 0
-    w = modes[ipup]                                   # [npup, n_act]
-    x = (np.arange(res) - res / 2) * diameter / res
-    X, Y = np.meshgrid(x, x)
-    px, py = X.reshape(-1)[ipup], Y.reshape(-1)[ipup]
-    wsum = w.sum(axis=0)
-    cx, cy = (w * px[:, None]).sum(0) / wsum, (w * py[:, None]).sum(0) / wsum
-    r = np.hypot(cx[:, None] - cx[None], cy[:, None] - cy[None])
+    F = modes[ipup]                                   # [npup, n_act]
+    npup = F.shape[0]
+    n2 = 2 * res
+    dx = diameter / res
+    off = np.fft.fftfreq(n2, 1.0 / n2) * dx           # offsets 0..res-1, -res..-1 (pixels * dx)
+    r = np.hypot(off[:, None], off[None, :])
     k0 = 2 * np.pi / L0
     c = (L0 / r0) ** (5 / 3) * gamma(11 / 6) / (2 ** (5 / 6) * np.pi ** (8 / 3)) * \
         (24 / 5 * gamma(6 / 5)) ** (5 / 6)
-    rr = np.maximum(r, 1e-9)
-    cov = c * (k0 * rr) ** (5 / 6) * kv(5 / 6, k0 * rr)
-    cov[r < 1e-9] = c * gamma(5 / 6) / 2 ** (1 / 6)
-    ev, vec = np.linalg.eigh(cov)
-    vec = vec[:, np.argsort(ev)[::-1][:n_modes]]
-    # RMS over the pupil of w @ vec from the Gram matrix (no per-mode OPD maps)
-    npup = w.shape[0]
-    gram = w.T @ w
-    mean = (w.sum(axis=0) @ vec) / npup
-    msq = np.einsum('ij,ij->j', vec, gram @ vec) / npup
+    rr = np.maximum(r, 1e-12)
+    kern = c * (k0 * rr) ** (5 / 6) * kv(5 / 6, k0 * rr)
+    kern[r < 1e-12] = c * gamma(5 / 6) / 2 ** (1 / 6)
+    dev = 'cuda' if torch.cuda.is_available() else 'cpu'
+    kf = torch.fft.fft2(torch.as_tensor(kern, device=dev))
+    Fd = torch.as_tensor(F, device=dev)
+    ip = torch.as_tensor(np.flatnonzero(ipup), device=dev)
+    P = torch.empty((n_act, n_act), dtype=torch.float64, device=dev)
+    mt = torch.as_tensor(modes * pupil.reshape(-1, 1), device=dev)
+    for a0 in range(0, n_act, 64):
+        a1 = min(n_act, a0 + 64)
+        blk = torch.zeros((a1 - a0, n2, n2), dtype=torch.float64, device=dev)
+        blk[:, :res, :res] = mt[:, a0:a1].T.reshape(a1 - a0, res, res)
+        conv = torch.fft.ifft2(torch.fft.fft2(blk) * kf).real[:, :res, :res].reshape(a1 - a0, -1)
+        P[:, a0:a1] = Fd.T @ conv[:, ip].T
+    P = P.cpu().numpy()
+    P = 0.5 * (P + P.T)
+    G = F.T @ F
+    lam, vec = scipy.linalg.eigh(P, G)
+    # the largest-variance mode is the DM's piston, which no slope sees: left out
+    vec = vec[:, np.argsort(lam)[::-1][1:n_modes + 1]]
+    mean = (F.sum(axis=0) @ vec) / npup
+    msq = np.einsum('ij,ij->j', vec, G @ vec) / npup
     vec = vec / np.sqrt(np.maximum(msq - mean ** 2, 1e-300))[None]
     return np.ascontiguousarray(vec)
 
@@ -135,17 +155,24 @@ def im_comparison(tel, ngs, dm, wfs, m2c, n_per_mode, with_error=True):
 def cl_rate(n_steps=2000):
     """Graph-replayed closed-loop steps/s on the 40x40 configuration: 240 px,
     N=504, modulation 5 l/D x 96 points, 41x41 DM, 3 frozen-flow layers
-    (r0 0.12 m, L0 30 m, 10/15/20 m/s), gain 0.4, delay 1; BF16 tensor-core
-    IF projection with FP32 accumulation."""
+    (r0 0.12 m, L0 30 m, 10/15/20 m/s), 1000-mode KL integrator (gain 0.4,
+    delay 1, reconstructor M2C @ M from the JVP interaction matrix and its
+    full FP64 pseudo-inverse); BF16 tensor-core IF projection with FP32
+    accumulation.  Reports the replay rate and the residual of the loop."""
     import torch
+    from oopao_gb300.autodiff import jvp_interaction_matrix
+    from oopao_gb300.calibration import CalibrationVault
     from oopao_gb300.closed_loop import ClosedLoop, VonKarmanLayers
     from oopao_gb300 import autotune
     tel, ngs, dm, wfs = build_system(0, 240, 40, 5, 96, max_batch=16, if_dtype='bf16')
+    m2c = kl_like_basis(dm.modes, tel.pupil, 1000, r0=0.12, L0=30.0)
+    D = jvp_interaction_matrix(ngs, tel, dm, wfs, m2c).double().cpu().numpy()
+    with _quiet():
+        R = m2c @ np.asarray(CalibrationVault(D).M)
     autotune.tune_pyramid(wfs, batch=1)
     layers = VonKarmanLayers(tel, r0=0.12, L0=30, fractionalR0=(1 / 3, 1 / 3, 1 / 3), windSpeed=(10., 15., 20.),
                              windDirection=(0., 72., 144.), seed=0)
-    R = np.zeros((dm.nValidAct, wfs.nSignal), np.float32)
-    cl = ClosedLoop(tel, ngs, dm, wfs, R, gain=0.4, layers=layers, max_steps=n_steps + 10)
+    cl = ClosedLoop(tel, ngs, dm, wfs, R, gain=0.4, layers=layers, max_steps=n_steps + 30)
     cl.capture()
     cl.run(20)
     torch.cuda.synchronize()
@@ -156,18 +183,22 @@ def cl_rate(n_steps=2000):
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / n_steps
-    return {'config': '40x40 PWFS, 240 px, N=504, 96 points, 41x41 DM (%d act), 3 layers' % dm.nValidAct,
+    wfe = cl.residual_wfe
+    return {'config': '40x40 PWFS, 240 px, N=504, 96 points, 41x41 DM (%d act), 3 layers, 1000 KL modes'
+                      % dm.nValidAct,
             'steps': n_steps, 'us_per_step': ms * 1000.0, 'khz': 1.0 / ms,
             'graph': True, 'variant': int(N_variant(wfs)), 'dm': 'bf16 tcgen05',
-            'tc_status': dm.tensor_core_status()}
+            'tc_status': dm.tensor_core_status(), 'wfe_first_nm': float(wfe[0] * 1e9),
+            'wfe_mean_last_500_nm': float(wfe[-500:].mean() * 1e9)}
 
 
 def cl_strehl(n_steps=500, n_oracle=100):
     """Plain closed loop on the 20x20 configuration: 8 m, 120 px, modulation
     3 l/D x 48 points, 21x21 DM, one frozen-flow von Karman layer (r0 0.15 m
-    at 500 nm, L0 25 m, 10 m/s), 300-mode KL-like integrator (gain 0.4,
-    delay 1, reconstructor from the batched IM and the FP64 SVD keeping 280
-    modes), `n_steps` frames at 1 kHz with the science PSF summed on the GPU.
+    at 500 nm, L0 25 m, 10 m/s), 300-mode KL integrator (gain 0.4, delay 1,
+    reconstructor M2C @ M from the batched IM and its full FP64 pseudo-inverse,
+    as the reference tutorial builds it), `n_steps` frames at 1 kHz with the
+    science PSF summed on the GPU.
     The float64 oracle runs the first `n_oracle` frames of the same loop with
     the same reconstructor; the error of the residual WFE trajectory, of the
     long-exposure PSF and of its Strehl ratio over those frames is reported."""
@@ -178,8 +209,8 @@ def cl_strehl(n_steps=500, n_oracle=100):
     tel, ngs, dm, wfs = build_system(0)
     m2c = kl_like_basis(dm.modes, tel.pupil, NMODES)
     with _quiet():
-        calib = InteractionMatrix(ngs, tel, dm, wfs, m2c, STROKE, single_pass=False, nTrunc=NTRUNC)
-    R = m2c @ np.asarray(calib.Mtrunc)
+        calib = InteractionMatrix(ngs, tel, dm, wfs, m2c, STROKE, single_pass=False)
+    R = m2c @ np.asarray(calib.M)
     layers = VonKarmanLayers(tel, r0=0.15, L0=25, windSpeed=(10.,), seed=0)
     out = {'config': '20x20 PWFS, 120 px, N=264, 48 points, 21x21 DM, 1 layer r0 0.15 m, 300-mode integrator '
                      'gain 0.4, %d frames' % n_steps}
