@@ -105,6 +105,19 @@ int oopao_pwfs_measure(const oopao_pwfs_plan* plan, const float* opd, double pha
                        int batch, float* frame, float* raw, void* workspace,
                        size_t workspace_bytes, void* stream);
 
+/* oopao_pwfs_measure plus the focal-plane (modulation) camera image.
+ * Replaces the modulation_camera_em list of pyramid_transform
+ * (OOPAO/Pyramid.py:642: the focal field F/N of every modulation point) and
+ * its use by a focal-plane camera (Pyramid.__mul__ :1182-1190:
+ * sum over points of |F/N|^2).
+ * focal: device [batch][n_fft][n_fft] float32, overwritten; F is the focal
+ * field before the pyramid mask (after the 1-pixel-centring shift when
+ * psfCentering is off).  Summed with float atomics, so the last bits of
+ * focal depend on the order of the additions; frame and raw do not. */
+int oopao_pwfs_measure_focal(const oopao_pwfs_plan* plan, const float* opd, double phase_scale,
+                             int batch, float* frame, float* raw, float* focal, void* workspace,
+                             size_t workspace_bytes, void* stream);
+
 /* Allocation-free variant of oopao_pwfs_measure.  It has no counterpart in
  * the reference.  It is for callers that cannot allocate device memory while
  * they measure: a real-time control loop that forbids allocation once it

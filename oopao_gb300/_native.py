@@ -35,7 +35,9 @@ SIGNATURES = {
     'oopao_pwfs_workspace_bytes': (c_size_t, [c_void_p, c_int]),
     'oopao_pwfs_measure': (c_int, [c_void_p, c_void_p, c_double, c_int, c_void_p, c_void_p, c_void_p,
                                    c_size_t, c_void_p]),
-    'oopao_pwfs_measure_noalloc': (c_int, [c_void_p, c_void_p, c_double, c_int, c_void_p, c_void_p, c_void_p]),
+    'oopao_pwfs_measure_focal': (c_int, [c_void_p, c_void_p, c_double, c_int, c_void_p, c_void_p, c_void_p,
+                                         c_void_p, c_size_t, c_void_p]),
+    'oopao_pwfs_measure_noalloc':(c_int, [c_void_p, c_void_p, c_double, c_int, c_void_p, c_void_p, c_void_p]),
     'oopao_pwfs_set_profiling': (c_int, [c_void_p, c_int]),
     'oopao_pwfs_profile_read': (c_int, [c_void_p, c_void_p, c_void_p]),
     'oopao_pwfs_set_signal_processing': (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p,

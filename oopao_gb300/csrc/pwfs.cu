@@ -174,6 +174,10 @@ struct ColsArgs {
   const float2* colfac;  // [K][res] row-direction phasor of each point
   float2* z;             // [B][kp][n][n] for the points [k0, k0+kp)
   int res, n, k0, kp, ng, off, cols;
+  // focal-plane (modulation) camera: sum over points of |F_k|^2 * focal_scale
+  // into [B][n][n] (atomic adds), or null
+  float* focal;
+  float focal_scale;
 };
 
 __global__ void __launch_bounds__(kThreads) pwfs_cols(ColsArgs a) {
@@ -204,7 +208,10 @@ __global__ void __launch_bounds__(kThreads) pwfs_cols(ColsArgs a) {
   for (int idx = tid; idx < C * n; idx += blockDim.x) {
     const int c = idx % C;
     const int r = idx / C;
-    if (c0 + c < n) f[c * n + r] = cmul(f[c * n + r], a.mask[(size_t)r * n + c0 + c]);
+    if (c0 + c < n) {
+      if (a.focal) atomicAdd(a.focal + ((size_t)b * n + r) * n + c0 + c, a.focal_scale * cabs2(f[c * n + r]));
+      f[c * n + r] = cmul(f[c * n + r], a.mask[(size_t)r * n + c0 + c]);
+    }
   }
   __syncthreads();
   float2* gg = fft_lines<true>(f, other, a.fft, tw, C, n, tid, blockDim.x);
@@ -742,9 +749,29 @@ __global__ void pwfs_reduce_binned(const float* __restrict__ binned, float* __re
   frame[(size_t)b * cam2 + i] = s;
 }
 
+namespace {
+int measure_impl(const oopao_pwfs_plan* p, const float* opd, double phase_scale, int batch, float* frame,
+                 float* raw, float* focal, void* ws, size_t ws_bytes, void* stream);
+}  // namespace
+
 extern "C" int oopao_pwfs_measure(const oopao_pwfs_plan* p, const float* opd, double phase_scale,
                                   int batch, float* frame, float* raw, void* ws, size_t ws_bytes,
                                   void* stream) {
+  return measure_impl(p, opd, phase_scale, batch, frame, raw, nullptr, ws, ws_bytes, stream);
+}
+
+extern "C" int oopao_pwfs_measure_focal(const oopao_pwfs_plan* p, const float* opd, double phase_scale,
+                                        int batch, float* frame, float* raw, float* focal, void* ws,
+                                        size_t ws_bytes, void* stream) {
+  OOPAO_CHECK_ARG(p && focal, "NULL argument");
+  OOPAO_CHECK_ARG(batch >= 1, "batch must be >= 1");
+  OOPAO_CUDA_TRY(cudaMemsetAsync(focal, 0, sizeof(float) * (size_t)batch * p->n * p->n, (cudaStream_t)stream));
+  return measure_impl(p, opd, phase_scale, batch, frame, raw, focal, ws, ws_bytes, stream);
+}
+
+namespace {
+int measure_impl(const oopao_pwfs_plan* p, const float* opd, double phase_scale, int batch, float* frame,
+                 float* raw, float* focal, void* ws, size_t ws_bytes, void* stream) {
   OOPAO_CHECK_ARG(p && opd && frame && ws, "NULL argument");
   OOPAO_CHECK_ARG(batch >= 1, "batch must be >= 1");
   cudaStream_t st = (cudaStream_t)stream;
@@ -798,7 +825,8 @@ extern "C" int oopao_pwfs_measure(const oopao_pwfs_plan* p, const float* opd, do
       }
       mark(0);
       ColsArgs ca{p->fft, p->d_tw, p->d_mask, y, grouped ? p->d_group : nullptr, p->d_colfac, z,
-                  res, n, k0, kc, ng, p->off, p->cols_per_cta};
+                  res, n, k0, kc, ng, p->off, p->cols_per_cta,
+                  focal ? focal + (size_t)b0 * n * n : nullptr, (float)((double)n * n)};
       mark(1);
       if (f) {
         dim3 g2(ceil_div(n, f->l_cols), kc, bc);
@@ -837,6 +865,7 @@ extern "C" int oopao_pwfs_measure(const oopao_pwfs_plan* p, const float* opd, do
   OOPAO_CUDA_TRY(cudaGetLastError());
   return OOPAO_OK;
 }
+}  // namespace
 
 extern "C" int oopao_pwfs_set_signal_processing(oopao_pwfs_plan* p, int mode, int nq,
                                                 const int* quad_origin, const unsigned char* valid,

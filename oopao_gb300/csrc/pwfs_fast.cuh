@@ -195,6 +195,12 @@ __global__ void __launch_bounds__(T* L) pwfs_cols2(ColsArgs a) {
         v[m] = (m == 0) ? u : cmul(u, tw[m * R1 + j]);
       }
       dft<R2, false>(v);
+      if (a.focal && active) {
+        // focal-plane camera: |F|^2 of this point, row j + q*R1 of column c
+        float* fo = a.focal + (size_t)b * N * N + c;
+#pragma unroll
+        for (int q = 0; q < R2; q++) atomicAdd(fo + (size_t)(j + q * R1) * N, a.focal_scale * cabs2(v[q]));
+      }
 #pragma unroll
       for (int q = 0; q < R2; q++) {
         const float2 mq = active ? mk[(size_t)(j + q * R1) * N] : make_float2(0.f, 0.f);

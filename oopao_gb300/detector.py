@@ -68,6 +68,19 @@ class Detector:
             f = f * self.gain
         return f
 
+    def integrate(self, frame):
+        """``Detector.integrate`` + ``readout`` (OOPAO/Detector.py:331-354) for a
+        frame computed outside the WFS camera path (the focal-plane camera):
+        the frame is kept as ``perfect_frame``, then QE, noise and gain apply."""
+        self._unsupported()
+        self.perfect_frame = np.array(frame, dtype=np.float64)
+        if self.photonNoise or self.readoutNoise != 0 or self.QE != 1 or self.gain != 1:
+            dev = torch.device('cuda', torch.cuda.current_device())
+            t = torch.as_tensor(np.ascontiguousarray(frame, dtype=np.float32), device=dev)[None]
+            self._set_device_frame(self._integrate_device(t))
+        else:
+            self.frame = self.perfect_frame.copy()
+
     def _set_device_frame(self, t):
         self._frame_dev = t
         self._frame_host = None

@@ -394,7 +394,7 @@ class Pyramid:
     def _amplitude_key(self):
         return (id(self.src), self.src._intensity_version)
 
-    def _measure_frames(self, opd_dev, scale, plan=None, want_raw=False):
+    def _measure_frames(self, opd_dev, scale, plan=None, want_raw=False, want_focal=False):
         plan = plan or self.plan
         if self.src.intensity is None:
             raise OopaoError('No flux: propagate the source through the telescope first (src**tel)')
@@ -408,9 +408,49 @@ class Pyramid:
                           device=self._dev) if want_raw else None
         nb = plan.workspace_bytes(min(B, self.max_batch))
         ws = self._ws.get(nb)
+        if want_focal:
+            focal = torch.empty((B, self.resolution, self.resolution), dtype=torch.float32, device=self._dev)
+            N.call('oopao_pwfs_measure_focal', plan.h, N.ptr(x), float(scale), B, N.ptr(frame), N.ptr(raw),
+                   N.ptr(focal), N.ptr(ws), nb, N.stream_handle())
+            return frame, raw, focal
         N.call('oopao_pwfs_measure', plan.h, N.ptr(x), float(scale), B, N.ptr(frame), N.ptr(raw),
                N.ptr(ws), nb, N.stream_handle())
         return frame, raw
+
+    def focal_plane_image(self):
+        """Sum over modulation points of |F_k/N|^2 for the last measured wavefront
+        (the intensity the reference's focal-plane camera reads from
+        modulation_camera_em, OOPAO/Pyramid.py:642, :1182-1190), [N,N] float64.
+        In the 1-pixel-centred branch the field carries the spatial filter."""
+        last = getattr(self, '_last_measure', None)
+        if last is None:
+            raise OopaoError('No wavefront measured yet')
+        opd, scale = last
+        _, _, focal = self._measure_frames(opd, scale, want_focal=True)
+        img = focal[0] if opd.ndim == 2 else focal
+        if not self.psfCentering and self.spatialFilter is not None:
+            f = torch.as_tensor(np.abs(np.asarray(self.spatialFilter)) ** 2, dtype=torch.float32, device=self._dev)
+            img = img * f
+        a = img.double().cpu().numpy()
+        return np.moveaxis(a, 0, -1) if a.ndim == 3 else a
+
+    def get_modulation_frame(self, radius=6, norma=True):
+        """Zoom of the focal-plane camera frame on +-radius lambda/D
+        (OOPAO/Pyramid.py:928-944)."""
+        if radius <= 0:
+            warning('radius for the field of view must be a strictly positive number. Ignoring the input value.')
+            radius = self.telescope.resolution // 2
+        self.modulation_camera_frame = np.asarray(self.focal_plane_camera.frame, dtype=float)
+        n_trunc = int(self.resolution / 2 - radius * self.zeroPaddingFactor)
+        if n_trunc <= 0:
+            warning('radius Value is too high as the field of view is limited to ' + str(int(self.fov_l_d / 2)) +
+                    ' lambda/D -- ignoring')
+            zoom = self.modulation_camera_frame.copy()
+        else:
+            zoom = self.modulation_camera_frame[n_trunc:-n_trunc, n_trunc:-n_trunc]
+        if norma:
+            zoom = zoom / zoom.max()
+        return zoom
 
     def _select_valid(self, frame):
         """Valid pixels from a camera frame (OOPAO/Pyramid.py:557-579)."""
@@ -517,6 +557,7 @@ class Pyramid:
         else:
             opd, scale = self.src.device_opd(self._dev), 2 * np.pi / self.src.wavelength
         single = opd.ndim == 2
+        self._last_measure = (opd, scale)
         want_raw = self.keep_raw_data and (single or opd.shape[0] == 1)
         frame, raw = self._measure_frames(opd, scale, want_raw=want_raw)
         frame = self.cam._integrate_device(frame)
@@ -604,7 +645,22 @@ class Pyramid:
     def __mul__(self, obj):
         if obj.tag == 'detector':
             if obj.is_focal_plane_camera:
-                raise OopaoError('The focal-plane (modulation) camera is not provided by oopao_gb300')
+                # OOPAO/Pyramid.py:1182-1190: centred crop of the focal-plane
+                # intensity to the camera size, then the camera's integration
+                intensity = self.focal_plane_image()
+                if intensity.ndim == 3:
+                    intensity = intensity.sum(axis=2)
+                n = intensity.shape[0]
+                if obj.resolution > self.resolution:
+                    frame = intensity
+                    warning('Maximum resolution for focal plane camera is %i, cropping field to this dimension'
+                            % self.resolution)
+                else:
+                    h = obj.resolution // 2
+                    frame = intensity[n // 2 - h:n // 2 + h, n // 2 - h:n // 2 + h]
+                obj._integrated_time = getattr(obj, '_integrated_time', 0) + self.telescope.samplingTime
+                obj.integrate(frame)
+                return
             if obj is not self.cam:
                 raise OopaoError('Only the pyramid camera wfs.cam is supported')
             return

@@ -284,6 +284,29 @@ def pyramid_transform_stack(phase_pts: np.ndarray, amplitude: np.ndarray,
     return np.abs(G) ** 2
 
 
+def focal_plane_image(phase: np.ndarray, intensity: np.ndarray, tt: np.ndarray, geom: PyramidGeometry) -> np.ndarray:
+    """Intensity the focal-plane camera reads for a phase map: sum over the
+    modulation points of |F_k / N|^2, F_k the focal field of
+    ``pyramid_transform`` before the mask (``OOPAO/Pyramid.py:629-642``,
+    summed by ``Pyramid.__mul__`` ``:1182-1185``)."""
+    N, res, c = geom.N, geom.res, geom.center
+    lo = c - res // 2
+    K = tt.shape[0]
+    amp = np.sqrt(intensity / K)
+    out = np.zeros((N, N))
+    for k in range(K):
+        support = np.zeros((N, N), dtype=np.complex128)
+        support[lo:lo + res, lo:lo + res] = amp * np.exp(1j * (phase + tt[k].astype(np.float64)))
+        if geom.psf_centering:
+            F = scipy.fft.fft2(support * geom.phasor)
+        else:
+            F = np.fft.fftshift(scipy.fft.fft2(support))
+            if geom.spatial_filter is not None:
+                F = F * geom.spatial_filter
+        out += np.abs(F / N) ** 2
+    return out
+
+
 def wfs_raw(phase: np.ndarray, intensity: np.ndarray, tt: np.ndarray, geom: PyramidGeometry,
             weight_vector=None, workers: int = 1, chunk: int = 16) -> np.ndarray:
     """``raw_data`` for one phase map or a cube [res,res,B].

@@ -61,9 +61,13 @@ def measure_dm(tel, ngs, dm, wfs, coefs):
     with _quiet():
         dm.coefs = coefs
         ngs ** tel * dm * wfs
+        # focal-plane (modulation) camera of the same measurement
+        wfs * wfs.focal_plane_camera
     return dict(raw=np.array(wfs.raw_data), frame=np.array(wfs.cam.frame),
                 signal=np.array(wfs.signal), signal_2D=np.array(wfs.signal_2D),
-                phase=np.array(ngs.phase))
+                phase=np.array(ngs.phase),
+                focal=np.sum(np.abs(np.asarray(wfs.modulation_camera_em)) ** 2, axis=0),
+                focal_cam=np.array(wfs.focal_plane_camera.frame))
 
 
 def measure_phase(tel, ngs, dm, wfs, phase):

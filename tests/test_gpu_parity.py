@@ -84,6 +84,20 @@ def test_dm_path(system):
     assert rel(wfs.signal, d['dm_signal']) < TOL_FP32
 
 
+def test_focal_plane_camera(system):
+    """``wfs * wfs.focal_plane_camera`` after the DM measurement: the summed
+    |F/N|^2 of the modulation points and the camera's centred crop."""
+    name, d, (tel, ngs, dm, wfs) = system
+    dm.coefs = d['dm_coefs']
+    ngs ** tel * dm * wfs
+    assert rel(wfs.focal_plane_image(), d['dm_focal']) < TOL_FP32
+    wfs * wfs.focal_plane_camera
+    assert wfs.focal_plane_camera.frame.shape == d['dm_focal_cam'].shape
+    assert rel(wfs.focal_plane_camera.frame, d['dm_focal_cam']) < TOL_FP32
+    # the signal of the measurement is unchanged by the extra propagation
+    assert rel(wfs.signal, d['dm_signal']) < TOL_FP32
+
+
 def test_screen_path(system):
     name, d, (tel, ngs, dm, wfs) = system
     dm.coefs = 0

@@ -79,6 +79,18 @@ def test_dm_path(case):
     assert O.rel_l2(s, d['dm_signal']) < TOL
 
 
+def test_focal_plane_camera(case):
+    """Sum over points of |F/N|^2 (modulation_camera_em) and the focal-plane
+    camera frame (its centred crop) of the DM measurement."""
+    name, d, wfs = case
+    img = O.focal_plane_image(d['dm_phase'], wfs.intensity, wfs.tt, wfs.geom)
+    assert O.rel_l2(img, d['dm_focal']) < TOL
+    n, m = img.shape[0], d['dm_focal_cam'].shape[0]
+    if m <= n:
+        crop = img[n // 2 - m // 2:n // 2 + m // 2, n // 2 - m // 2:n // 2 + m // 2]
+        assert O.rel_l2(crop, d['dm_focal_cam']) < TOL
+
+
 def test_screen_path(case):
     name, d, wfs = case
     raw, frame, s2d, s = wfs.measure(d['screen_phase'])
