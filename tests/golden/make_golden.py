@@ -159,6 +159,42 @@ def case_small(OOPAO, name, res, n_subap, modulation, light_ratio, co=0.0, full=
           'nAct', rec['n_act'])
 
 
+ATM_CASE = dict(res=32, diameter=8.0, r0=0.15, L0=25.0, fractionalR0=[0.5, 0.3, 0.2],
+                windSpeed=[10.0, 370.0, 300.0], windDirection=[0.0, 135.0, 30.0],
+                altitude=[0.0, 5000.0, 10000.0], steps=40)
+
+
+def case_atmosphere(OOPAO, name='atm_small', **p):
+    """Infinite-screen atmosphere: OPD seen by an on-axis NGS after each of
+    `steps` updates (the wind speeds are large so that every branch of the
+    integer-step logic of updateLayer runs: axis-aligned sub-pixel drift, a
+    diagonal layer moving more than one pixel per step, unequal components)."""
+    import json
+    from OOPAO.Atmosphere import Atmosphere
+    from OOPAO.Source import Source
+    from OOPAO.Telescope import Telescope
+    p = dict(ATM_CASE, **p)
+    with _quiet():
+        tel = Telescope(resolution=p['res'], diameter=p['diameter'], samplingTime=1e-3)
+        ngs = Source(optBand='V0', magnitude=8)
+        ngs * tel
+        atm = Atmosphere(telescope=tel, r0=p['r0'], L0=p['L0'], fractionalR0=p['fractionalR0'],
+                         windSpeed=p['windSpeed'], windDirection=p['windDirection'], altitude=p['altitude'])
+        atm.initializeAtmosphere(tel)
+        opds = []
+        ngs ** atm * tel
+        opds.append(np.array(ngs.OPD_no_pupil))
+        for _ in range(p['steps']):
+            atm.update()
+            ngs ** atm * tel
+            opds.append(np.array(ngs.OPD_no_pupil))
+    layer = atm.layer_1
+    rec = dict(params=json.dumps(p), opd=np.stack(opds), A=np.array(layer.A), B=np.array(layer.B),
+               screen0=np.array(atm.layer_1.initial_OPD))
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **rec)
+    print(name, 'steps', p['steps'], 'A', layer.A.shape, 'B', layer.B.shape)
+
+
 CASES = [
     ('tiny', (24, 4, 3, 0.5), {}),
     ('tiny_nocenter', (24, 4, 2, 0.5), dict(psfCentering=False, n_im=0)),
@@ -180,6 +216,8 @@ def main():
     for name, args, kw in CASES:
         if not only or name in only:
             case_small(OOPAO, name, *args, **kw)
+    if not only or 'atm_small' in only:
+        case_atmosphere(OOPAO)
 
 
 if __name__ == '__main__':

@@ -70,7 +70,10 @@ def import_reference(ref_root='/root/reference', work='/tmp/OOPAO_refcopy'):
         if name not in sys.modules:
             sys.modules[name] = _StubModule(name)
     sys.modules['astropy.io'].fits = sys.modules['astropy.io.fits']
-    sys.modules['skimage'].transform = sys.modules['skimage.transform']
+    # the atmosphere's sub-pixel shift needs a working warp (see skimage_emulation)
+    import skimage_emulation
+    sys.modules['skimage.transform'] = skimage_emulation
+    sys.modules['skimage'].transform = skimage_emulation
     sys.modules['matplotlib'].pyplot = sys.modules['matplotlib.pyplot']
     sys.modules['matplotlib'].gridspec = sys.modules['matplotlib.gridspec']
     if work not in sys.path:
