@@ -224,6 +224,28 @@ int oopao_cl_integrate(const float* R, const float* s, int n_act, int n_sig, flo
 int oopao_cl_pupil_rms(const float* opd, const int* idx, int npup, const int* step, float* out, int out_len,
                        void* stream);
 
+/* One update of the infinite-phase-screen atmosphere and its OPD for an
+ * on-axis source.  Replaces Atmosphere.update -> updateLayer / add_row
+ * (OOPAO/Atmosphere.py:410-531) and fill_OPD_support (:589-622).
+ * maps: device float64 [2][n_layers][n][n] ping-pong phase maps (radians,
+ *   n = res + 6); the current maps are in the first half on entry and exit.
+ * sched: device [n_steps][n_layers][slots] entries {active, dx, dy,
+ *   normal row} of int32: the one-pixel moves (add_row) of each step, at most
+ *   `slots` (even) per step; buff: device float64 [n_steps][n_layers][2]
+ *   sub-pixel offsets (x, y) after each step, or NULL for the unshifted maps.
+ * A [n_outer][n_inner], B [n_outer][n_outer]: float64 extrusion matrices;
+ *   inner_idx / outer_idx: map indices of the Z and X rings; normals:
+ *   float64 [rows][n_outer] drawn by the host.
+ * range: device float64 [n_layers][2] scratch (value range of each map);
+ * scale: device float64 [n_layers] = lambda/2pi * sqrt(fractional r0);
+ * opd: device float32 [res][res] output; step: device int32, the step whose
+ *   entries are used, incremented at the end when `advance`; err: device
+ *   int32 set to 1 when *step is outside [0, n_steps) (nothing moves then). */
+int oopao_atm_update(double* maps, int n_layers, int n, int slots, const void* sched, const double* buff,
+                     int n_steps, const double* A, const double* B, const int* inner_idx, const int* outer_idx,
+                     int n_inner, int n_outer, const double* normals, double* range, const double* scale, int res,
+                     float* opd, int* step, int advance, int* err, void* stream);
+
 /* Adjoint of the projection (no reference counterpart; used by the
  * gradients of wfs.signal with respect to dm.coefs):
  * out[a][b] = scale * sum_p modes_t[a][p] * g[b][p];

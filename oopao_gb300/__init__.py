@@ -20,6 +20,7 @@ from .detector import Detector
 from .deformable_mirror import DeformableMirror
 from .pyramid import Pyramid
 from .calibration import InteractionMatrix, CalibrationVault
+from .atmosphere import Atmosphere
 
 __all__ = ['OopaoError', 'warning', 'Source', 'Telescope', 'Detector', 'DeformableMirror', 'Pyramid',
-           'InteractionMatrix', 'CalibrationVault']
+           'InteractionMatrix', 'CalibrationVault', 'Atmosphere']

@@ -135,7 +135,15 @@ class ClosedLoop:
         self.ws_bytes = plan.workspace_bytes(1)
         self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=d)
         self.layers = layers
-        if layers is not None:
+        self._atm = None
+        if layers is not None and hasattr(layers, 'prepare'):
+            # infinite-screen Atmosphere: plan the whole horizon, then its
+            # device update is one more part of the captured step
+            self._atm = layers
+            layers.reset_state()
+            layers.prepare(max_steps + 1)
+            self._atm_opd = layers.device_opd().view(1, res, res)
+        elif layers is not None:
             self._scr = [torch.as_tensor(s, device=d) for s in layers.screens]
             nl = len(self._scr)
             self._scr_ptr = (N.c_void_p * nl)(*[t.data_ptr() for t in self._scr])
@@ -177,6 +185,8 @@ class ClosedLoop:
         self.wfe.zero_()
         if self.science:
             self.psf_le.zero_()
+        if self._atm is not None:
+            self._atm.reset_state()
 
     def _science(self):
         lo, res = self._sci_lo, self.res
@@ -199,7 +209,10 @@ class ClosedLoop:
         st = N.stream_handle()
         dm, wfs = self.dm, self.wfs
         base = None
-        if self.layers is not None:
+        if self._atm is not None:
+            self._atm._launch(advance=True)
+            base = self._atm_opd
+        elif self.layers is not None:
             N.call('oopao_cl_screen', len(self._scr), self._scr_ptr, self._h, self._w, self._y0, self._x0,
                    self._vy, self._vx, self.res, self.step_counter, self.opd_atm, st)
             base = self.opd_atm
@@ -242,6 +255,8 @@ class ClosedLoop:
         with torch.cuda.graph(g):
             self._launch_step()
         self.graph = g
+        if self._atm is not None:
+            self._atm._frozen = True
         self.reset()
         torch.cuda.synchronize()
         return g

@@ -1,0 +1,216 @@
+// Infinite-phase-screen atmosphere on the GPU (frozen flow with ring
+// extrusion), the per-step part of OOPAO/Atmosphere.py updateLayer / add_row
+// (:410-531) and fill_OPD_support (:589-622) for an on-axis source.
+//
+// Every layer keeps its phase map (radians, float64, n x n with n = res + 6)
+// in two ping-pong buffers.  The host precomputes, for every step, the
+// integer one-pixel moves of each layer (the reference's add_row calls, at
+// most `slots` per step) and the sub-pixel offset left in its buffer, and
+// draws the extrusion normals from each layer's RandomState; the kernels read
+// the entries of the step held in a device counter, so the same launches
+// serve eager updates and a captured CUDA graph.
+//
+//   atm_shift    one add_row slot: interior one-pixel move (or plain copy
+//                when the slot is idle), map[s%2] -> map[(s+1)%2]
+//   atm_extrude  the new outer ring X = A Z + B w (float64), Z = the inner
+//                ring of the moved interior
+//   atm_minmax   value range of each map (the clip of the cubic warp)
+//   atm_opd      bicubic (Keys, a = -0.5) sub-pixel shift of every layer,
+//                clipped, cropped to the pupil footprint, scaled by
+//                lambda/2pi * sqrt(fractional r0) and summed -> OPD [res][res]
+#include <cfloat>
+
+#include "common.cuh"
+
+namespace {
+
+struct AtmEntry {
+  int active, dx, dy, normal;  // move (dx, dy) of the slot; row of its normals
+};
+
+__device__ __forceinline__ int atm_step(const int* step, int n_steps, int* err) {
+  const int t = *step;
+  if (t < 0 || t >= n_steps) {
+    if (err) atomicExch(err, 1);
+    return -1;
+  }
+  return t;
+}
+
+__global__ void atm_shift(const double* __restrict__ src, double* __restrict__ dst, const AtmEntry* __restrict__ sched,
+                          const int* step, int n_steps, int slots, int slot, int n_layers, int n, int* err) {
+  const int l = blockIdx.y;
+  const int t = atm_step(step, n_steps, err);
+  const size_t nn = (size_t)n * n;
+  const double* s = src + l * nn;
+  double* d = dst + l * nn;
+  AtmEntry e{0, 0, 0, 0};
+  if (t >= 0) e = sched[((size_t)t * n_layers + l) * slots + slot];
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += (size_t)gridDim.x * blockDim.x) {
+    const int y = (int)(i / n), x = (int)(i % n);
+    const bool interior = y > 0 && y < n - 1 && x > 0 && x < n - 1;
+    if (e.active && interior) {
+      // output (y, x) reads input (y - dy, x - dx): one-pixel translation
+      d[i] = s[(size_t)(y - e.dy) * n + (x - e.dx)];
+    } else {
+      d[i] = s[i];
+    }
+  }
+}
+
+// one warp per ring pixel: X[o] = sum_i A[o][i] Z[i] + sum_j B[o][j] w[j]
+__global__ void atm_extrude(double* __restrict__ map, const double* __restrict__ A, const double* __restrict__ B,
+                            const int* __restrict__ inner_idx, const int* __restrict__ outer_idx,
+                            const double* __restrict__ normals, const AtmEntry* __restrict__ sched, const int* step,
+                            int n_steps, int slots, int slot, int n_layers, int n, int n_inner, int n_outer,
+                            int* err) {
+  extern __shared__ double z[];
+  const int l = blockIdx.y;
+  const int t = atm_step(step, n_steps, err);
+  if (t < 0) return;
+  const AtmEntry e = sched[((size_t)t * n_layers + l) * slots + slot];
+  if (!e.active) return;
+  double* m = map + (size_t)l * n * n;
+  for (int i = threadIdx.x; i < n_inner; i += blockDim.x) z[i] = m[inner_idx[i]];
+  __syncthreads();
+  const double* w = normals + (size_t)e.normal * n_outer;
+  const int warps = blockDim.x >> 5, lane = threadIdx.x & 31;
+  for (int o = blockIdx.x * warps + (threadIdx.x >> 5); o < n_outer; o += gridDim.x * warps) {
+    const double* a = A + (size_t)o * n_inner;
+    const double* b = B + (size_t)o * n_outer;
+    double acc = 0.0;
+    for (int i = lane; i < n_inner; i += 32) acc = fma(a[i], z[i], acc);
+    for (int j = lane; j < n_outer; j += 32) acc = fma(b[j], w[j], acc);
+    for (int s = 16; s > 0; s >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, s);
+    if (lane == 0) m[outer_idx[o]] = acc;
+  }
+}
+
+__global__ void atm_minmax(const double* __restrict__ map, double* __restrict__ range, int n) {
+  __shared__ double lo_s[32], hi_s[32];
+  const int l = blockIdx.x;
+  const double* m = map + (size_t)l * n * n;
+  double lo = DBL_MAX, hi = -DBL_MAX;
+  for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
+    lo = fmin(lo, m[i]);
+    hi = fmax(hi, m[i]);
+  }
+  for (int s = 16; s > 0; s >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, s));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, s));
+  }
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    lo_s[wid] = lo;
+    hi_s[wid] = hi;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+    lo = lane < nw ? lo_s[lane] : DBL_MAX;
+    hi = lane < nw ? hi_s[lane] : -DBL_MAX;
+    for (int s = 16; s > 0; s >>= 1) {
+      lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, s));
+      hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, s));
+    }
+    if (lane == 0) {
+      range[2 * l] = lo;
+      range[2 * l + 1] = hi;
+    }
+  }
+}
+
+// Keys cubic convolution of f at offset x in [0, 1) from f1
+__device__ __forceinline__ double keys(double x, double f0, double f1, double f2, double f3) {
+  return f1 + 0.5 * x * (f2 - f0 + x * (2.0 * f0 - 5.0 * f1 + 4.0 * f2 - f3 + x * (3.0 * (f1 - f2) + f3 - f0)));
+}
+
+__device__ __forceinline__ double map_at(const double* m, int n, int r, int c) {
+  return (r >= 0 && r < n && c >= 0 && c < n) ? m[(size_t)r * n + c] : 0.0;
+}
+
+__global__ void atm_opd(const double* __restrict__ map, const double* __restrict__ range,
+                        const double2* __restrict__ buff, const int* step, int n_steps, int use_buff,
+                        const double* __restrict__ scale, int n_layers, int n, int res, int off, float* __restrict__ opd,
+                        int* err) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= res * res) return;
+  int t = -1;
+  if (use_buff) {
+    t = atm_step(step, n_steps, err);
+    if (t < 0) return;
+  }
+  const int y = p / res, x = p % res;
+  double acc = 0.0;
+  for (int l = 0; l < n_layers; l++) {
+    const double* m = map + (size_t)l * n * n;
+    double tx = 0.0, ty = 0.0;
+    if (use_buff) {
+      const double2 b = buff[(size_t)t * n_layers + l];
+      tx = b.x;
+      ty = b.y;
+    }
+    // output pixel (r, c) of the warped map reads (r - ty, c - tx); the OPD
+    // crop starts `off` pixels into the map
+    const double rr = (double)(y + off) - ty, cc = (double)(x + off) - tx;
+    const double fr = floor(rr), fc = floor(cc);
+    const int r0 = (int)fr, c0 = (int)fc;
+    const double xr = rr - fr, xc = cc - fc;
+    double rows[4];
+#pragma unroll
+    for (int pr = 0; pr < 4; pr++) {
+      const int r = r0 + pr - 1;
+      rows[pr] = keys(xc, map_at(m, n, r, c0 - 1), map_at(m, n, r, c0), map_at(m, n, r, c0 + 1),
+                      map_at(m, n, r, c0 + 2));
+    }
+    double v = keys(xr, rows[0], rows[1], rows[2], rows[3]);
+    v = fmin(fmax(v, range[2 * l]), range[2 * l + 1]);
+    acc += v * scale[l];
+  }
+  opd[p] = (float)acc;
+}
+
+__global__ void atm_advance(int* step) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *step += 1;
+}
+
+}  // namespace
+
+extern "C" int oopao_atm_update(double* maps, int n_layers, int n, int slots, const void* sched, const double* buff,
+                                int n_steps, const double* A, const double* B, const int* inner_idx,
+                                const int* outer_idx, int n_inner, int n_outer, const double* normals,
+                                double* range, const double* scale, int res, float* opd, int* step, int advance,
+                                int* err, void* stream) {
+  OOPAO_CHECK_ARG(maps && scale && opd && step && range, "NULL argument");
+  OOPAO_CHECK_ARG(n_layers > 0 && n >= 8 && res > 0 && res <= n - 6 && slots >= 0 && slots % 2 == 0,
+                  "bad sizes (n >= res + 6, an even number of slots)");
+  OOPAO_CHECK_ARG(slots == 0 || (sched && A && B && inner_idx && outer_idx && normals && n_inner > 0 && n_outer > 0),
+                  "moving layers need the schedule, A, B, ring indices and normals");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t nn = (size_t)n * n;
+  const AtmEntry* e = reinterpret_cast<const AtmEntry*>(sched);
+  double* buf[2] = {maps, maps + (size_t)n_layers * nn};
+  int launches = 0;
+  for (int s = 0; s < slots; s++) {
+    const dim3 g1((unsigned)ceil_div((int)nn, 256), n_layers);
+    atm_shift<<<g1, 256, 0, st>>>(buf[s & 1], buf[(s + 1) & 1], e, step, n_steps, slots, s, n_layers, n, err);
+    const dim3 g2((unsigned)ceil_div(n_outer, 8), n_layers);
+    atm_extrude<<<g2, 256, sizeof(double) * n_inner, st>>>(buf[(s + 1) & 1], A, B, inner_idx, outer_idx, normals, e,
+                                                          step, n_steps, slots, s, n_layers, n, n_inner, n_outer,
+                                                          err);
+    launches += 2;
+  }
+  atm_minmax<<<n_layers, 512, 0, st>>>(maps, range, n);
+  const int off = (n - res) / 2;  // crop of the warped map: [1:-1] then the pupil footprint
+  atm_opd<<<ceil_div(res * res, 256), 256, 0, st>>>(maps, range, reinterpret_cast<const double2*>(buff), step,
+                                                   n_steps, buff != nullptr ? 1 : 0, scale, n_layers, n, res, off,
+                                                   opd, err);
+  launches += 2;
+  if (advance) {
+    atm_advance<<<1, 32, 0, st>>>(step);
+    launches += 1;
+  }
+  oopao_count_launches(launches);
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}
