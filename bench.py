@@ -154,15 +154,17 @@ def im_comparison(tel, ngs, dm, wfs, m2c, n_per_mode, with_error=True):
 
 def cl_rate(n_steps=2000):
     """Graph-replayed closed-loop steps/s on the 40x40 configuration: 240 px,
-    N=504, modulation 5 l/D x 96 points, 41x41 DM, 3 frozen-flow layers
-    (r0 0.12 m, L0 30 m, 10/15/20 m/s), 1000-mode KL integrator (gain 0.4,
+    N=504, modulation 5 l/D x 96 points, 41x41 DM, 3-layer infinite phase
+    screens (r0 0.12 m, L0 30 m, 0/5/10 km, 10/15/20 m/s, updated on the GPU
+    inside the captured step), 1000-mode KL integrator (gain 0.4,
     delay 1, reconstructor M2C @ M from the JVP interaction matrix and its
     full FP64 pseudo-inverse); BF16 tensor-core IF projection with FP32
     accumulation.  Reports the replay rate and the residual of the loop."""
     import torch
     from oopao_gb300.autodiff import jvp_interaction_matrix
     from oopao_gb300.calibration import CalibrationVault
-    from oopao_gb300.closed_loop import ClosedLoop, VonKarmanLayers
+    from oopao_gb300 import Atmosphere
+    from oopao_gb300.closed_loop import ClosedLoop
     from oopao_gb300 import autotune
     tel, ngs, dm, wfs = build_system(0, 240, 40, 5, 96, max_batch=16, if_dtype='bf16')
     m2c = kl_like_basis(dm.modes, tel.pupil, 1000, r0=0.12, L0=30.0)
@@ -170,9 +172,11 @@ def cl_rate(n_steps=2000):
     with _quiet():
         R = m2c @ np.asarray(CalibrationVault(D).M)
     autotune.tune_pyramid(wfs, batch=1)
-    layers = VonKarmanLayers(tel, r0=0.12, L0=30, fractionalR0=(1 / 3, 1 / 3, 1 / 3), windSpeed=(10., 15., 20.),
-                             windDirection=(0., 72., 144.), seed=0)
-    cl = ClosedLoop(tel, ngs, dm, wfs, R, gain=0.4, layers=layers, max_steps=n_steps + 30)
+    with _quiet():
+        atm = Atmosphere(telescope=tel, r0=0.12, L0=30, fractionalR0=[1 / 3, 1 / 3, 1 / 3],
+                         windSpeed=[10., 15., 20.], windDirection=[0., 72., 144.], altitude=[0., 5000., 10000.])
+        atm.initializeAtmosphere(tel)
+    cl = ClosedLoop(tel, ngs, dm, wfs, R, gain=0.4, layers=atm, max_steps=n_steps + 30)
     cl.capture()
     cl.run(20)
     torch.cuda.synchronize()
@@ -184,7 +188,8 @@ def cl_rate(n_steps=2000):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / n_steps
     wfe = cl.residual_wfe
-    return {'config': '40x40 PWFS, 240 px, N=504, 96 points, 41x41 DM (%d act), 3 layers, 1000 KL modes'
+    return {'config': '40x40 PWFS, 240 px, N=504, 96 points, 41x41 DM (%d act), 3 infinite-screen layers, '
+                      '1000 KL modes'
                       % dm.nValidAct,
             'steps': n_steps, 'us_per_step': ms * 1000.0, 'khz': 1.0 / ms,
             'graph': True, 'variant': int(N_variant(wfs)), 'dm': 'bf16 tcgen05',
@@ -194,8 +199,9 @@ def cl_rate(n_steps=2000):
 
 def cl_strehl(n_steps=500, n_oracle=100):
     """Plain closed loop on the 20x20 configuration: 8 m, 120 px, modulation
-    3 l/D x 48 points, 21x21 DM, one frozen-flow von Karman layer (r0 0.15 m
-    at 500 nm, L0 25 m, 10 m/s), 300-mode KL integrator (gain 0.4, delay 1,
+    3 l/D x 48 points, 21x21 DM, one infinite-screen von Karman layer (r0
+    0.15 m at 500 nm, L0 25 m, 10 m/s, the reference's seeds), 300-mode KL
+    integrator (gain 0.4, delay 1,
     reconstructor M2C @ M from the batched IM and its full FP64 pseudo-inverse,
     as the reference tutorial builds it), `n_steps` frames at 1 kHz with the
     science PSF summed on the GPU.
@@ -204,14 +210,18 @@ def cl_strehl(n_steps=500, n_oracle=100):
     long-exposure PSF and of its Strehl ratio over those frames is reported."""
     import torch
     from oopao_gb300.calibration import InteractionMatrix
-    from oopao_gb300.closed_loop import ClosedLoop, VonKarmanLayers
+    from oopao_gb300 import Atmosphere
+    from oopao_gb300.closed_loop import ClosedLoop
+    from oracle import atm_oracle as A
     from oracle import pwfs_oracle as O
     tel, ngs, dm, wfs = build_system(0)
     m2c = kl_like_basis(dm.modes, tel.pupil, NMODES)
     with _quiet():
         calib = InteractionMatrix(ngs, tel, dm, wfs, m2c, STROKE, single_pass=False)
+        layers = Atmosphere(telescope=tel, r0=0.15, L0=25, fractionalR0=[1.0], windSpeed=[10.], windDirection=[0.],
+                            altitude=[0.])
+        layers.initializeAtmosphere(tel)
     R = m2c @ np.asarray(calib.M)
-    layers = VonKarmanLayers(tel, r0=0.15, L0=25, windSpeed=(10.,), seed=0)
     out = {'config': '20x20 PWFS, 120 px, N=264, 48 points, 21x21 DM, 1 layer r0 0.15 m, 300-mode integrator '
                      'gain 0.4, %d frames' % n_steps}
     for science in (False, True):
@@ -234,7 +244,13 @@ def cl_strehl(n_steps=500, n_oracle=100):
     inten = O.source_intensity(pup, O.n_photon('V0', 8), 1e-3, 8.0)
     ow = O.build_pyramid(RES, NSUB, MOD, 0.5, inten, n_theta_user=NTHETA, workers=os.cpu_count())
     t0 = time.perf_counter()
-    ref = O.closed_loop(ow, O.dm_modes(RES, 8.0, NSUB), R.astype(np.float64), lambda t: layers.opd(t, RES), pup,
+    ora = A.OracleAtmosphere(RES, 8.0, 1e-3, 0.15, 25.0, [1.0], [10.0], [0.0], [0.0])
+
+    def turbulence(t):
+        ora.update()            # step t sees the atmosphere after t + 1 updates
+        return ora.opd
+
+    ref = O.closed_loop(ow, O.dm_modes(RES, 8.0, NSUB), R.astype(np.float64), turbulence, pup,
                         ngs.wavelength, 0.4, n_oracle, workers=os.cpu_count())
     out['oracle'] = {'frames': n_oracle, 'seconds': time.perf_counter() - t0,
                      'strehl_le_pct': ref['strehl_le'], 'gpu_strehl_le_pct': sr100,

@@ -236,7 +236,8 @@ int oopao_cl_pupil_rms(const float* opd, const int* idx, int npup, const int* st
  * A [n_outer][n_inner], B [n_outer][n_outer]: float64 extrusion matrices;
  *   inner_idx / outer_idx: map indices of the Z and X rings; normals:
  *   float64 [rows][n_outer] drawn by the host.
- * range: device float64 [n_layers][2] scratch (value range of each map);
+ * range: device float64 [n_layers][32][2] scratch (partial value ranges of
+ *   each map); at most 64 layers;
  * scale: device float64 [n_layers] = lambda/2pi * sqrt(fractional r0);
  * opd: device float32 [res][res] output; step: device int32, the step whose
  *   entries are used, incremented at the end when `advance`; err: device

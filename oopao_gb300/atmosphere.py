@@ -187,7 +187,7 @@ class Atmosphere:
         self._frozen = False
         self._step_dev = torch.zeros(1, dtype=torch.int32, device=d)
         self._err = torch.zeros(1, dtype=torch.int32, device=d)
-        self._range = torch.zeros((self.nLayer, 2), dtype=torch.float64, device=d)
+        self._range = torch.zeros((self.nLayer, 32, 2), dtype=torch.float64, device=d)
         self._opd_dev = torch.zeros((res, res), dtype=torch.float32, device=d)
         self.hasNotBeenInitialized = False
         self.generateNewPhaseScreen(0)

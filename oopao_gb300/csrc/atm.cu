@@ -86,12 +86,18 @@ __global__ void atm_extrude(double* __restrict__ map, const double* __restrict__
   }
 }
 
+constexpr int kRangeBlocks = 32;  // partial value ranges per layer
+
+// partial value range of each map: block b of layer l covers a contiguous
+// chunk; range[l][b] = (min, max)
 __global__ void atm_minmax(const double* __restrict__ map, double* __restrict__ range, int n) {
   __shared__ double lo_s[32], hi_s[32];
-  const int l = blockIdx.x;
+  const int l = blockIdx.y, b = blockIdx.x;
   const double* m = map + (size_t)l * n * n;
+  const int nn = n * n, chunk = (nn + gridDim.x - 1) / gridDim.x;
+  const int i0 = b * chunk, i1 = min(nn, i0 + chunk);
   double lo = DBL_MAX, hi = -DBL_MAX;
-  for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
+  for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
     lo = fmin(lo, m[i]);
     hi = fmax(hi, m[i]);
   }
@@ -114,60 +120,87 @@ __global__ void atm_minmax(const double* __restrict__ map, double* __restrict__ 
       hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, s));
     }
     if (lane == 0) {
-      range[2 * l] = lo;
-      range[2 * l + 1] = hi;
+      range[((size_t)l * gridDim.x + b) * 2] = lo;
+      range[((size_t)l * gridDim.x + b) * 2 + 1] = hi;
     }
   }
 }
 
-// Keys cubic convolution of f at offset x in [0, 1) from f1
-__device__ __forceinline__ double keys(double x, double f0, double f1, double f2, double f3) {
-  return f1 + 0.5 * x * (f2 - f0 + x * (2.0 * f0 - 5.0 * f1 + 4.0 * f2 - f3 + x * (3.0 * (f1 - f2) + f3 - f0)));
+// Weights of the Keys cubic convolution (a = -0.5) at offset x in [0, 1):
+// f1 + x/2 (f2 - f0 + x (2 f0 - 5 f1 + 4 f2 - f3 + x (3 (f1 - f2) + f3 - f0)))
+__device__ __forceinline__ void keys_weights(float x, float* w) {
+  const float x2 = x * x, x3 = x2 * x;
+  w[0] = 0.5f * (-x + 2.f * x2 - x3);
+  w[1] = 1.f + 0.5f * (-5.f * x2 + 3.f * x3);
+  w[2] = 0.5f * (x + 4.f * x2 - 3.f * x3);
+  w[3] = 0.5f * (-x2 + x3);
 }
 
-__device__ __forceinline__ double map_at(const double* m, int n, int r, int c) {
-  return (r >= 0 && r < n && c >= 0 && c < n) ? m[(size_t)r * n + c] : 0.0;
+__device__ __forceinline__ float map_at(const double* m, int n, int r, int c) {
+  return (r >= 0 && r < n && c >= 0 && c < n) ? (float)m[(size_t)r * n + c] : 0.f;
 }
 
+constexpr int kMaxAtmLayers = 64;
+
+// The sub-pixel offset is the same for every pixel of a layer, so the
+// per-layer integer base, separable weights and value range are set up once
+// per block in shared memory; each pixel is then 16 loads and FP32 FMAs per
+// layer (the interpolated values are rounded to float32 like the output).
 __global__ void atm_opd(const double* __restrict__ map, const double* __restrict__ range,
                         const double2* __restrict__ buff, const int* step, int n_steps, int use_buff,
                         const double* __restrict__ scale, int n_layers, int n, int res, int off, float* __restrict__ opd,
                         int* err) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= res * res) return;
+  __shared__ float wr_s[kMaxAtmLayers][4], wc_s[kMaxAtmLayers][4], lo_s[kMaxAtmLayers], hi_s[kMaxAtmLayers],
+      sc_s[kMaxAtmLayers];
+  __shared__ int dr_s[kMaxAtmLayers], dc_s[kMaxAtmLayers];
   int t = -1;
   if (use_buff) {
     t = atm_step(step, n_steps, err);
     if (t < 0) return;
   }
-  const int y = p / res, x = p % res;
-  double acc = 0.0;
-  for (int l = 0; l < n_layers; l++) {
-    const double* m = map + (size_t)l * n * n;
+  for (int l = threadIdx.x; l < n_layers; l += blockDim.x) {
     double tx = 0.0, ty = 0.0;
     if (use_buff) {
       const double2 b = buff[(size_t)t * n_layers + l];
       tx = b.x;
       ty = b.y;
     }
-    // output pixel (r, c) of the warped map reads (r - ty, c - tx); the OPD
-    // crop starts `off` pixels into the map
-    const double rr = (double)(y + off) - ty, cc = (double)(x + off) - tx;
-    const double fr = floor(rr), fc = floor(cc);
-    const int r0 = (int)fr, c0 = (int)fc;
-    const double xr = rr - fr, xc = cc - fc;
-    double rows[4];
+    // output pixel (r, c) of the warped map reads (r - ty, c - tx)
+    const double fr = floor(-ty), fc = floor(-tx);
+    dr_s[l] = (int)fr;
+    dc_s[l] = (int)fc;
+    keys_weights((float)(-ty - fr), wr_s[l]);
+    keys_weights((float)(-tx - fc), wc_s[l]);
+    double lo = DBL_MAX, hi = -DBL_MAX;
+    for (int b = 0; b < kRangeBlocks; b++) {
+      lo = fmin(lo, range[((size_t)l * kRangeBlocks + b) * 2]);
+      hi = fmax(hi, range[((size_t)l * kRangeBlocks + b) * 2 + 1]);
+    }
+    lo_s[l] = (float)lo;
+    hi_s[l] = (float)hi;
+    sc_s[l] = (float)scale[l];
+  }
+  __syncthreads();
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= res * res) return;
+  const int y = p / res, x = p % res;
+  float acc = 0.f;
+  for (int l = 0; l < n_layers; l++) {
+    const double* m = map + (size_t)l * n * n;
+    // the OPD crop starts `off` pixels into the map
+    const int r0 = y + off + dr_s[l], c0 = x + off + dc_s[l];
+    float v = 0.f;
 #pragma unroll
     for (int pr = 0; pr < 4; pr++) {
       const int r = r0 + pr - 1;
-      rows[pr] = keys(xc, map_at(m, n, r, c0 - 1), map_at(m, n, r, c0), map_at(m, n, r, c0 + 1),
-                      map_at(m, n, r, c0 + 2));
+      const float row = wc_s[l][0] * map_at(m, n, r, c0 - 1) + wc_s[l][1] * map_at(m, n, r, c0) +
+                        wc_s[l][2] * map_at(m, n, r, c0 + 1) + wc_s[l][3] * map_at(m, n, r, c0 + 2);
+      v = fmaf(wr_s[l][pr], row, v);
     }
-    double v = keys(xr, rows[0], rows[1], rows[2], rows[3]);
-    v = fmin(fmax(v, range[2 * l]), range[2 * l + 1]);
-    acc += v * scale[l];
+    v = fminf(fmaxf(v, lo_s[l]), hi_s[l]);
+    acc = fmaf(v, sc_s[l], acc);
   }
-  opd[p] = (float)acc;
+  opd[p] = acc;
 }
 
 __global__ void atm_advance(int* step) {
@@ -182,8 +215,9 @@ extern "C" int oopao_atm_update(double* maps, int n_layers, int n, int slots, co
                                 double* range, const double* scale, int res, float* opd, int* step, int advance,
                                 int* err, void* stream) {
   OOPAO_CHECK_ARG(maps && scale && opd && step && range, "NULL argument");
-  OOPAO_CHECK_ARG(n_layers > 0 && n >= 8 && res > 0 && res <= n - 6 && slots >= 0 && slots % 2 == 0,
-                  "bad sizes (n >= res + 6, an even number of slots)");
+  OOPAO_CHECK_ARG(n_layers > 0 && n_layers <= kMaxAtmLayers && n >= 8 && res > 0 && res <= n - 6 && slots >= 0 &&
+                      slots % 2 == 0,
+                  "bad sizes (1 to 64 layers, n >= res + 6, an even number of slots)");
   OOPAO_CHECK_ARG(slots == 0 || (sched && A && B && inner_idx && outer_idx && normals && n_inner > 0 && n_outer > 0),
                   "moving layers need the schedule, A, B, ring indices and normals");
   cudaStream_t st = (cudaStream_t)stream;
@@ -200,7 +234,7 @@ extern "C" int oopao_atm_update(double* maps, int n_layers, int n, int slots, co
                                                           err);
     launches += 2;
   }
-  atm_minmax<<<n_layers, 512, 0, st>>>(maps, range, n);
+  atm_minmax<<<dim3(kRangeBlocks, n_layers), 256, 0, st>>>(maps, range, n);
   const int off = (n - res) / 2;  // crop of the warped map: [1:-1] then the pupil footprint
   atm_opd<<<ceil_div(res * res, 256), 256, 0, st>>>(maps, range, reinterpret_cast<const double2*>(buff), step,
                                                    n_steps, buff != nullptr ? 1 : 0, scale, n_layers, n, res, off,
