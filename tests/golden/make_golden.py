@@ -195,6 +195,37 @@ def case_atmosphere(OOPAO, name='atm_small', **p):
     print(name, 'steps', p['steps'], 'A', layer.A.shape, 'B', layer.B.shape)
 
 
+def case_large(OOPAO, name='c5_screen'):
+    """80x80 pyramid on a 39 m, 480 px pupil (N = 1920 with n_pix_separation
+    80, n_pix_edge 40; 320x320 camera; modulation 4 l/D with 128 points):
+    geometry, valid pixels, reference slopes and one seeded screen measured
+    through wfs_measure.  No DM (its 230400 x 5209 float64 IF matrix is not
+    needed for the sensor)."""
+    import json
+    from OOPAO.Pyramid import Pyramid
+    from OOPAO.Source import Source
+    from OOPAO.Telescope import Telescope
+    p = dict(res=480, diameter=39.0, n_subap=80, modulation=4, light_ratio=0.5, n_pix_separation=80,
+             n_pix_edge=40, nTheta_user_defined=128)
+    with _quiet():
+        tel = Telescope(resolution=p['res'], diameter=p['diameter'], samplingTime=1e-3)
+        ngs = Source(optBand='V0', magnitude=8)
+        ngs * tel
+        wfs = Pyramid(nSubap=p['n_subap'], telescope=tel, modulation=p['modulation'], lightRatio=p['light_ratio'],
+                      n_pix_separation=p['n_pix_separation'], n_pix_edge=p['n_pix_edge'],
+                      nTheta_user_defined=p['nTheta_user_defined'])
+        ph = screen(p['res'], 5, 2.0) * tel.pupil
+        ngs ** tel
+        wfs.wfs_measure(phase_in=ph)
+    rec = dict(params=json.dumps(p), pupil=np.array(tel.pupil), intensity=np.array(ngs.intensity),
+               wavelength=ngs.wavelength, N=wfs.resolution, cam=wfs.cam.resolution, n_theta=wfs.nTheta,
+               n_signal=wfs.nSignal, valid_i4q=np.array(wfs.validI4Q), reference_2d=np.array(wfs.referenceSignal_2D),
+               screen_phase=ph, screen_frame=np.array(wfs.cam.frame), screen_signal=np.array(wfs.signal),
+               screen_signal_2D=np.array(wfs.signal_2D))
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **rec)
+    print(name, 'N', rec['N'], 'cam', rec['cam'], 'K', rec['n_theta'], 'nSignal', rec['n_signal'])
+
+
 CASES = [
     ('tiny', (24, 4, 3, 0.5), {}),
     ('tiny_nocenter', (24, 4, 2, 0.5), dict(psfCentering=False, n_im=0)),
@@ -218,6 +249,8 @@ def main():
             case_small(OOPAO, name, *args, **kw)
     if not only or 'atm_small' in only:
         case_atmosphere(OOPAO)
+    if not only or 'c5_screen' in only:
+        case_large(OOPAO)
 
 
 if __name__ == '__main__':
