@@ -21,6 +21,7 @@ from .deformable_mirror import DeformableMirror
 from .pyramid import Pyramid
 from .calibration import InteractionMatrix, CalibrationVault
 from .atmosphere import Atmosphere
+from .bioedge import BioEdge
 
 __all__ = ['OopaoError', 'warning', 'Source', 'Telescope', 'Detector', 'DeformableMirror', 'Pyramid',
-           'InteractionMatrix', 'CalibrationVault', 'Atmosphere']
+           'InteractionMatrix', 'CalibrationVault', 'Atmosphere', 'BioEdge']

@@ -226,6 +226,54 @@ def case_large(OOPAO, name='c5_screen'):
     print(name, 'N', rec['N'], 'cam', rec['cam'], 'K', rec['n_theta'], 'nSignal', rec['n_signal'])
 
 
+def case_bioedge(OOPAO, name, res, n_subap, modulation, light_ratio, seeds=(3, 4), n_im=4, **kw):
+    """Bi-O Edge sensor: masks, geometry, valid pixels, reference slopes, a DM
+    measurement, a screen measurement and push-pull IM columns."""
+    import json
+    from OOPAO.BioEdge import BioEdge
+    from OOPAO.DeformableMirror import DeformableMirror
+    from OOPAO.Source import Source
+    from OOPAO.Telescope import Telescope
+    with _quiet():
+        tel = Telescope(resolution=res, diameter=8.0, samplingTime=1e-3)
+        ngs = Source(optBand='V0', magnitude=8)
+        ngs * tel
+        dm = DeformableMirror(tel, nSubap=n_subap, mechCoupling=0.35)
+        wfs = BioEdge(nSubap=n_subap, telescope=tel, modulation=modulation, lightRatio=light_ratio, **kw)
+    rec = dict(params=json.dumps(dict(res=res, n_subap=n_subap, modulation=modulation, light_ratio=light_ratio,
+                                      **kw)),
+               masks=np.array(wfs.mask), N=wfs.resolution, cam=wfs.cam.resolution, n_theta=wfs.nTheta,
+               n_signal=wfs.nSignal, valid_i4q=np.array(wfs.validI4Q), reference_2d=np.array(wfs.referenceSignal_2D),
+               intensity=np.array(ngs.intensity), pupil=np.array(tel.pupil), wavelength=ngs.wavelength)
+    coefs = np.random.default_rng(seeds[0]).standard_normal(dm.nValidAct) * 60e-9
+    with _quiet():
+        dm.coefs = coefs
+        ngs ** tel * dm * wfs
+    rec.update(dm_coefs=coefs, dm_phase=np.array(ngs.phase), dm_raw=np.array(wfs.raw_data),
+               dm_frame=np.array(wfs.cam.frame), dm_signal=np.array(wfs.signal), dm_signal_2D=np.array(wfs.signal_2D))
+    ph = screen(res, seeds[1], 2.0) * tel.pupil
+    with _quiet():
+        dm.coefs = 0
+        ngs ** tel
+        wfs.wfs_measure(phase_in=ph)
+    rec.update(screen_phase=ph, screen_frame=np.array(wfs.cam.frame), screen_signal=np.array(wfs.signal))
+    if n_im:
+        from OOPAO.calibration.InteractionMatrix import InteractionMatrix
+        m2c = np.eye(dm.nValidAct)[:, :n_im]
+        with _quiet():
+            calib = InteractionMatrix(ngs, tel, dm, wfs, M2C=m2c, stroke=1e-8, nMeasurements=1, single_pass=False)
+        rec.update(im_m2c=m2c, im_pp_D=np.array(calib.D))
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **rec)
+    print(name, 'N', rec['N'], 'cam', rec['cam'], 'K', rec['n_theta'], 'nSignal', rec['n_signal'])
+
+
+BIOEDGE_CASES = [
+    ('bioedge_tiny', (24, 4, 3, 0.5), {}),
+    ('bioedge_grey', (32, 4, 2, 0.3), dict(grey_width=1.0, quadrants_numbering=[2, 3, 0, 1], n_pix_separation=4,
+                                           nTheta_user_defined=12)),
+]
+
+
 CASES = [
     ('tiny', (24, 4, 3, 0.5), {}),
     ('tiny_nocenter', (24, 4, 2, 0.5), dict(psfCentering=False, n_im=0)),
@@ -251,6 +299,9 @@ def main():
         case_atmosphere(OOPAO)
     if not only or 'c5_screen' in only:
         case_large(OOPAO)
+    for name, args, kw in BIOEDGE_CASES:
+        if not only or name in only:
+            case_bioedge(OOPAO, name, *args, **kw)
 
 
 if __name__ == '__main__':

@@ -1,0 +1,76 @@
+"""Bi-O Edge drop-in against golden vectors made by the unmodified reference:
+geometry, valid pixels, reference slopes, a DM measurement through
+``ngs**tel*dm*wfs``, a screen through ``wfs_measure`` and push-pull IM
+columns.  FP32 path bounds: 1e-5 (frames, signals), 1e-4 (IM columns)."""
+import contextlib
+import io
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pwfs_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden')
+
+
+def _quiet():
+    return contextlib.redirect_stdout(io.StringIO())
+
+
+@pytest.fixture(scope='module', params=['bioedge_tiny', 'bioedge_grey'])
+def system(request):
+    import oopao_gb300 as og
+    z = np.load(os.path.join(HERE, request.param + '.npz'))
+    d = {k: z[k] for k in z.files}
+    p = json.loads(str(d['params']))
+    kw = {k: v for k, v in p.items() if k not in ('res', 'n_subap', 'modulation', 'light_ratio')}
+    with _quiet():
+        tel = og.Telescope(resolution=p['res'], diameter=8.0, samplingTime=1e-3)
+        ngs = og.Source(optBand='V0', magnitude=8)
+        ngs * tel
+        dm = og.DeformableMirror(tel, nSubap=p['n_subap'], mechCoupling=0.35)
+        wfs = og.BioEdge(nSubap=p['n_subap'], telescope=tel, modulation=p['modulation'], lightRatio=p['light_ratio'],
+                         **kw)
+    return d, tel, ngs, dm, wfs
+
+
+def test_geometry_and_calibration(system):
+    d, tel, ngs, dm, wfs = system
+    assert wfs.resolution == int(d['N']) and wfs.cam.resolution == int(d['cam'])
+    assert wfs.nTheta == int(d['n_theta'])
+    for m, g in zip(wfs.mask, d['masks']):
+        np.testing.assert_allclose(m, g, rtol=0, atol=1e-14)
+    np.testing.assert_array_equal(wfs.validI4Q, d['valid_i4q'])
+    assert wfs.nSignal == int(d['n_signal'])
+    assert O.rel_l2(wfs.referenceSignal_2D, d['reference_2d']) < 1e-5
+
+
+def test_dm_measurement(system):
+    d, tel, ngs, dm, wfs = system
+    dm.coefs = d['dm_coefs']
+    ngs ** tel * dm * wfs
+    assert O.rel_l2(wfs.raw_data, d['dm_raw']) < 1e-5
+    assert O.rel_l2(wfs.cam.frame, d['dm_frame']) < 1e-5
+    assert O.rel_l2(wfs.signal_2D, d['dm_signal_2D']) < 1e-5
+    assert O.rel_l2(wfs.signal, d['dm_signal']) < 1e-5
+
+
+def test_screen_measurement(system):
+    d, tel, ngs, dm, wfs = system
+    dm.coefs = 0
+    ngs ** tel
+    wfs.wfs_measure(phase_in=d['screen_phase'])
+    assert O.rel_l2(wfs.cam.frame, d['screen_frame']) < 1e-5
+    assert O.rel_l2(wfs.signal, d['screen_signal']) < 1e-5
+
+
+def test_interaction_matrix(system):
+    import oopao_gb300 as og
+    d, tel, ngs, dm, wfs = system
+    with _quiet():
+        calib = og.InteractionMatrix(ngs, tel, dm, wfs, d['im_m2c'], 1e-8, single_pass=False, invert=False)
+    assert O.rel_l2(np.asarray(calib.D), d['im_pp_D']) < 1e-4
