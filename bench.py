@@ -3,7 +3,7 @@
 Workload (N=1): the "batched calibration" configuration — 8 m pupil, 120 px
 (6 px/subaperture), 20x20 pyramid (N=264 FFT grid, 44x44 camera),
 modulation 3 lambda/D with 48 points, 21x21 Gaussian-IF DM (357 valid
-actuators, coupling 0.35), 300 KL-like modes, push-pull +-1e-8 m RMS,
+actuators, coupling 0.35), 300 KL modes, push-pull +-1e-8 m RMS,
 float32 commands, FP64 SVD reconstructor keeping 280 modes.  One step = one
 push-pull interaction matrix = 600 PWFS frames (each frame = 48 modulation
 points).
@@ -38,7 +38,7 @@ sys.path.insert(0, ROOT)
 
 RES, NSUB, MOD, NTHETA, NMODES, STROKE, NTRUNC = 120, 20, 3, 48, 300, 1e-8, 20
 WORKLOAD = ('batched push-pull interaction matrix: 8 m, 120 px, 20x20 PWFS (N=264, cam 44), '
-            'modulation 3 l/D x 48 points, 21x21 Gaussian DM (357 act), 300 KL-like modes, '
+            'modulation 3 l/D x 48 points, 21x21 Gaussian DM (357 act), 300 KL modes, '
             '+-1e-8 m RMS, FP64 SVD 280 modes')
 
 
@@ -46,57 +46,24 @@ def _quiet():
     return contextlib.redirect_stdout(io.StringIO())
 
 
+_KL_CACHE = {}
+
+
 def kl_like_basis(modes, pupil, n_modes, diameter=8.0, r0=0.15, L0=25.0):
-    """Synthetic KL modal basis M2C [n_act, n_modes] in the DM space: the
-    von Karman phase covariance projected on the in-pupil influence
-    functions, P = F^T C_phi F, diagonalised in the pupil metric G = F^T F
-    (generalised eigenproblem P c = lambda G c, modes orthonormal over the
-    pupil, decreasing turbulence variance), each mode scaled to 1 m RMS OPD
-    over the pupil.  The construction of the reference's KL basis (covariance
-    diagonalised in the DM's pupil metric, OOPAO/calibration/ao_cockpit_psim.py:
-    649-736, HHt by FFT :847) restated for the bench inputs; the modes are not
-    on the measured path.  F^T C_phi F is computed by FFT convolution of
-    each influence function with the covariance kernel (torch on the GPU)."""
-    import scipy.linalg
-    import torch
-    from scipy.special import gamma, kv
-    res = pupil.shape[0]
-    n_act = modes.shape[1]
-    ipup = pupil.reshape(-1) > 0
-    F = modes[ipup]                                   # [npup, n_act]
-    npup = F.shape[0]
-    n2 = 2 * res
-    dx = diameter / res
-    off = np.fft.fftfreq(n2, 1.0 / n2) * dx           # offsets 0..res-1, -res..-1 (pixels * dx)
-    r = np.hypot(off[:, None], off[None, :])
-    k0 = 2 * np.pi / L0
-    c = (L0 / r0) ** (5 / 3) * gamma(11 / 6) / (2 ** (5 / 6) * np.pi ** (8 / 3)) * \
-        (24 / 5 * gamma(6 / 5)) ** (5 / 6)
-    rr = np.maximum(r, 1e-12)
-    kern = c * (k0 * rr) ** (5 / 6) * kv(5 / 6, k0 * rr)
-    kern[r < 1e-12] = c * gamma(5 / 6) / 2 ** (1 / 6)
-    dev = 'cuda' if torch.cuda.is_available() else 'cpu'
-    kf = torch.fft.fft2(torch.as_tensor(kern, device=dev))
-    Fd = torch.as_tensor(F, device=dev)
-    ip = torch.as_tensor(np.flatnonzero(ipup), device=dev)
-    P = torch.empty((n_act, n_act), dtype=torch.float64, device=dev)
-    mt = torch.as_tensor(modes * pupil.reshape(-1, 1), device=dev)
-    for a0 in range(0, n_act, 64):
-        a1 = min(n_act, a0 + 64)
-        blk = torch.zeros((a1 - a0, n2, n2), dtype=torch.float64, device=dev)
-        blk[:, :res, :res] = mt[:, a0:a1].T.reshape(a1 - a0, res, res)
-        conv = torch.fft.ifft2(torch.fft.fft2(blk) * kf).real[:, :res, :res].reshape(a1 - a0, -1)
-        P[:, a0:a1] = Fd.T @ conv[:, ip].T
-    P = P.cpu().numpy()
-    P = 0.5 * (P + P.T)
-    G = F.T @ F
-    lam, vec = scipy.linalg.eigh(P, G)
-    # the largest-variance mode is the DM's piston, which no slope sees: left out
-    vec = vec[:, np.argsort(lam)[::-1][1:n_modes + 1]]
-    mean = (F.sum(axis=0) @ vec) / npup
-    msq = np.einsum('ij,ij->j', vec, G @ vec) / npup
-    vec = vec / np.sqrt(np.maximum(msq - mean ** 2, 1e-300))[None]
-    return np.ascontiguousarray(vec)
+    """KL modal basis M2C [n_act, n_modes] of the DM, computed as the
+    reference's compute_KL_basis does (oopao_gb300.modal_basis: tip/tilt
+    fitted, seed basis, diagonalisation of the von Karman HHt; piston
+    removed), truncated to the first n_modes.  Modes are orthonormal over the
+    pupil (1 m RMS per unit coefficient).  Cached per DM geometry."""
+    import types
+    from oopao_gb300.modal_basis import compute_KL_basis
+    key = (modes.shape, pupil.shape, float(np.asarray(modes).sum()), diameter, r0, L0)
+    if key not in _KL_CACHE:
+        tel = types.SimpleNamespace(pupil=pupil, resolution=pupil.shape[0], D=diameter)
+        atm = types.SimpleNamespace(r0=r0, L0=L0)
+        dm = types.SimpleNamespace(modes=modes, nValidAct=modes.shape[1], isM4=False)
+        _KL_CACHE[key] = compute_KL_basis(tel, atm, dm)
+    return np.ascontiguousarray(_KL_CACHE[key][:, :n_modes])
 
 
 def build_system(dev_index, res=RES, nsub=NSUB, mod=MOD, ntheta=NTHETA, max_batch=100, if_dtype='fp32'):
@@ -572,7 +539,7 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_cpu:
         r, frames, el, thr = cpu_oracle_rate()
         cpu = {'value': r, 'unit': 'frames/s', 'cores': thr, 'kind': 'port',
-               'sample': '%d push-pull frames (%d KL-like modes) in %.1f s, float64 oracle, '
+               'sample': '%d push-pull frames (%d KL modes) in %.1f s, float64 oracle, '
                          'scipy.fft workers=%d' % (frames, frames // 2, el, thr)}
 
     # accuracy of this step's IM against the float64 oracle on 2 columns
@@ -607,7 +574,7 @@ def run_ours(args):
             'metric': 'PWFS frames/s (batched IM build)', 'value': value, 'unit': 'frames/s',
             'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms_step,
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
-            'data': 'synthetic (seeded KL-like basis, Gaussian IFs)',
+            'data': 'synthetic (seeded KL basis, Gaussian IFs)',
             'config': {'workload': WORKLOAD, 'frames_per_step': frames_step, 'modulation_points': k,
                        'fft_grid': n, 'camera': cam, 'batch_per_launch': wfs.max_batch,
                        'l2': 'intermediates (>=2.4 GB per launch) exceed L2; no flush needed',

@@ -267,6 +267,32 @@ def case_bioedge(OOPAO, name, res, n_subap, modulation, light_ratio, seeds=(3, 4
     print(name, 'N', rec['N'], 'cam', rec['cam'], 'K', rec['n_theta'], 'nSignal', rec['n_signal'])
 
 
+KL_CASES = [('kl_tiny', dict(res=24, n_subap=4)), ('kl_c1', dict(res=120, n_subap=20))]
+
+
+def case_kl(OOPAO, name, res, n_subap, r0=0.15, L0=25.0):
+    """KL modal basis of the reference (compute_KL_basis, lim 1e-3, piston
+    removed) for a Gaussian-IF DM, with its input IFs summarised."""
+    import json
+    from OOPAO.Atmosphere import Atmosphere
+    from OOPAO.DeformableMirror import DeformableMirror
+    from OOPAO.Source import Source
+    from OOPAO.Telescope import Telescope
+    from OOPAO.calibration.compute_KL_modal_basis import compute_KL_basis
+    with _quiet():
+        tel = Telescope(resolution=res, diameter=8.0, samplingTime=1e-3)
+        ngs = Source(optBand='V0', magnitude=8)
+        ngs * tel
+        dm = DeformableMirror(tel, nSubap=n_subap, mechCoupling=0.35)
+        atm = Atmosphere(telescope=tel, r0=r0, L0=L0, fractionalR0=[1.0], windSpeed=[10.], windDirection=[0.],
+                         altitude=[0.])
+        m2c = compute_KL_basis(tel, atm, dm, lim=1e-3, remove_piston=True)
+    rec = dict(params=json.dumps(dict(res=res, n_subap=n_subap, r0=r0, L0=L0)), m2c=np.asarray(m2c),
+               n_act=dm.nValidAct)
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **rec)
+    print(name, 'M2C', rec['m2c'].shape)
+
+
 BIOEDGE_CASES = [
     ('bioedge_tiny', (24, 4, 3, 0.5), {}),
     ('bioedge_grey', (32, 4, 2, 0.3), dict(grey_width=1.0, quadrants_numbering=[2, 3, 0, 1], n_pix_separation=4,
@@ -302,6 +328,12 @@ def main():
     for name, args, kw in BIOEDGE_CASES:
         if not only or name in only:
             case_bioedge(OOPAO, name, *args, **kw)
+    if not only or any(n in only for n, _ in KL_CASES):
+        from refimport import install_kl_shims
+        install_kl_shims()
+        for name, kw in KL_CASES:
+            if not only or name in only:
+                case_kl(OOPAO, name, **kw)
 
 
 if __name__ == '__main__':

@@ -54,6 +54,50 @@ _STUBS = [
 ]
 
 
+def install_kl_shims():
+    """Numerical stand-ins for the three accelerators the reference's KL basis
+    imports (``OOPAO/calibration/ao_cockpit_psim.py:13-22``): numba.jit as the
+    identity, pyfftw's in-place FFTW object as numpy's fftn, and
+    numexpr.evaluate as numpy evaluation of the expression in the caller's
+    scope.  They change how the arithmetic is scheduled, not what it is."""
+    import numpy as np
+
+    numba = types.ModuleType('numba')
+
+    def jit(*a, **k):
+        if a and callable(a[0]) and len(a) == 1 and not k:
+            return a[0]
+        return lambda f: f
+    numba.jit = numba.njit = jit
+    numba.prange = range
+    sys.modules['numba'] = numba
+
+    pyfftw = types.ModuleType('pyfftw')
+    pyfftw.empty_aligned = lambda shape, dtype='complex128', n=None: np.empty(shape, dtype=dtype)
+
+    class FFTW:
+        def __init__(self, a, b, axes=(-1,), flags=(), direction='FFTW_FORWARD', threads=1):
+            self.a, self.b, self.axes, self.direction = a, b, axes, direction
+
+        def __call__(self):
+            f = np.fft.fftn if self.direction == 'FFTW_FORWARD' else np.fft.ifftn
+            self.b[...] = f(self.a, axes=self.axes)
+            return self.b
+    pyfftw.FFTW = FFTW
+    sys.modules['pyfftw'] = pyfftw
+
+    numexpr = types.ModuleType('numexpr')
+
+    def evaluate(expr, local_dict=None, global_dict=None, **k):
+        frame = sys._getframe(1)
+        scope = dict(frame.f_globals)
+        scope.update(frame.f_locals if local_dict is None else local_dict)
+        scope.update(complex=lambda a, b: np.asarray(a) + 1j * np.asarray(b), conj=np.conj)
+        return np.asarray(eval(expr, {'__builtins__': {}}, scope))
+    numexpr.evaluate = evaluate
+    sys.modules['numexpr'] = numexpr
+
+
 def import_reference(ref_root='/root/reference', work='/tmp/OOPAO_refcopy'):
     """Return the imported ``OOPAO`` package from a stubbed copy of ``ref_root``."""
     if 'OOPAO' in sys.modules:
