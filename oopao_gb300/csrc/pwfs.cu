@@ -282,6 +282,10 @@ int fast_candidates(int n, const FastPasses** out) {
                                     make_fast<504, 24, 21, 24, 8, 8, 12>(),
                                     make_fast<504, 21, 24, 12, 16, 8, 12>(),
                                     make_fast<504, 24, 21, 24, 8, 16, 6>()};
+  static const FastPasses f1920[] = {make_fast<1920, 48, 40, 48, 2, 8, 6>(),
+                                     make_fast<1920, 48, 40, 48, 2, 4, 6>(),
+                                     make_fast<1920, 48, 40, 48, 2, 2, 6>(),
+                                     make_fast<1920, 40, 48, 48, 2, 4, 6>()};
 #define OOPAO_CANDS(arr) (*out = arr, (int)(sizeof(arr) / sizeof(arr[0])))
   switch (n) {
     case 72: return OOPAO_CANDS(f72);
@@ -292,6 +296,7 @@ int fast_candidates(int n, const FastPasses** out) {
     case 264: return OOPAO_CANDS(f264);
     case 480: return OOPAO_CANDS(f480);
     case 504: return OOPAO_CANDS(f504);
+    case 1920: return OOPAO_CANDS(f1920);
     default: *out = nullptr; return 0;
   }
 #undef OOPAO_CANDS
@@ -1150,12 +1155,14 @@ const AdPasses* ad_passes(int n) {
   static const AdPasses a128 = make_ad<128, 16, 8, 8, 16>();
   static const AdPasses a264 = make_ad<264, 24, 11, 12, 12>();
   static const AdPasses a504 = make_ad<504, 24, 21, 12, 12>();
+  static const AdPasses a1920 = make_ad<1920, 48, 40, 48, 6>();
   switch (n) {
     case 72: return &a72;
     case 112: return &a112;
     case 128: return &a128;
     case 264: return &a264;
     case 504: return &a504;
+    case 1920: return &a1920;
     default: return nullptr;
   }
 }

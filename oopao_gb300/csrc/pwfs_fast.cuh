@@ -144,11 +144,14 @@ __global__ void __launch_bounds__(T* L) pwfs_cols2(ColsArgs a) {
   constexpr int R2P = LAY2 >> 16, LS2 = LAY2 & 0xFFFF;
   constexpr int PBA = (R2 + T - 1) / T;   // forward stage A / inverse stage B' butterflies
   constexpr int PBB = (R1 + T - 1) / T;   // forward stage B / inverse stage A' butterflies
+  // one stage-B butterfly per thread: its values stay in registers across a
+  // barrier, so the inverse exchange reuses the forward buffer
+  constexpr bool ALIAS = PBB == 1;
   extern __shared__ float2 sm[];
   float2* tw = sm;            // tw[m*R1 + j]  = W_N^{j m},  j < R1, m < R2
   float2* twi = sm + N;       // twi[m*R2 + j] = W_N^{-j m}, j < R2, m < R1
   float2* b1 = sm + 2 * N;    // [L][LS1] forward exchange
-  float2* b2 = b1 + L * LS1;  // [L][LS2] inverse exchange
+  float2* b2 = ALIAS ? b1 : b1 + L * LS1;  // [L][LS2] inverse exchange
   const int tid = threadIdx.x;
   const int l = tid % L, t = tid / L;
   for (int i = tid; i < N; i += T * L) {
@@ -187,8 +190,8 @@ __global__ void __launch_bounds__(T* L) pwfs_cols2(ColsArgs a) {
 #pragma unroll
   for (int p = 0; p < PBB; p++) {
     const int j = t + p * T;
+    float2 v[R2];
     if (j < R1) {
-      float2 v[R2];
 #pragma unroll
       for (int m = 0; m < R2; m++) {
         const float2 u = x1[m * R1P + j];
@@ -207,6 +210,9 @@ __global__ void __launch_bounds__(T* L) pwfs_cols2(ColsArgs a) {
         v[q] = cmul(v[q], mq);
       }
       dft<R2, true>(v);
+    }
+    if constexpr (ALIAS) __syncthreads();  // every read of the forward exchange is done
+    if (j < R1) {
 #pragma unroll
       for (int q = 0; q < R2; q++) x2[j * R2P + q] = v[q];
     }
@@ -233,11 +239,19 @@ __global__ void __launch_bounds__(T* L) pwfs_cols2(ColsArgs a) {
   }
 }
 
+// Row-inverse exchange: double-buffered over modulation points (one barrier
+// per point) while both buffers fit in ~110 KB; a single buffer with a second
+// barrier per point above that, so that two CTAs still share an SM.
+__host__ __device__ constexpr bool inv_double_buffer(int N, int L, int LS) {
+  return (size_t)(N + 2 * L * LS) * 8 <= 110 * 1024;
+}
+
 // ---- pass 3: row inverse FFT, |.|^2 summed over a slot of points, binning ----
 template <int N, int R1, int R2, int T, int L>
 __global__ void __launch_bounds__(T* L) pwfs_rows_inv2(RowsInvArgs a) {
   constexpr int R2P = pad_odd(R2);
   constexpr int LS = xchg_stride(R1 * R2P, T, L, R2P, R1, R2);
+  constexpr bool DB = inv_double_buffer(N, L, LS);
   constexpr int PBA = (R1 + T - 1) / T;  // inverse stage A' (radix R2) butterflies
   constexpr int PBB = (R2 + T - 1) / T;  // inverse stage B' (radix R1) butterflies
   extern __shared__ float2 sm[];
@@ -259,7 +273,8 @@ __global__ void __launch_bounds__(T* L) pwfs_rows_inv2(RowsInvArgs a) {
     for (int q = 0; q < R1; q++) acc[p][q] = 0.f;
   __syncthreads();
   for (int kk = kbeg; kk < kend; kk++) {
-    float2* x = xb + ((kk - kbeg) & 1) * L * LS + l * LS;
+    float2* x = xb + (DB ? ((kk - kbeg) & 1) : 0) * L * LS + l * LS;
+    if (!DB && kk > kbeg) __syncthreads();  // the previous point's reads of x are done
     const float2* z = a.z + (((size_t)b * a.kp + (kk - a.k0)) * N + row) * N;
 #pragma unroll
     for (int p = 0; p < PBA; p++) {
@@ -347,7 +362,9 @@ template <int N, int R1, int R2, int T, int LR, int LC, int LI>
 FastPasses make_fast() {
   constexpr int R1P = pad_odd(R1), R2P = pad_odd(R2);
   constexpr int LSR = xchg_stride(R2 * R1P, T, LR, R1P, R2, R1);
-  constexpr int LSC = (cols_layout(R1, R2, T, LC) & 0xFFFF) + (cols_layout(R2, R1, T, LC) & 0xFFFF);
+  constexpr int LS1C = cols_layout(R1, R2, T, LC) & 0xFFFF, LS2C = cols_layout(R2, R1, T, LC) & 0xFFFF;
+  // the column pass shares one exchange buffer when each thread has one stage-B butterfly
+  constexpr int LSC = ((R1 + T - 1) / T == 1) ? imax(LS1C, LS2C) : LS1C + LS2C;
   constexpr int LSI = xchg_stride(R1 * R2P, T, LI, R2P, R1, R2);
   FastPasses f;
   f.n = N; f.r1 = R1; f.r2 = R2; f.t = T; f.l_rows = LR; f.l_cols = LC; f.l_inv = LI;
@@ -356,6 +373,6 @@ FastPasses make_fast() {
   f.inv = pwfs_rows_inv2<N, R1, R2, T, LI>;
   f.smem_rows = sizeof(float2) * (N + (size_t)LR * LSR);
   f.smem_cols = sizeof(float2) * (2 * N + (size_t)LC * LSC);
-  f.smem_inv = sizeof(float2) * (N + 2 * (size_t)LI * LSI);
+  f.smem_inv = sizeof(float2) * (N + (inv_double_buffer(N, LI, LSI) ? 2 : 1) * (size_t)LI * LSI);
   return f;
 }

@@ -76,7 +76,8 @@ def test_measure_matches_oracle(lib, res, nsub, sep, mod, k):
 
 
 @pytest.mark.parametrize('n,res,cam', [(72, 24, 12), (96, 32, 16), (112, 40, 28), (128, 32, 16),
-                                       (240, 120, 40), (264, 120, 44), (480, 240, 80), (504, 240, 84)])
+                                       (240, 120, 40), (264, 120, 44), (480, 240, 80), (504, 240, 84),
+                                       (1920, 480, 320)])
 def test_variants_agree(lib, n, res, cam):
     """Compile-time two-stage passes == generic runtime-planned passes."""
     N = lib
