@@ -227,6 +227,43 @@ def cl_strehl(n_steps=500, n_oracle=100):
     return out
 
 
+def large_config(n_tangents=64):
+    """39 m, 480 px, 80x80 pyramid (N=1920, 320x320 camera, modulation 4 l/D
+    x 128 points): frames/s of the autotuned compiled plan at batch 1 and 4,
+    and tangents/s of the JVP (the columns of an interaction matrix built from
+    tangents) for `n_tangents` smooth pupil-plane directions, batch 8."""
+    import torch
+    import oopao_gb300 as og
+    from oopao_gb300 import autodiff as AD
+    from oopao_gb300 import autotune
+    with _quiet():
+        tel = og.Telescope(resolution=480, diameter=39.0, samplingTime=1e-3)
+        ngs = og.Source(optBand='V0', magnitude=8)
+        ngs * tel
+        wfs = og.Pyramid(nSubap=80, telescope=tel, modulation=4, lightRatio=0.5, n_pix_separation=80, n_pix_edge=40,
+                         nTheta_user_defined=128, max_batch=8)
+    ngs ** tel
+    wfs.plan.set_amplitude(ngs.intensity, wfs._amplitude_key())
+    out = {'config': '39 m, 480 px, 80x80 PWFS, N=1920, cam 320, modulation 4 l/D x 128 points',
+           'n_signal': wfs.nSignal}
+    g = torch.Generator(device='cuda').manual_seed(0)
+    for B in (1, 4):
+        tune = autotune.tune_pyramid(wfs, batch=B)
+        opd = torch.randn((B, 480, 480), device='cuda', generator=g) * 50e-9
+        wfs._measure_frames(opd, 2 * np.pi / ngs.wavelength)
+        _, t = _timed(lambda: [wfs._measure_frames(opd, 2 * np.pi / ngs.wavelength) for _ in range(3)])
+        out['frames_per_s_batch%d' % B] = 3 * B / t
+        out['variant_batch%d' % B] = tune['variant']
+    pup = torch.as_tensor(tel.pupil, dtype=torch.float32, device='cuda')
+    opd0 = torch.zeros((1, 480, 480), device='cuda')
+    dirs = torch.randn((n_tangents, 480, 480), device='cuda', generator=g) * pup * 10e-9
+    AD.frame_jvp(wfs, opd0, dirs[:8])
+    _, t = _timed(lambda: [AD.frame_jvp(wfs, opd0, dirs[i:i + 8]) for i in range(0, n_tangents, 8)])
+    out['jvp_tangents_per_s'] = n_tangents / t
+    out['im_4000_modes_estimate_s'] = 4000 / out['jvp_tangents_per_s']
+    return out
+
+
 def dm_projection(peaks):
     """DM influence-function projection OPD = modes @ coefs at the 20x20,
     40x40 and 80x80 sizes: FP32 CUDA-core path vs BF16 tcgen05 path, per
@@ -563,6 +600,7 @@ def run_ours(args):
         del tel3, ngs3, dm3, wfs3
         extra['cl_step'] = cl_rate()
         extra['cl_strehl_20x20'] = cl_strehl()
+        extra['large_80x80'] = large_config()
         try:
             pk = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
         except Exception:
