@@ -80,7 +80,8 @@ int oopao_pwfs_set_pass_budget(oopao_pwfs_plan* plan, size_t bytes);
 /* Kernel variant (autotuner hook, no reference counterpart): 0 = generic
  * runtime-planned kernels (any n_fft whose prime factors are <= 13),
  * 1..oopao_pwfs_num_variants = compile-time two-stage FFT plans for this
- * n_fft (1 is the default where one exists).  An index beyond the count
+ * n_fft (a new plan starts on the fastest one measured for its n_fft;
+ * oopao_pwfs_get_variant reports it).  An index beyond the count
  * returns OOPAO_ERR_UNSUPPORTED.  variant_info fills info[6] with
  * (R1, R2, threads per line, row / column / row-inverse lines per CTA). */
 int oopao_pwfs_set_variant(oopao_pwfs_plan* plan, int variant);

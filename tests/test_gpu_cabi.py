@@ -87,9 +87,9 @@ def test_variants_agree(lib, n, res, cam):
     amp = rng.uniform(0.5, 1.5, (res, res))
     h = make_plan(N, res, n, cam, mask, path, amp=amp)
     try:
-        assert N.load().oopao_pwfs_get_variant(h) == 1
         nv = N.load().oopao_pwfs_num_variants(h)
         assert nv >= 1
+        assert 1 <= N.load().oopao_pwfs_get_variant(h) <= nv    # starts on a compiled plan
         phase = rng.standard_normal((2, res, res))
         N.call('oopao_pwfs_set_variant', h, 0)
         f0, r0 = measure(N, h, phase, n, cam)
