@@ -319,6 +319,69 @@ def dm_projection(peaks):
     return out
 
 
+def gsc_leg(peaks):
+    """Gain-sensing camera: optical gains per focal-plane frame at the 20x20
+    (N=264, 300 modes) and 40x40 (N=504, 1000 modes) pyramid sizes, batch 1
+    and 16, through oopao_gsc_optical_gains (seven launches: frame sums,
+    two 2-D transforms, contraction with the basis product, sums over
+    chunks).  The basis product (modes x N^2 float32) is streamed once per
+    call; `bp_gbs` is its bytes over the whole call's time, a lower bound on
+    the contraction's bandwidth.  The float64 oracle (numpy, the reference's
+    algorithm) is timed on one frame at 20x20."""
+    import torch
+    from oopao_gb300 import GainSensingCamera
+    from oopao_gb300 import _native as N
+    from oracle import gsc_oracle as G
+    from oracle import pwfs_oracle as O
+    out = {}
+    for name, res, nsub, n_modes in (('20x20', 120, 20, 300), ('40x40', 240, 40, 1000)):
+        geom = O.pyramid_geometry(res, nsub, 2)
+        n = geom.N
+        rng = np.random.default_rng(0)
+        basis = rng.standard_normal((res, res, n_modes)).astype(np.float32) * 1e-8
+        r = np.hypot(*np.meshgrid(np.arange(n) - n / 2, np.arange(n) - n / 2))
+        frame = (np.exp(-(r / 10.0) ** 2) + 1e-3).astype(np.float32)
+        gsc = GainSensingCamera(np.asarray(geom.mask, np.complex64), basis)
+        _, t_cal = _timed(lambda: gsc.calibration(frame))
+        lib = N.load()
+        st = N.stream_handle()
+        rows = []
+        for B in (1, 16):
+            f = torch.as_tensor(np.broadcast_to(frame, (B, n, n)).copy(), device='cuda')
+            og = torch.empty((B, n_modes), dtype=torch.float64, device='cuda')
+            nb = lib.oopao_gsc_workspace_bytes(gsc._plan, B)
+            ws = torch.empty(nb, dtype=torch.uint8, device='cuda')
+            fn = lambda: N.call('oopao_gsc_optical_gains', gsc._plan, f, B, og, None, None, ws, nb, st)
+            for _ in range(3):
+                fn()
+            reps = 20
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            bp_bytes = n_modes * n * n * 4
+            row = {'batch': B, 'ms': ms, 'frames_per_s': B / ms * 1e3, 'bp_gbs': bp_bytes / ms / 1e6,
+                   'og_at_calibration_point_max_dev': float((og - 1).abs().max())}
+            if peaks.get('hbm_gbs'):
+                row['bp_hbm_frac_of_measured'] = row['bp_gbs'] / peaks['hbm_gbs']
+            rows.append(row)
+        entry = {'N': n, 'modes': n_modes, 'basis_product_mb': n_modes * n * n * 4 / 1e6,
+                 'calibration_s': t_cal, 'rows': rows}
+        if name == '20x20':
+            ref = G.OracleGSC(geom.mask, basis.astype(np.float64))
+            ref.calibration(frame.astype(np.float64))
+            t0 = time.perf_counter()
+            ref.compute_optical_gains(frame.astype(np.float64))
+            entry['oracle_cpu_ms_per_frame'] = (time.perf_counter() - t0) * 1e3
+        out[name] = entry
+        del gsc
+        torch.cuda.empty_cache()
+    return out
+
+
 def N_variant(wfs):
     from oopao_gb300 import _native as N
     return N.load().oopao_pwfs_get_variant(wfs.plan.h)
@@ -606,6 +669,7 @@ def run_ours(args):
         except Exception:
             pk = {'hbm_gbs': 6800.0, 'bf16_tflops': 1900.0}
         extra['dm_projection'] = dm_projection(pk)
+        extra['gsc'] = gsc_leg(pk)
 
     if rank == 0:
         line = {
@@ -686,6 +750,9 @@ def run_case(args):
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_pop()
         out = {'case': args.case, 'batch': args.batch, 'reps': args.reps, 'tc_status': dm.tensor_core_status()}
+    elif args.case == 'gsc':
+        hbm, _ = load_peaks()
+        out = {'case': args.case, 'gsc': gsc_leg({'hbm_gbs': hbm})}
     else:
         raise SystemExit('unknown case %s' % args.case)
     out['seconds'] = time.perf_counter() - t0
@@ -701,7 +768,7 @@ def main():
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline and accuracy legs')
     ap.add_argument('--no-extra', action='store_true',
                     help='skip the interaction-matrix comparisons and the closed-loop rate')
-    ap.add_argument('--case', default=None, help='run a small profiling workload (%s, dm40) instead'
+    ap.add_argument('--case', default=None, help='run a small profiling workload (%s, dm40, gsc) instead'
                     % ', '.join(CASES))
     ap.add_argument('--batch', type=int, default=16)
     ap.add_argument('--reps', type=int, default=3)

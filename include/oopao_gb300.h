@@ -284,6 +284,49 @@ int oopao_pwfs_signal_jvp(const oopao_pwfs_plan* plan, const float* frame0, int 
 int oopao_pwfs_signal_vjp(const oopao_pwfs_plan* plan, const float* frame0, int frame0_batch,
                           const float* sbar, int batch, float* fbar, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Gain-sensing camera: optical gains of the modulated pyramid from its
+ * full-resolution focal-plane frame (OOPAO/GainSensingCamera.py:13-199,
+ * Chambouleyron et al. 2021).  The plan holds the mask, its centred
+ * spectrum, the basis product (float32 [n_modes][n][n], the reference's
+ * split_basis_product :158-173 for a real basis) and the calibration.
+ * Sizes: n = mask size (even, prime factors <= 13).
+ * ------------------------------------------------------------------------ */
+typedef struct oopao_gsc_plan oopao_gsc_plan;
+enum { OOPAO_GSC_IR_CALIB = 0, OOPAO_GSC_SENSI_CALIB = 1, OOPAO_GSC_BASIS_PRODUCT = 2, OOPAO_GSC_MODE_POWER = 3 };
+/* GainSensingCamera.__init__ (:15-76).  mask_host: complex64 [n][n]
+ * (interleaved re, im), the pyramid's wfs.mask. */
+int oopao_gsc_plan_create(oopao_gsc_plan** plan, int n, int n_modes, const float* mask_host);
+int oopao_gsc_plan_destroy(oopao_gsc_plan* plan);
+/* Workspace of calibrate (batch 1) and optical_gains (batch frames). */
+size_t oopao_gsc_workspace_bytes(const oopao_gsc_plan* plan, int batch);
+/* Basis product of split_basis_product (:158-173) and padder (:140-147):
+ * basis: device float32 [n_modes][n0][n0] (the reference's [n0, n0, modes]
+ * transposed), zero-padded by (n - n0)/2 on each side.  Rows are stored
+ * divided by the mode's power (the gains do not depend on it).  Any
+ * workspace of at least n*n*8 bytes; larger ones transform more modes per
+ * launch. */
+int oopao_gsc_set_basis(oopao_gsc_plan* plan, const float* basis, int n0, void* workspace, size_t workspace_bytes,
+                        void* stream);
+/* calibration (:78-95): frame = device float32 [n][n] focal-plane frame at
+ * the working point (normalised to unit sum inside).  Stores IR_calib,
+ * ifft3(IR_calib) and sensi_calib in the plan. */
+int oopao_gsc_calibrate(oopao_gsc_plan* plan, const float* frame, void* workspace, size_t workspace_bytes,
+                        void* stream);
+/* compute_optical_gains (:104-120) for `batch` frames: frames device float32
+ * [batch][n][n]; og device float64 [batch][n_modes]; optional sensitivity
+ * device complex128 [batch][n_modes] (sensitivity(IR_sky, IR_calib)) and ir
+ * device float32 [batch][n][n] (IR_sky).  Status OOPAO_ERR_INVALID before
+ * a calibration. */
+int oopao_gsc_optical_gains(const oopao_gsc_plan* plan, const float* frames, int batch, double* og,
+                            double* sensitivity, float* ir, void* workspace, size_t workspace_bytes, void* stream);
+/* Device-to-device copy of a plan array: OOPAO_GSC_IR_CALIB float32 [n][n],
+ * OOPAO_GSC_SENSI_CALIB complex128 [n_modes], OOPAO_GSC_BASIS_PRODUCT
+ * float32 [n_modes][n][n] with each row divided by the mode's power,
+ * OOPAO_GSC_MODE_POWER float64 [n_modes] (sum of the mode's squares, which
+ * is also the row sum of its basis product). */
+int oopao_gsc_read(const oopao_gsc_plan* plan, int what, void* dst, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

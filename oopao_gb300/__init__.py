@@ -22,6 +22,7 @@ from .pyramid import Pyramid
 from .calibration import InteractionMatrix, CalibrationVault
 from .atmosphere import Atmosphere
 from .bioedge import BioEdge
+from .gain_sensing import GainSensingCamera
 
 __all__ = ['OopaoError', 'warning', 'Source', 'Telescope', 'Detector', 'DeformableMirror', 'Pyramid',
-           'InteractionMatrix', 'CalibrationVault', 'Atmosphere', 'BioEdge']
+           'InteractionMatrix', 'CalibrationVault', 'Atmosphere', 'BioEdge', 'GainSensingCamera']

@@ -66,6 +66,14 @@ SIGNATURES = {
                                c_void_p]),
     'oopao_pwfs_signal_jvp': (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     'oopao_pwfs_signal_vjp': (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),
+    'oopao_gsc_plan_create': (c_int, [P(c_void_p), c_int, c_int, c_void_p]),
+    'oopao_gsc_plan_destroy': (c_int, [c_void_p]),
+    'oopao_gsc_workspace_bytes': (c_size_t, [c_void_p, c_int]),
+    'oopao_gsc_set_basis': (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_size_t, c_void_p]),
+    'oopao_gsc_calibrate': (c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    'oopao_gsc_optical_gains': (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                        c_size_t, c_void_p]),
+    'oopao_gsc_read': (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
 }
 
 _lib = None

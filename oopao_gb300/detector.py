@@ -71,15 +71,61 @@ class Detector:
     def integrate(self, frame):
         """``Detector.integrate`` + ``readout`` (OOPAO/Detector.py:331-354) for a
         frame computed outside the WFS camera path (the focal-plane camera):
-        the frame is kept as ``perfect_frame``, then QE, noise and gain apply."""
+        the frame is kept as ``perfect_frame``, then QE, noise and gain apply.
+        A device tensor stays on the device."""
         self._unsupported()
-        self.perfect_frame = np.array(frame, dtype=np.float64)
+        if isinstance(frame, torch.Tensor):
+            t = frame.to(torch.float32)
+            self._perfect_dev, self._perfect_host = t, None
+            self._set_device_frame(self._integrate_device(t[None]))
+            return
+        self._perfect_dev, self._perfect_host = None, np.array(frame, dtype=np.float64)
         if self.photonNoise or self.readoutNoise != 0 or self.QE != 1 or self.gain != 1:
             dev = torch.device('cuda', torch.cuda.current_device())
             t = torch.as_tensor(np.ascontiguousarray(frame, dtype=np.float32), device=dev)[None]
             self._set_device_frame(self._integrate_device(t))
         else:
-            self.frame = self.perfect_frame.copy()
+            self.frame = self._perfect_host.copy()
+
+    @property
+    def perfect_frame(self):
+        if getattr(self, '_perfect_host', None) is None and getattr(self, '_perfect_dev', None) is not None:
+            self._perfect_host = self._perfect_dev.detach().to('cpu', torch.float64).numpy()
+        return getattr(self, '_perfect_host', None)
+
+    @property
+    def device_frame(self):
+        """The frame as a float32 device tensor ([cam, cam], or [B, cam, cam])."""
+        if self._frame_dev is not None:
+            t = self._frame_dev
+            return t[0] if t.ndim == 3 and t.shape[0] == 1 else t
+        if self._frame_host is None:
+            return None
+        return torch.as_tensor(np.ascontiguousarray(self._frame_host, dtype=np.float32),
+                               device=torch.device('cuda', torch.cuda.current_device()))
+
+    def properties(self):
+        """Display lines of the camera (the reference's ``properties``, :361-383)."""
+        return {'resolution': f'{"Resolution [px]":<25s}|{str(self.resolution):^9s}',
+                'qe': f'{"Quantum efficiency":<25s}|{self.QE:^9.2f}',
+                'gain': f'{"Gain":<25s}|{str(self.gain):^9s}',
+                'photon': f'{"Photon noise":<25s}|{str(self.photonNoise):^9s}',
+                'ron': f'{"Readout noise [e-]":<25s}|{float(self.readoutNoise):^9.1f}'}
+
+    def __mul__(self, obj):
+        """Camera * GainSensingCamera (OOPAO/Detector.py:385-393): the first
+        product calibrates, the next ones compute the optical gains."""
+        if getattr(obj, 'tag', None) == 'GSC':
+            frame = self.device_frame
+            if frame is None:
+                raise OopaoError('The camera has no frame yet')
+            if obj.calibration_ready is False:
+                obj.calibration(frame)
+                obj.detector_properties = self.properties()
+            else:
+                obj.compute_optical_gains(frame)
+            return
+        raise OopaoError(f'Coupled object should be a "GSC" but is {getattr(obj, "tag", type(obj).__name__)}')
 
     def _set_device_frame(self, t):
         self._frame_dev = t

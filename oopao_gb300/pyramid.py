@@ -417,11 +417,9 @@ class Pyramid:
                N.ptr(ws), nb, N.stream_handle())
         return frame, raw
 
-    def focal_plane_image(self):
-        """Sum over modulation points of |F_k/N|^2 for the last measured wavefront
-        (the intensity the reference's focal-plane camera reads from
-        modulation_camera_em, OOPAO/Pyramid.py:642, :1182-1190), [N,N] float64.
-        In the 1-pixel-centred branch the field carries the spatial filter."""
+    def _focal_device(self):
+        """Sum over modulation points of |F_k/N|^2 for the last measured
+        wavefront, float32 device tensor [N,N] (or [B,N,N])."""
         last = getattr(self, '_last_measure', None)
         if last is None:
             raise OopaoError('No wavefront measured yet')
@@ -431,7 +429,14 @@ class Pyramid:
         if not self.psfCentering and self.spatialFilter is not None:
             f = torch.as_tensor(np.abs(np.asarray(self.spatialFilter)) ** 2, dtype=torch.float32, device=self._dev)
             img = img * f
-        a = img.double().cpu().numpy()
+        return img
+
+    def focal_plane_image(self):
+        """Sum over modulation points of |F_k/N|^2 for the last measured wavefront
+        (the intensity the reference's focal-plane camera reads from
+        modulation_camera_em, OOPAO/Pyramid.py:642, :1182-1190), [N,N] float64.
+        In the 1-pixel-centred branch the field carries the spatial filter."""
+        a = self._focal_device().double().cpu().numpy()
         return np.moveaxis(a, 0, -1) if a.ndim == 3 else a
 
     def get_modulation_frame(self, radius=6, norma=True):
@@ -647,9 +652,9 @@ class Pyramid:
             if obj.is_focal_plane_camera:
                 # OOPAO/Pyramid.py:1182-1190: centred crop of the focal-plane
                 # intensity to the camera size, then the camera's integration
-                intensity = self.focal_plane_image()
+                intensity = self._focal_device()
                 if intensity.ndim == 3:
-                    intensity = intensity.sum(axis=2)
+                    intensity = intensity.sum(dim=0)
                 n = intensity.shape[0]
                 if obj.resolution > self.resolution:
                     frame = intensity

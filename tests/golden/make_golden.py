@@ -293,6 +293,48 @@ def case_kl(OOPAO, name, res, n_subap, r0=0.15, L0=25.0):
     print(name, 'M2C', rec['m2c'].shape)
 
 
+GSC_CASES = [('gsc_tiny', dict(res=24, n_subap=4, modulation=3, n_modes=12)),
+             ('gsc_small', dict(res=40, n_subap=10, modulation=2, n_modes=40))]
+
+
+def case_gsc(OOPAO, name, res, n_subap, modulation, n_modes, light_ratio=0.5, seed=7):
+    """GainSensingCamera: calibration on the flat-wavefront focal-plane frame,
+    optical gains on a screen, following the reference's GSC tutorial (basis =
+    tel.OPD of a DM mode set, full-resolution focal-plane camera)."""
+    import json
+    from OOPAO.GainSensingCamera import GainSensingCamera
+    tel, ngs, dm, wfs = build(OOPAO, res, n_subap, modulation, light_ratio)
+    rng = np.random.default_rng(seed)
+    m2c = rng.standard_normal((dm.nValidAct, n_modes)) * 20e-9
+    with _quiet():
+        dm.coefs = m2c
+        ngs ** tel * dm
+        basis = np.array(tel.OPD)
+        dm.coefs = 0
+        gsc = GainSensingCamera(mask=wfs.mask, basis=basis)
+        wfs.focal_plane_camera.resolution = wfs.nRes
+        ngs ** tel * wfs
+        wfs * wfs.focal_plane_camera
+        calib_frame = np.array(wfs.focal_plane_camera.frame)
+        wfs.focal_plane_camera * gsc
+    sky_opd = screen(res, seed + 1, 1.5) * tel.pupil * ngs.wavelength / (2 * np.pi)
+    with _quiet():
+        ngs ** tel
+        # tel.OPD alone would be reset by the relay (OPD = OPD_no_pupil * pupil)
+        tel.OPD_no_pupil = sky_opd
+        tel * wfs
+        wfs * wfs.focal_plane_camera
+        sky_frame = np.array(wfs.focal_plane_camera.frame)
+        wfs.focal_plane_camera * gsc
+    rec = dict(params=json.dumps(dict(res=res, n_subap=n_subap, modulation=modulation, n_modes=n_modes,
+                                      light_ratio=light_ratio)),
+               m2c=m2c, basis=basis, mask=np.array(wfs.mask), sky_opd=sky_opd, calib_frame=calib_frame,
+               sky_frame=sky_frame, ir_calib=np.array(gsc.IR_calib), ir_sky=np.array(gsc.IR_sky),
+               sensi_calib=np.array(gsc.sensi_calib), og=np.array(gsc.og), N=wfs.resolution)
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **rec)
+    print(name, 'N', rec['N'], 'modes', n_modes, 'og', rec['og'][:4])
+
+
 BIOEDGE_CASES = [
     ('bioedge_tiny', (24, 4, 3, 0.5), {}),
     ('bioedge_grey', (32, 4, 2, 0.3), dict(grey_width=1.0, quadrants_numbering=[2, 3, 0, 1], n_pix_separation=4,
@@ -328,6 +370,9 @@ def main():
     for name, args, kw in BIOEDGE_CASES:
         if not only or name in only:
             case_bioedge(OOPAO, name, *args, **kw)
+    for name, kw in GSC_CASES:
+        if not only or name in only:
+            case_gsc(OOPAO, name, **kw)
     if not only or any(n in only for n, _ in KL_CASES):
         from refimport import install_kl_shims
         install_kl_shims()
