@@ -628,8 +628,10 @@ def run_ours(args):
     barrier()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     ns = wfs.nSignal
-    h2d = m2c.size * 4 + ns * NMODES * 8      # commands (float32) + D for the FP64 SVD
-    d2h = ns * NMODES * 4 + (ns * NMODES + NMODES + NMODES * NMODES) * 8  # D + U, s, V
+    # host -> device: commands (float32), D for the float64 vault, the Gram eigenvectors
+    h2d = m2c.size * 4 + ns * NMODES * 8 + NMODES * NMODES * 8
+    # device -> host: D (float64), the Gram matrix, and the vault's U, s, V, D, M, Mtrunc, Dtrunc
+    d2h = ns * NMODES * 8 + NMODES * NMODES * 8 + (5 * ns * NMODES + NMODES + NMODES * NMODES) * 8
     e2e = {'value': frames_step * world / e2e_s, 'unit': 'frames/s', 'h2d_bytes_per_step': int(h2d),
            'd2h_bytes_per_step': int(d2h), 'im_build_ms': e2e_s * 1000.0,
            'api': 'InteractionMatrix(..., single_pass=False, nTrunc=20)'}
