@@ -85,6 +85,10 @@ int oopao_pwfs_set_pass_budget(oopao_pwfs_plan* plan, size_t bytes);
  * returns OOPAO_ERR_UNSUPPORTED.  variant_info fills info[6] with
  * (R1, R2, threads per line, row / column / row-inverse lines per CTA). */
 int oopao_pwfs_set_variant(oopao_pwfs_plan* plan, int variant);
+/* Device status word of the plan's kernels, read synchronously and reset:
+ * 0, or the code of a bounded wait that timed out (the kernel then stopped
+ * without finishing its work; the results of that call are invalid). */
+int oopao_pwfs_device_status(oopao_pwfs_plan* plan, int* code);
 int oopao_pwfs_get_variant(const oopao_pwfs_plan* plan);
 int oopao_pwfs_num_variants(const oopao_pwfs_plan* plan);
 int oopao_pwfs_variant_info(const oopao_pwfs_plan* plan, int variant, int* info);

@@ -30,6 +30,7 @@ SIGNATURES = {
     'oopao_pwfs_set_pass_budget': (c_int, [c_void_p, c_size_t]),
     'oopao_pwfs_set_variant': (c_int, [c_void_p, c_int]),
     'oopao_pwfs_get_variant': (c_int, [c_void_p]),
+    'oopao_pwfs_device_status': (c_int, [c_void_p, c_void_p]),
     'oopao_pwfs_num_variants': (c_int, [c_void_p]),
     'oopao_pwfs_variant_info': (c_int, [c_void_p, c_int, c_void_p]),
     'oopao_pwfs_workspace_bytes': (c_size_t, [c_void_p, c_int]),

@@ -99,6 +99,8 @@ struct oopao_pwfs_plan {
   const struct FastPasses* fast;  // compile-time plan for n, or null (generic kernels)
   int variant;                    // 1 = use `fast` when available, 0 = generic
   int inv_target_ctas;            // row-inverse CTAs wanted per launch (2 resident waves)
+  int cols3_ctas;                 // resident CTAs of the persistent column pass (0 = not used)
+  int* d_err;                     // device error word (bounded waits of the persistent column pass)
   // signal processing
   int sp_mode, nq, n2d, n_signal, cam2;
   int q_r0[4], q_c0[4];
@@ -178,6 +180,9 @@ struct ColsArgs {
   // into [B][n][n] (atomic adds), or null
   float* focal;
   float focal_scale;
+  // persistent column pass (pwfs_cols3): items in this pass, error word
+  int items;
+  int* err;
 };
 
 __global__ void __launch_bounds__(kThreads) pwfs_cols(ColsArgs a) {
@@ -277,7 +282,8 @@ int fast_candidates(int n, const FastPasses** out) {
   static const FastPasses f264[] = {make_fast<264, 24, 11, 12, 16, 16, 12>(),
                                     make_fast<264, 24, 11, 24, 8, 8, 12>(),
                                     make_fast<264, 11, 24, 12, 16, 16, 12>(),
-                                    make_fast<264, 12, 22, 12, 16, 16, 12>()};
+                                    make_fast<264, 12, 22, 12, 16, 16, 12>(),
+                                    make_fast3<264, 12, 22, 12, 16, 16, 12, 8>()};
   static const FastPasses f480[] = {make_fast<480, 24, 20, 12, 16, 8, 12>()};
   static const FastPasses f504[] = {make_fast<504, 24, 21, 12, 16, 8, 12>(),
                                     make_fast<504, 24, 21, 24, 8, 8, 12>(),
@@ -323,8 +329,10 @@ const FastPasses* fast_passes(int n, int idx = 0) {
 }
 
 // Opt the variant's kernels into their shared memory and return, in
-// *inv_target, two resident waves of row-inverse CTAs on this device.
-cudaError_t fast_attrs(const FastPasses* f, int* inv_target) {
+// *inv_target, two resident waves of row-inverse CTAs on this device and, in
+// *cols3_ctas, the resident CTAs of its persistent column pass for pupils of
+// `res` pixels (0 when the variant has none or res is above a TMA box).
+cudaError_t fast_attrs(const FastPasses* f, int res, int* inv_target, int* cols3_ctas) {
   cudaError_t e = cudaFuncSetAttribute(f->rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->smem_rows);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(f->cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->smem_cols);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(f->inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->smem_inv);
@@ -333,7 +341,38 @@ cudaError_t fast_attrs(const FastPasses* f, int* inv_target) {
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, f->inv, f->t * f->l_inv, f->smem_inv);
   if (e == cudaSuccess) *inv_target = 2 * sms * std::max(occ, 1);
+  *cols3_ctas = 0;
+  if (e == cudaSuccess && f->cols3 && res <= 256) {
+    const size_t sm3 = f->smem_cols3(res);
+    int occ3 = 0;
+    e = cudaFuncSetAttribute(f->cols3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ3, f->cols3, f->t * f->l_cols3, sm3);
+    if (e == cudaSuccess) *cols3_ctas = occ3 * sms;
+  }
   return e;
+}
+
+// 2-D TMA map of the row transforms Y [rows][n] complex64, viewed as float32
+// pairs, with [res][l3] boxes (l3 columns of res rows).
+int encode_y_map(CUtensorMap* map, const float2* y, int n, size_t rows, int l3, int res) {
+  PFN_cuTensorMapEncodeTiled_v12000 fn = tma::encode_fn();
+  if (!fn) {
+    oopao_set_last_error("cuTensorMapEncodeTiled is not available from the driver", __FILE__, __LINE__);
+    return OOPAO_ERR_CUDA;
+  }
+  const cuuint64_t dims[2] = {(cuuint64_t)2 * n, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)n * sizeof(float2)};
+  const cuuint32_t box[2] = {(cuuint32_t)(2 * l3), (cuuint32_t)res};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float2*>(y), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    oopao_set_last_error("cuTensorMapEncodeTiled rejected the row-transform map", __FILE__, __LINE__);
+    return OOPAO_ERR_INVALID;
+  }
+  return OOPAO_OK;
 }
 }  // namespace
 
@@ -499,6 +538,7 @@ void free_plan(oopao_pwfs_plan* p) {
   cudaFree(p->d_valid);
   cudaFree(p->d_ref2d);
   cudaFree(p->d_sig_index);
+  cudaFree(p->d_err);
   free(p);
 }
 
@@ -623,7 +663,10 @@ extern "C" int oopao_pwfs_plan_create(oopao_pwfs_plan** out, int res, int n, int
   p->fast = fast_passes(n, fast_default_index(n));
   p->variant = p->fast ? fast_default_index(n) + 1 : 0;
   p->inv_target_ctas = kTargetCtas;
-  if (p->fast && e == cudaSuccess) e = fast_attrs(p->fast, &p->inv_target_ctas);
+  p->cols3_ctas = 0;
+  if (e == cudaSuccess) e = cudaMalloc((void**)&p->d_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(p->d_err, 0, sizeof(int));
+  if (p->fast && e == cudaSuccess) e = fast_attrs(p->fast, res, &p->inv_target_ctas, &p->cols3_ctas);
   if (e != cudaSuccess) {
     oopao_set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
     free_plan(p);
@@ -845,7 +888,18 @@ int measure_impl(const oopao_pwfs_plan* p, const float* opd, double phase_scale,
                   res, n, k0, kc, ng, p->off, p->cols_per_cta,
                   focal ? focal + (size_t)b0 * n * n : nullptr, (float)((double)n * n)};
       mark(1);
-      if (f) {
+      if (f && p->cols3_ctas > 0) {
+        // persistent column pass: each CTA keeps one column block's mask and
+        // streams its Y tiles with TMA over the (item, point) units
+        CUtensorMap ymap;
+        const int es = encode_y_map(&ymap, y, n, (size_t)bc * ng * res, f->l_cols3, res);
+        if (es) return es;
+        ca.items = bc;
+        ca.err = p->d_err;
+        const int blocks = n / f->l_cols3;
+        const int per = std::max(1, std::min(bc * kc, p->cols3_ctas / blocks));
+        f->cols3<<<dim3(blocks, per), f->t * f->l_cols3, f->smem_cols3(res), st>>>(ymap, ca);
+      } else if (f) {
         dim3 g2(ceil_div(n, f->l_cols), kc, bc);
         f->cols<<<g2, f->t * f->l_cols, f->smem_cols, st>>>(ca);
       } else {
@@ -1392,12 +1446,20 @@ extern "C" int oopao_pwfs_set_variant(oopao_pwfs_plan* p, int variant) {
   }
   if (variant >= 1) {
     const FastPasses* f = c + (variant - 1);
-    int target = kTargetCtas;
-    OOPAO_CUDA_TRY(fast_attrs(f, &target));
+    int target = kTargetCtas, c3 = 0;
+    OOPAO_CUDA_TRY(fast_attrs(f, p->res, &target, &c3));
     p->fast = f;
     p->inv_target_ctas = target;
+    p->cols3_ctas = c3;
   }
   p->variant = variant;
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_pwfs_device_status(oopao_pwfs_plan* p, int* code) {
+  OOPAO_CHECK_ARG(p && code, "NULL argument");
+  OOPAO_CUDA_TRY(cudaMemcpy(code, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  OOPAO_CUDA_TRY(cudaMemset(p->d_err, 0, sizeof(int)));
   return OOPAO_OK;
 }
 

@@ -4,6 +4,7 @@
 // registers.
 #pragma once
 #include "fft2.cuh"
+#include "tma.cuh"
 
 __host__ __device__ constexpr int odd_up(int v) { return (v % 2 == 0) ? v + 1 : v; }
 __host__ __device__ constexpr int imax(int a, int b) { return a > b ? a : b; }
@@ -239,6 +240,164 @@ __global__ void __launch_bounds__(T* L) pwfs_cols2(ColsArgs a) {
   }
 }
 
+// ---- pass 2, persistent form ----
+// A CTA owns a block of L columns for the whole pass: it loads that block of
+// the mask into shared memory once, then loops over (item, point) units,
+// bringing each unit's [res][L] tile of Y in with a TMA load issued one unit
+// ahead (two tile buffers, one mbarrier each).  The per-unit arithmetic is
+// that of pwfs_cols2; global traffic per unit is the Y tile in and Z out.
+__host__ __device__ constexpr size_t align128(size_t v) { return (v + 127) / 128 * 128; }
+
+template <int N, int R1, int R2, int T, int L>
+struct Cols3Smem {
+  static constexpr int LAY1 = cols_layout(R1, R2, T, L), LAY2 = cols_layout(R2, R1, T, L);
+  static constexpr int LS1 = LAY1 & 0xFFFF, LS2 = LAY2 & 0xFFFF;
+  static constexpr bool ALIAS = (R1 + T - 1) / T == 1;
+  static constexpr size_t kXchFloat2 = (size_t)(ALIAS ? imax(LS1, LS2) : LS1 + LS2) * L;
+  static constexpr size_t kBars = 0;                                  // 2 mbarriers
+  static constexpr size_t kTw = 128;                                  // tw[N], twi[N]
+  static constexpr size_t kMask = kTw + 2 * (size_t)N * 8;            // mask block [N][L]
+  static constexpr size_t kXch = kMask + (size_t)N * L * 8;           // exchange
+  static constexpr size_t kY = align128(kXch + kXchFloat2 * 8);       // two Y tiles
+  static __host__ __device__ size_t ytile(int res) { return align128((size_t)res * L * 8); }
+  static size_t bytes(int res) { return kY + 2 * ytile(res); }
+};
+
+template <int N, int R1, int R2, int T, int L>
+__global__ void __launch_bounds__(T* L) pwfs_cols3(const __grid_constant__ CUtensorMap ymap, ColsArgs a) {
+  using S = Cols3Smem<N, R1, R2, T, L>;
+  constexpr int R1P = S::LAY1 >> 16, LS1 = S::LS1;
+  constexpr int R2P = S::LAY2 >> 16, LS2 = S::LS2;
+  constexpr int PBA = (R2 + T - 1) / T;   // forward stage A / inverse stage B' butterflies
+  constexpr int PBB = (R1 + T - 1) / T;   // forward stage B / inverse stage A' butterflies
+  constexpr bool ALIAS = S::ALIAS;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smraw + S::kBars);
+  float2* tw = reinterpret_cast<float2*>(smraw + S::kTw);  // tw[m*R1 + j] = W_N^{j m}
+  float2* twi = tw + N;                                      // twi[m*R2 + j] = W_N^{-j m}
+  float2* mt = reinterpret_cast<float2*>(smraw + S::kMask); // mt[row*L + l] = mask[row][c0 + l]
+  float2* b1 = reinterpret_cast<float2*>(smraw + S::kXch);
+  float2* b2 = ALIAS ? b1 : b1 + L * LS1;
+  const int res = a.res, off = a.off;
+  float2* ybuf0 = reinterpret_cast<float2*>(smraw + S::kY);
+  float2* ybuf1 = reinterpret_cast<float2*>(smraw + S::kY + S::ytile(res));
+  const int tid = threadIdx.x;
+  const int l = tid % L, t = tid / L;
+  const int c0 = blockIdx.x * L, c = c0 + l;
+  for (int i = tid; i < N; i += T * L) {
+    tw[i] = a.tw[(i % R1) * (i / R1)];
+    const float2 w = a.tw[(i % R2) * (i / R2)];
+    twi[i] = make_float2(w.x, -w.y);
+  }
+  for (int i = tid; i < N * L; i += T * L) mt[i] = a.mask[(size_t)(i / L) * N + c0 + i % L];
+  if (tid == 0) {
+    tma::mbar_init(&bar[0], 1);
+    tma::mbar_init(&bar[1], 1);
+    tma::mbar_init_fence();
+  }
+  __syncthreads();
+  const int units = a.items * a.kp, P = gridDim.y;
+  const uint32_t tile_bytes = (uint32_t)res * L * 8;
+  auto issue = [&](int u, int s) {
+    const int b = u / a.kp, kk = u - (u / a.kp) * a.kp;
+    const int g = a.group ? a.group[a.k0 + kk] : kk;
+    tma::mbar_expect_tx(&bar[s], tile_bytes);
+    tma::load_2d(s ? ybuf1 : ybuf0, &ymap, &bar[s], 2 * c0, (b * a.ng + g) * res);
+  };
+  int u = blockIdx.y, it = 0;
+  bool ok = true;
+  if (tid == 0 && u < units) issue(u, 0);
+  for (; u < units; u += P, it++) {
+    const int s = it & 1;
+    // the other buffer was last read before the previous unit's first barrier
+    if (tid == 0 && u + P < units) {
+      tma::fence_proxy_async();
+      issue(u + P, s ^ 1);
+    }
+    const bool arrived = tma::mbar_wait(&bar[s], (uint32_t)((it >> 1) & 1), a.err, 11);
+    if (!__syncthreads_and(arrived)) {
+      ok = false;
+      break;
+    }
+    const int b = u / a.kp, kk = u - (u / a.kp) * a.kp;
+    const int kabs = a.k0 + kk;
+    const float2* yt = (s ? ybuf1 : ybuf0) + l;  // yt[i*L]: row i of this column
+    const float2* cf = a.colfac + (size_t)kabs * res;
+    float2* x1 = b1 + l * LS1;
+    float2* x2 = b2 + l * LS2;
+    // forward stage A: rows e = j + m*R2, non-zero for off <= e < off + res
+#pragma unroll
+    for (int p = 0; p < PBA; p++) {
+      const int j = t + p * T;
+      if (j < R2) {
+        float2 v[R1];
+#pragma unroll
+        for (int m = 0; m < R1; m++) {
+          const int i = j + m * R2 - off;
+          v[m] = (i >= 0 && i < res) ? cmul(yt[i * L], cf[i]) : make_float2(0.f, 0.f);
+        }
+        dft<R1, false>(v);
+#pragma unroll
+        for (int q = 0; q < R1; q++) x1[j * R1P + q] = v[q];
+      }
+    }
+    __syncthreads();
+    // forward stage B, mask (from shared memory), inverse stage A'
+#pragma unroll
+    for (int p = 0; p < PBB; p++) {
+      const int j = t + p * T;
+      float2 v[R2];
+      if (j < R1) {
+#pragma unroll
+        for (int m = 0; m < R2; m++) {
+          const float2 w = x1[m * R1P + j];
+          v[m] = (m == 0) ? w : cmul(w, tw[m * R1 + j]);
+        }
+        dft<R2, false>(v);
+        if (a.focal) {
+          float* fo = a.focal + (size_t)b * N * N + c;
+#pragma unroll
+          for (int q = 0; q < R2; q++) atomicAdd(fo + (size_t)(j + q * R1) * N, a.focal_scale * cabs2(v[q]));
+        }
+#pragma unroll
+        for (int q = 0; q < R2; q++) v[q] = cmul(v[q], mt[(j + q * R1) * L + l]);
+        dft<R2, true>(v);
+      }
+      if constexpr (ALIAS) __syncthreads();  // every read of the forward exchange is done
+      if (j < R1) {
+#pragma unroll
+        for (int q = 0; q < R2; q++) x2[j * R2P + q] = v[q];
+      }
+    }
+    __syncthreads();
+    // inverse stage B' (radix R1, span R2): outputs rows j + q*R2
+    float2* z = a.z + ((size_t)b * a.kp + kk) * N * N + c;
+#pragma unroll
+    for (int p = 0; p < PBA; p++) {
+      const int j = t + p * T;
+      if (j < R2) {
+        float2 v[R1];
+#pragma unroll
+        for (int m = 0; m < R1; m++) {
+          const float2 w = x2[m * R2P + j];
+          v[m] = (m == 0) ? w : cmul(w, twi[m * R2 + j]);
+        }
+        dft<R1, true>(v);
+#pragma unroll
+        for (int q = 0; q < R1; q++) z[(size_t)(j + q * R2) * N] = v[q];
+      }
+    }
+    // the next unit's first barrier (after its wait) orders these exchange
+    // reads before its stage-A writes
+  }
+  if (!ok && tid == 0) {
+    // a wait timed out: give the loads still in flight a bounded chance to
+    // land before the CTA's shared memory is released
+    tma::mbar_wait(&bar[it & 1], (uint32_t)((it >> 1) & 1), nullptr, 0);
+    if (u + P < units) tma::mbar_wait(&bar[(it + 1) & 1], (uint32_t)(((it + 1) >> 1) & 1), nullptr, 0);
+  }
+}
+
 // Row-inverse exchange: double-buffered over modulation points (one barrier
 // per point) while both buffers fit in ~110 KB; a single buffer with a second
 // barrier per point above that, so that two CTAs still share an SM.
@@ -356,6 +515,10 @@ struct FastPasses {
   void (*cols)(ColsArgs);
   void (*inv)(RowsInvArgs);
   size_t smem_rows, smem_cols, smem_inv;
+  // persistent column pass (null when the variant has none): L3 columns per CTA
+  int l_cols3;
+  void (*cols3)(const CUtensorMap, ColsArgs);
+  size_t (*smem_cols3)(int res);
 };
 
 template <int N, int R1, int R2, int T, int LR, int LC, int LI>
@@ -374,5 +537,19 @@ FastPasses make_fast() {
   f.smem_rows = sizeof(float2) * (N + (size_t)LR * LSR);
   f.smem_cols = sizeof(float2) * (2 * N + (size_t)LC * LSC);
   f.smem_inv = sizeof(float2) * (N + (inv_double_buffer(N, LI, LSI) ? 2 : 1) * (size_t)LI * LSI);
+  f.l_cols3 = 0;
+  f.cols3 = nullptr;
+  f.smem_cols3 = nullptr;
+  return f;
+}
+
+// make_fast plus the persistent TMA column pass with L3 columns per CTA.
+template <int N, int R1, int R2, int T, int LR, int LC, int LI, int L3>
+FastPasses make_fast3() {
+  static_assert(N % L3 == 0 && (2 * L3 * 4) % 16 == 0, "column blocks must tile N in 16-byte TMA rows");
+  FastPasses f = make_fast<N, R1, R2, T, LR, LC, LI>();
+  f.l_cols3 = L3;
+  f.cols3 = pwfs_cols3<N, R1, R2, T, L3>;
+  f.smem_cols3 = &Cols3Smem<N, R1, R2, T, L3>::bytes;
   return f;
 }
