@@ -382,6 +382,106 @@ def gsc_leg(peaks):
     return out
 
 
+def _event_ms(fn, reps, warm=3):
+    import torch
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def next_rows_leg():
+    """The components either side of the path, each against its float64 CPU
+    counterpart (the oracle, i.e. the reference's algorithm in numpy):
+
+    * BioEdge on the 20x20 configuration (120 px, N=264, 48 points, 4 Fourier
+      masks): frames/s at batch 100 of random screens; oracle s per frame.
+    * Atmosphere update (infinite screens, frozen flow, on the GPU): us per
+      update for 1 layer at 120 px (10 m/s), 3 layers at 240 px (0/5/10 km,
+      10/15/20 m/s) and 35 layers at 480 px (the 39 m configuration's
+      profile size); oracle ms per update at 120 px and 240 px.
+    * KL modal basis (compute_KL_basis, HHt on the GPU): seconds for the
+      21x21 (357 actuators) and 41x41 (1353 actuators) DMs."""
+    import types
+    import torch
+    import oopao_gb300 as og
+    from oopao_gb300.modal_basis import compute_KL_basis
+    from oracle import atm_oracle as A
+    from oracle import bioedge_oracle as BO
+    from oracle import pwfs_oracle as O
+    out = {}
+    # ---- BioEdge
+    with _quiet():
+        tel = og.Telescope(resolution=120, diameter=8.0, samplingTime=1e-3)
+        ngs = og.Source(optBand='V0', magnitude=8)
+        ngs * tel
+        wfs = og.BioEdge(nSubap=20, telescope=tel, modulation=3, lightRatio=0.5, nTheta_user_defined=48,
+                         max_batch=100)
+    ngs ** tel
+    g = torch.Generator(device='cuda').manual_seed(0)
+    opd = torch.randn((100, 120, 120), device='cuda', generator=g) * 50e-9
+    scale = 2 * np.pi / ngs.wavelength
+    ms = _event_ms(lambda: wfs._measure_frames(opd, scale), 5)
+    inten = O.source_intensity(O.telescope_pupil(120), O.n_photon('V0', 8), 1e-3, 8.0)
+    ob = BO.build_bioedge(120, 20, 3, 0.5, inten, n_theta_user=48)
+    ph = np.random.default_rng(1).standard_normal((120, 120)) * 0.3
+    t0 = time.perf_counter()
+    ob.frame(ph)
+    t_or = time.perf_counter() - t0
+    out['bioedge_20x20'] = {'frames_per_s': 100 / ms * 1e3, 'ms_per_100_frames': ms, 'masks': 4,
+                            'oracle_s_per_frame': t_or, 'speedup_vs_oracle': t_or / (ms / 100 / 1e3)}
+    del wfs
+    # ---- Atmosphere
+    rows = []
+    cases = (('1 layer, 120 px', 120, 8.0, [1.0], [10.], [0.], [0.]),
+             ('3 layers, 240 px', 240, 8.0, [1 / 3] * 3, [10., 15., 20.], [0., 72., 144.], [0., 5000., 10000.]),
+             ('35 layers, 480 px', 480, 39.0, [1 / 35] * 35, list(np.linspace(5., 30., 35)),
+              list(np.linspace(0., 340., 35)), list(np.linspace(0., 20000., 35))))
+    for name, res, D, fr, ws, wd, alt in cases:
+        with _quiet():
+            t = og.Telescope(resolution=res, diameter=D, samplingTime=1e-3)
+            s = og.Source(optBand='V0', magnitude=8)
+            s * t
+            atm = og.Atmosphere(telescope=t, r0=0.15, L0=25, fractionalR0=fr, windSpeed=ws, windDirection=wd,
+                                altitude=alt)
+            atm.initializeAtmosphere(t)
+        atm.prepare(260)
+        us = _event_ms(atm.update, 200, warm=10) * 1e3
+        row = {'case': name, 'us_per_update': us, 'status': atm.status()}
+        if res <= 240:
+            oa = A.OracleAtmosphere(res, D, 1e-3, 0.15, 25.0, fr, ws, wd, alt)
+            oa.update()
+            t0 = time.perf_counter()
+            for _ in range(5):
+                oa.update()
+            row['oracle_ms_per_update'] = (time.perf_counter() - t0) / 5 * 1e3
+        rows.append(row)
+        del atm
+    out['atmosphere'] = rows
+    # ---- KL basis
+    kl = []
+    for nsub, res in ((20, 120), (40, 240)):
+        pupil = O.telescope_pupil(res)
+        modes = O.dm_modes(res, 8.0, nsub)
+        tel_ = types.SimpleNamespace(pupil=pupil, resolution=res, D=8.0)
+        atm_ = types.SimpleNamespace(r0=0.15, L0=25.0)
+        dm_ = types.SimpleNamespace(modes=modes, nValidAct=modes.shape[1], isM4=False)
+        t0 = time.perf_counter()
+        m2c = compute_KL_basis(tel_, atm_, dm_)
+        torch.cuda.synchronize()
+        kl.append({'dm': '%dx%d' % (nsub + 1, nsub + 1), 'actuators': modes.shape[1], 'modes': m2c.shape[1],
+                   'seconds': time.perf_counter() - t0})
+    out['kl_basis'] = kl
+    torch.cuda.empty_cache()
+    return out
+
+
 def N_variant(wfs):
     from oopao_gb300 import _native as N
     return N.load().oopao_pwfs_get_variant(wfs.plan.h)
@@ -672,6 +772,7 @@ def run_ours(args):
             pk = {'hbm_gbs': 6800.0, 'bf16_tflops': 1900.0}
         extra['dm_projection'] = dm_projection(pk)
         extra['gsc'] = gsc_leg(pk)
+        extra['next_rows'] = next_rows_leg()
 
     if rank == 0:
         line = {
@@ -752,6 +853,8 @@ def run_case(args):
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_pop()
         out = {'case': args.case, 'batch': args.batch, 'reps': args.reps, 'tc_status': dm.tensor_core_status()}
+    elif args.case == 'next':
+        out = {'case': args.case, 'next_rows': next_rows_leg()}
     elif args.case == 'gsc':
         hbm, _ = load_peaks()
         out = {'case': args.case, 'gsc': gsc_leg({'hbm_gbs': hbm})}
@@ -770,7 +873,7 @@ def main():
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline and accuracy legs')
     ap.add_argument('--no-extra', action='store_true',
                     help='skip the interaction-matrix comparisons and the closed-loop rate')
-    ap.add_argument('--case', default=None, help='run a small profiling workload (%s, dm40, gsc) instead'
+    ap.add_argument('--case', default=None, help='run a small profiling workload (%s, dm40, gsc, next) instead'
                     % ', '.join(CASES))
     ap.add_argument('--batch', type=int, default=16)
     ap.add_argument('--reps', type=int, default=3)

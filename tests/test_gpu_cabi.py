@@ -102,6 +102,10 @@ def test_variants_agree(lib, n, res, cam):
             # binned path (no raw_data requested) agrees as well
             f1b, _ = measure(N, h, phase, n, cam, want_raw=False)
             assert O.rel_l2(f1b, f0b) < 2e-6, v
+            # no bounded wait of the variant's kernels timed out
+            code = np.ones(1, np.int32)
+            N.call('oopao_pwfs_device_status', h, code)
+            assert code[0] == 0, v
         assert N.load().oopao_pwfs_set_variant(h, nv + 1) == 2
     finally:
         N.load().oopao_pwfs_plan_destroy(h)
