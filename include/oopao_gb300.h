@@ -192,7 +192,9 @@ int oopao_dm_opd_f32(const float* modes_t, const float* coefs, int n_act, int n_
  * n_act_pad a multiple of 64), built once by oopao_dm_modes_bf16 from the
  * FP32 modes_t.  The coefficients enter as two BF16 terms (hi = bf16(c),
  * lo = bf16(c - hi)) summed in the FP32 accumulator, so only the IF matrix
- * is rounded to BF16.  workspace: device, 256-byte aligned,
+ * is rounded to BF16.  Batches of 1 to 4 (a closed-loop step) use a
+ * streaming GEMV over the BF16 rows with FP32 coefficients instead of the
+ * tensor cores.  workspace: device, 256-byte aligned,
  * oopao_dm_bf16_workspace_bytes(n_act_pad, batch) bytes; its first int
  * holds 0 after the call, or the code of a pipeline wait that timed out. */
 int oopao_dm_modes_bf16(const float* modes_t, int n_act, int n_pix, int n_act_pad, void* modes_out, void* stream);
@@ -241,14 +243,16 @@ int oopao_cl_pupil_rms(const float* opd, const int* idx, int npup, const int* st
  * A [n_outer][n_inner], B [n_outer][n_outer]: float64 extrusion matrices;
  *   inner_idx / outer_idx: map indices of the Z and X rings; normals:
  *   float64 [rows][n_outer] drawn by the host.
+ * mirror: device float32 [n_layers][n][n] scratch, the maps rounded to
+ *   float32 for the interpolation;
  * range: device float64 [n_layers][32][2] scratch (partial value ranges of
  *   each map); at most 64 layers;
  * scale: device float64 [n_layers] = lambda/2pi * sqrt(fractional r0);
  * opd: device float32 [res][res] output; step: device int32, the step whose
  *   entries are used, incremented at the end when `advance`; err: device
  *   int32 set to 1 when *step is outside [0, n_steps) (nothing moves then). */
-int oopao_atm_update(double* maps, int n_layers, int n, int slots, const void* sched, const double* buff,
-                     int n_steps, const double* A, const double* B, const int* inner_idx, const int* outer_idx,
+int oopao_atm_update(double* maps, float* mirror, int n_layers, int n, int slots, const void* sched,
+                     const double* buff, int n_steps, const double* A, const double* B, const int* inner_idx, const int* outer_idx,
                      int n_inner, int n_outer, const double* normals, double* range, const double* scale, int res,
                      float* opd, int* step, int advance, int* err, void* stream);
 

@@ -57,7 +57,7 @@ SIGNATURES = {
                                 c_int, c_void_p, c_void_p, c_void_p]),
     'oopao_cl_integrate': (c_int, [c_void_p, c_void_p, c_int, c_int, c_float, c_void_p, c_void_p, c_void_p]),
     'oopao_cl_pupil_rms': (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_int, c_void_p]),
-    'oopao_atm_update': (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p,
+    'oopao_atm_update': (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p,
                                  c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p,
                                  c_void_p, c_int, c_void_p, c_void_p]),
     'oopao_pwfs_ad_workspace_bytes': (c_size_t, [c_void_p, c_int]),

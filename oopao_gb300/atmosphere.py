@@ -9,9 +9,10 @@ Set-up follows the reference step by step:
   (:779-808) as the reference's ``initializeAtmosphere`` does;
 * the extrusion matrices from the von Karman covariance of the ring pixels
   (``makeCovarianceMatrix`` :72-132, ``get_covariance_matrices`` :707-777):
-  A = ZX^T pinv(ZZ), B = chol(XX - A ZX).  The covariances are evaluated on
-  the host in float64; the pseudo-inverse and the Cholesky factor are
-  computed in float64 on the GPU.
+  A = ZX^T pinv(ZZ), B = chol(XX - A ZX).  The covariances and the
+  pseudo-inverse are evaluated on the host in float64 (the reference's
+  calls); the products and the Cholesky factor are computed in float64 on
+  the GPU.
 
 Every ``update()`` (and every step of a captured closed loop) runs
 ``oopao_atm_update``: the one-pixel moves of each layer with their ring
@@ -176,11 +177,14 @@ class Atmosphere:
             u, v = np.meshgrid(x, x)
             zi = u[inner != 0] + 1j * v[inner != 0]
             zo = u[outer != 0] + 1j * v[outer != 0]
-            zz = torch.as_tensor(phase_covariance(zi, zi, self._L0), device=d)
+            zz = phase_covariance(zi, zi, self._L0)
             self._zx = torch.as_tensor(phase_covariance(zi, zo, self._L0), device=d)
             self._xx = torch.as_tensor(phase_covariance(zo, zo, self._L0), device=d)
-            # numpy's pinv cut-off (1e-15 of the largest singular value)
-            self._zz_inv = torch.linalg.pinv(zz, rtol=1e-15)
+            # the reference's own call (LAPACK gesdd on the host cores, cut-off
+            # 1e-15 of the largest singular value): for the ~2000 x 2000 ring
+            # covariance it takes ~1.5 s there against ~4 s for the GPU's
+            # float64 Jacobi SVD
+            self._zz_inv = torch.as_tensor(np.linalg.pinv(zz), device=d)
             self._set_matrices()
         self._idx_dev = (torch.as_tensor(self._inner_idx, device=d), torch.as_tensor(self._outer_idx, device=d))
         self._scale_dev = self._scale()
@@ -188,6 +192,7 @@ class Atmosphere:
         self._step_dev = torch.zeros(1, dtype=torch.int32, device=d)
         self._err = torch.zeros(1, dtype=torch.int32, device=d)
         self._range = torch.zeros((self.nLayer, 32, 2), dtype=torch.float64, device=d)
+        self._mirror = torch.zeros((self.nLayer, n, n), dtype=torch.float32, device=d)
         self._opd_dev = torch.zeros((res, res), dtype=torch.float32, device=d)
         self.hasNotBeenInitialized = False
         self.generateNewPhaseScreen(0)
@@ -345,15 +350,16 @@ class Atmosphere:
         st = N.stream_handle(stream)
         res = self.telescope.resolution
         if not moved:
-            N.call('oopao_atm_update', self._maps, self.nLayer, self._n, 0, None, None, 0, None, None, None, None,
-                   0, 0, None, self._range, self._scale_dev, res, self._opd_dev, self._step_dev, 0, self._err, st)
+            N.call('oopao_atm_update', self._maps, self._mirror, self.nLayer, self._n, 0, None, None, 0, None, None,
+                   None, None, 0, 0, None, self._range, self._scale_dev, res, self._opd_dev, self._step_dev, 0,
+                   self._err, st)
             return
         slots = self._slots if self._slots else 0
         if slots:
             slots = max(slots, 2)
         inner, outer = self._idx_dev
-        N.call('oopao_atm_update', self._maps, self.nLayer, self._n, slots, self._sched_dev, self._buff_dev,
-               self._dev_plan_len, self._A if slots else None, self._B if slots else None, inner, outer,
+        N.call('oopao_atm_update', self._maps, self._mirror, self.nLayer, self._n, slots, self._sched_dev,
+               self._buff_dev, self._dev_plan_len, self._A if slots else None, self._B if slots else None, inner, outer,
                len(self._inner_idx), len(self._outer_idx), self._normals_dev, self._range, self._scale_dev, res,
                self._opd_dev, self._step_dev, 1 if advance else 0, self._err, st)
 

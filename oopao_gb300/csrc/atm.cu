@@ -88,22 +88,30 @@ __global__ void atm_extrude(double* __restrict__ map, const double* __restrict__
 
 constexpr int kRangeBlocks = 32;  // partial value ranges per layer
 
-// partial value range of each map: block b of layer l covers a contiguous
-// chunk; range[l][b] = (min, max)
-__global__ void atm_minmax(const double* __restrict__ map, double* __restrict__ range, int n) {
-  __shared__ double lo_s[32], hi_s[32];
+// Float32 mirror of each map (what the OPD interpolation reads; the maps
+// themselves stay float64 for the extrusion) and its partial value ranges:
+// block b of layer l covers a contiguous chunk; range[l][b] = (min, max) of
+// the float32 values, which is the float32 rounding of the float64 range.
+// One float64 -> float32 conversion per pixel here replaces sixteen per
+// output pixel and layer in the interpolation.
+__global__ void atm_minmax(const double* __restrict__ map, float* __restrict__ mirror, double* __restrict__ range,
+                           int n) {
+  __shared__ float lo_s[32], hi_s[32];
   const int l = blockIdx.y, b = blockIdx.x;
   const double* m = map + (size_t)l * n * n;
+  float* mf = mirror + (size_t)l * n * n;
   const int nn = n * n, chunk = (nn + gridDim.x - 1) / gridDim.x;
   const int i0 = b * chunk, i1 = min(nn, i0 + chunk);
-  double lo = DBL_MAX, hi = -DBL_MAX;
+  float lo = FLT_MAX, hi = -FLT_MAX;
   for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-    lo = fmin(lo, m[i]);
-    hi = fmax(hi, m[i]);
+    const float v = (float)m[i];
+    mf[i] = v;
+    lo = fminf(lo, v);
+    hi = fmaxf(hi, v);
   }
   for (int s = 16; s > 0; s >>= 1) {
-    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, s));
-    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, s));
+    lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, s));
+    hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, s));
   }
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (lane == 0) {
@@ -113,11 +121,11 @@ __global__ void atm_minmax(const double* __restrict__ map, double* __restrict__ 
   __syncthreads();
   if (wid == 0) {
     const int nw = blockDim.x >> 5;
-    lo = lane < nw ? lo_s[lane] : DBL_MAX;
-    hi = lane < nw ? hi_s[lane] : -DBL_MAX;
+    lo = lane < nw ? lo_s[lane] : FLT_MAX;
+    hi = lane < nw ? hi_s[lane] : -FLT_MAX;
     for (int s = 16; s > 0; s >>= 1) {
-      lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, s));
-      hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, s));
+      lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, s));
+      hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, s));
     }
     if (lane == 0) {
       range[((size_t)l * gridDim.x + b) * 2] = lo;
@@ -136,8 +144,8 @@ __device__ __forceinline__ void keys_weights(float x, float* w) {
   w[3] = 0.5f * (-x2 + x3);
 }
 
-__device__ __forceinline__ float map_at(const double* m, int n, int r, int c) {
-  return (r >= 0 && r < n && c >= 0 && c < n) ? (float)m[(size_t)r * n + c] : 0.f;
+__device__ __forceinline__ float map_at(const float* m, int n, int r, int c) {
+  return (r >= 0 && r < n && c >= 0 && c < n) ? m[(size_t)r * n + c] : 0.f;
 }
 
 constexpr int kMaxAtmLayers = 64;
@@ -146,7 +154,7 @@ constexpr int kMaxAtmLayers = 64;
 // per-layer integer base, separable weights and value range are set up once
 // per block in shared memory; each pixel is then 16 loads and FP32 FMAs per
 // layer (the interpolated values are rounded to float32 like the output).
-__global__ void atm_opd(const double* __restrict__ map, const double* __restrict__ range,
+__global__ void atm_opd(const float* __restrict__ mirror, const double* __restrict__ range,
                         const double2* __restrict__ buff, const int* step, int n_steps, int use_buff,
                         const double* __restrict__ scale, int n_layers, int n, int res, int off, float* __restrict__ opd,
                         int* err) {
@@ -171,13 +179,13 @@ __global__ void atm_opd(const double* __restrict__ map, const double* __restrict
     dc_s[l] = (int)fc;
     keys_weights((float)(-ty - fr), wr_s[l]);
     keys_weights((float)(-tx - fc), wc_s[l]);
-    double lo = DBL_MAX, hi = -DBL_MAX;
+    float lo = FLT_MAX, hi = -FLT_MAX;
     for (int b = 0; b < kRangeBlocks; b++) {
-      lo = fmin(lo, range[((size_t)l * kRangeBlocks + b) * 2]);
-      hi = fmax(hi, range[((size_t)l * kRangeBlocks + b) * 2 + 1]);
+      lo = fminf(lo, (float)range[((size_t)l * kRangeBlocks + b) * 2]);
+      hi = fmaxf(hi, (float)range[((size_t)l * kRangeBlocks + b) * 2 + 1]);
     }
-    lo_s[l] = (float)lo;
-    hi_s[l] = (float)hi;
+    lo_s[l] = lo;
+    hi_s[l] = hi;
     sc_s[l] = (float)scale[l];
   }
   __syncthreads();
@@ -186,7 +194,7 @@ __global__ void atm_opd(const double* __restrict__ map, const double* __restrict
   const int y = p / res, x = p % res;
   float acc = 0.f;
   for (int l = 0; l < n_layers; l++) {
-    const double* m = map + (size_t)l * n * n;
+    const float* m = mirror + (size_t)l * n * n;
     // the OPD crop starts `off` pixels into the map
     const int r0 = y + off + dr_s[l], c0 = x + off + dc_s[l];
     float v = 0.f;
@@ -209,12 +217,12 @@ __global__ void atm_advance(int* step) {
 
 }  // namespace
 
-extern "C" int oopao_atm_update(double* maps, int n_layers, int n, int slots, const void* sched, const double* buff,
-                                int n_steps, const double* A, const double* B, const int* inner_idx,
+extern "C" int oopao_atm_update(double* maps, float* mirror, int n_layers, int n, int slots, const void* sched,
+                                const double* buff, int n_steps, const double* A, const double* B, const int* inner_idx,
                                 const int* outer_idx, int n_inner, int n_outer, const double* normals,
                                 double* range, const double* scale, int res, float* opd, int* step, int advance,
                                 int* err, void* stream) {
-  OOPAO_CHECK_ARG(maps && scale && opd && step && range, "NULL argument");
+  OOPAO_CHECK_ARG(maps && mirror && scale && opd && step && range, "NULL argument");
   OOPAO_CHECK_ARG(n_layers > 0 && n_layers <= kMaxAtmLayers && n >= 8 && res > 0 && res <= n - 6 && slots >= 0 &&
                       slots % 2 == 0,
                   "bad sizes (1 to 64 layers, n >= res + 6, an even number of slots)");
@@ -234,9 +242,9 @@ extern "C" int oopao_atm_update(double* maps, int n_layers, int n, int slots, co
                                                           err);
     launches += 2;
   }
-  atm_minmax<<<dim3(kRangeBlocks, n_layers), 256, 0, st>>>(maps, range, n);
+  atm_minmax<<<dim3(kRangeBlocks, n_layers), 256, 0, st>>>(maps, mirror, range, n);
   const int off = (n - res) / 2;  // crop of the warped map: [1:-1] then the pupil footprint
-  atm_opd<<<ceil_div(res * res, 256), 256, 0, st>>>(maps, range, reinterpret_cast<const double2*>(buff), step,
+  atm_opd<<<ceil_div(res * res, 256), 256, 0, st>>>(mirror, range, reinterpret_cast<const double2*>(buff), step,
                                                    n_steps, buff != nullptr ? 1 : 0, scale, n_layers, n, res, off,
                                                    opd, err);
   launches += 2;

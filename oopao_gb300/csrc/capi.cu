@@ -23,6 +23,6 @@ void oopao_count_launches(int n) { g_launches.fetch_add((unsigned long long)n, s
 
 extern "C" unsigned long long oopao_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
-extern "C" int oopao_abi_version(void) { return 1; }
+extern "C" int oopao_abi_version(void) { return 2; }
 
 extern "C" const char* oopao_last_error(void) { return g_last_error; }

@@ -52,50 +52,106 @@ __global__ void cl_screen(ScreenArgs a) {
   a.opd[p] = s;
 }
 
-// coefs[a] -= gain * sum_j R[a][j] s[j]  (one warp per actuator); block 0
-// thread 0 advances the step counter.
-__global__ void cl_integrate(const float* __restrict__ R, const float* __restrict__ s, int n_act, int n_sig,
-                             float gain, float* __restrict__ coefs, int* step) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (warp < n_act) {
-    const float* r = R + (size_t)warp * n_sig;
-    float acc = 0.f;
-    for (int j = lane; j < n_sig; j += 32) acc = fmaf(r[j], s[j], acc);
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) coefs[warp] -= gain * acc;
+// coefs[a] -= gain * sum_j R[a][j] s[j].  Four warps per actuator, each over
+// an interleaved quarter of the signals with eight loads per lane in flight
+// (enough bytes in flight to stream R at HBM rate); block 0 thread 0
+// advances the step counter.
+constexpr int kIntActPerBlock = 2;  // 256 threads = 2 actuators x 4 warps
+
+__global__ void __launch_bounds__(256) cl_integrate(const float* __restrict__ R, const float* __restrict__ s,
+                                                    int n_act, int n_sig, float gain, float* __restrict__ coefs,
+                                                    int* step) {
+  __shared__ float red[8];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int act = blockIdx.x * kIntActPerBlock + (w >> 2), part = w & 3;
+  float acc = 0.f;
+  if (act < n_act) {
+    const float* r = R + (size_t)act * n_sig;
+    int j = part * 32 + lane;
+    for (; j + 7 * 128 < n_sig; j += 8 * 128) {
+      float rv[8], sv[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        rv[u] = r[j + u * 128];
+        sv[u] = s[j + u * 128];
+      }
+#pragma unroll
+      for (int u = 0; u < 8; u++) acc = fmaf(rv[u], sv[u], acc);
+    }
+    for (; j < n_sig; j += 128) acc = fmaf(r[j], s[j], acc);
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) red[w] = acc;
+  __syncthreads();
+  if (threadIdx.x < kIntActPerBlock) {
+    const int a = blockIdx.x * kIntActPerBlock + threadIdx.x;
+    if (a < n_act) {
+      const float* q = red + 4 * threadIdx.x;
+      coefs[a] -= gain * ((q[0] + q[1]) + (q[2] + q[3]));
+    }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0 && step) *step += 1;
 }
 
-// RMS of (opd - mean) over the pupil pixels idx[0..npup) -> out[*step].
-__global__ void cl_pupil_rms(const float* __restrict__ opd, const int* __restrict__ idx, int npup,
-                             const int* step, float* out, int out_len) {
-  __shared__ double red[2][32];
-  double s = 0.0, s2 = 0.0;
-  for (int i = threadIdx.x; i < npup; i += blockDim.x) {
-    const double v = opd[idx[i]];
-    s += v;
-    s2 += v * v;
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    s += __shfl_xor_sync(0xffffffffu, s, o);
-    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-  }
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
+  const float y = x - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
+// Sum over the CTA (blockDim.x = 1024) of one float per thread.
+__device__ float cta_sum_1024(float v, float* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) {
-    red[0][w] = s;
-    red[1][w] = s2;
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    float t = red[l];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (l == 0) red[32] = t;
   }
   __syncthreads();
+  const float r = red[32];
+  __syncthreads();
+  return r;
+}
+
+// RMS of (opd - mean) over the pupil pixels idx[0..npup) -> out[*step].
+// Two passes (mean, then the squared deviations) with compensated float32
+// sums; float64 is a narrow pipe on this part, and the two-pass form keeps
+// the variance free of the cancellation of sum(v^2)/n - mean^2.
+__global__ void __launch_bounds__(1024) cl_pupil_rms(const float* __restrict__ opd, const int* __restrict__ idx,
+                                                     int npup, const int* step, float* out, int out_len) {
+  __shared__ float red[33];
+  float s = 0.f, c = 0.f;
+  int i = threadIdx.x;
+  for (; i + 3 * 1024 < npup; i += 4 * 1024) {
+    float v[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) v[u] = opd[idx[i + u * 1024]];
+#pragma unroll
+    for (int u = 0; u < 4; u++) kahan_add(s, c, v[u]);
+  }
+  for (; i < npup; i += 1024) kahan_add(s, c, opd[idx[i]]);
+  const float mean = cta_sum_1024(s, red) / (float)npup;
+  float q = 0.f, cq = 0.f;
+  i = threadIdx.x;
+  for (; i + 3 * 1024 < npup; i += 4 * 1024) {
+    float v[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) v[u] = opd[idx[i + u * 1024]] - mean;
+#pragma unroll
+    for (int u = 0; u < 4; u++) kahan_add(q, cq, v[u] * v[u]);
+  }
+  for (; i < npup; i += 1024) {
+    const float d = opd[idx[i]] - mean;
+    kahan_add(q, cq, d * d);
+  }
+  const float var = cta_sum_1024(q, red) / (float)npup;
   if (threadIdx.x == 0) {
-    double a = 0.0, b = 0.0;
-    for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
-      a += red[0][i];
-      b += red[1][i];
-    }
-    const double m = a / npup;
     const int t = step ? *step : 0;
-    if (t >= 0 && t < out_len) out[t] = (float)sqrt(fmax(b / npup - m * m, 0.0));
+    if (t >= 0 && t < out_len) out[t] = sqrtf(var);
   }
 }
 
@@ -125,7 +181,8 @@ extern "C" int oopao_cl_integrate(const float* R, const float* s, int n_act, int
                                   int* step, void* stream) {
   OOPAO_CHECK_ARG(R && s && coefs, "NULL argument");
   OOPAO_CHECK_ARG(n_act > 0 && n_sig > 0, "sizes must be positive");
-  cl_integrate<<<ceil_div(n_act * 32, 256), 256, 0, (cudaStream_t)stream>>>(R, s, n_act, n_sig, gain, coefs, step);
+  cl_integrate<<<ceil_div(n_act, kIntActPerBlock), 256, 0, (cudaStream_t)stream>>>(R, s, n_act, n_sig, gain, coefs,
+                                                                                  step);
   oopao_count_launches(1);
   OOPAO_CUDA_TRY(cudaGetLastError());
   return OOPAO_OK;

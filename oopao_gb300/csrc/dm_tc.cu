@@ -210,6 +210,91 @@ __global__ void dm_coefs_to_bf16(const float* __restrict__ coefs, int n_act, int
   out[plane + i] = __float2bfloat16_rn(c - __bfloat162float(hi));
 }
 
+// Small batches (a closed-loop step): the tensor-core tile would be mostly
+// padding, so the projection is a streaming GEMV over the BF16 IF rows with
+// the FP32 coefficients held in shared memory.  One warp per pixel row at a
+// time (8 rows per warp, two in flight); each lane loads 16 bytes (8 BF16) per
+// step.  Bound by the HBM read of the IF matrix.
+constexpr int kGemvMaxBatch = 4;
+constexpr int kGemvRowsPerWarp = 8;
+
+template <int B>
+__global__ void __launch_bounds__(256) dm_gemv_bf16(const __nv_bfloat16* __restrict__ modes, int n_act_pad,
+                                                    const float* __restrict__ coefs, int n_act, int n_pix,
+                                                    float scale, const float* __restrict__ base,
+                                                    float* __restrict__ opd) {
+  extern __shared__ float cs[];  // [B][n_act_pad], zero padded
+  for (int i = threadIdx.x; i < B * n_act_pad; i += blockDim.x) {
+    const int b = i / n_act_pad, a = i - (i / n_act_pad) * n_act_pad;
+    cs[i] = a < n_act ? coefs[(size_t)a * B + b] : 0.f;
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row0 = (blockIdx.x * (blockDim.x >> 5) + warp) * kGemvRowsPerWarp;
+  const int steps = n_act_pad / 256;  // n_act_pad is a multiple of 64; the tail is handled below
+  for (int rr = 0; rr < kGemvRowsPerWarp; rr += 2) {
+    const int p0 = row0 + rr, p1 = row0 + rr + 1;
+    if (p0 >= n_pix) break;
+    const bool has1 = p1 < n_pix;
+    const uint4* m0 = reinterpret_cast<const uint4*>(modes + (size_t)p0 * n_act_pad);
+    const uint4* m1 = reinterpret_cast<const uint4*>(modes + (size_t)(has1 ? p1 : p0) * n_act_pad);
+    float acc0[B], acc1[B];
+#pragma unroll
+    for (int b = 0; b < B; b++) acc0[b] = acc1[b] = 0.f;
+    auto accumulate = [&](uint4 w0, uint4 w1, int a0) {
+      const __nv_bfloat162* h0 = reinterpret_cast<const __nv_bfloat162*>(&w0);
+      const __nv_bfloat162* h1 = reinterpret_cast<const __nv_bfloat162*>(&w1);
+#pragma unroll
+      for (int e = 0; e < 4; e++) {
+        const float2 f0 = __bfloat1622float2(h0[e]);
+        const float2 f1 = __bfloat1622float2(h1[e]);
+#pragma unroll
+        for (int b = 0; b < B; b++) {
+          const float c0 = cs[b * n_act_pad + a0 + 2 * e], c1 = cs[b * n_act_pad + a0 + 2 * e + 1];
+          acc0[b] = fmaf(f0.x, c0, fmaf(f0.y, c1, acc0[b]));
+          acc1[b] = fmaf(f1.x, c0, fmaf(f1.y, c1, acc1[b]));
+        }
+      }
+    };
+    for (int st = 0; st < steps; st++) {
+      const int q = st * 32 + lane;  // 16-byte chunk index
+      accumulate(m0[q], m1[q], q * 8);
+    }
+    {
+      const int q = steps * 32 + lane;
+      if (q * 8 < n_act_pad) accumulate(m0[q], m1[q], q * 8);
+    }
+#pragma unroll
+    for (int b = 0; b < B; b++) {
+      float v0 = acc0[b], v1 = acc1[b];
+      for (int o = 16; o > 0; o >>= 1) {
+        v0 += __shfl_xor_sync(0xffffffffu, v0, o);
+        v1 += __shfl_xor_sync(0xffffffffu, v1, o);
+      }
+      if (lane == 0) {
+        const size_t o0 = (size_t)b * n_pix + p0;
+        opd[o0] = scale * v0 + (base ? base[o0] : 0.f);
+        if (has1) {
+          const size_t o1 = (size_t)b * n_pix + p1;
+          opd[o1] = scale * v1 + (base ? base[o1] : 0.f);
+        }
+      }
+    }
+  }
+}
+
+template <int B>
+cudaError_t launch_gemv(const void* modes, int n_act_pad, const float* coefs, int n_act, int n_pix, float scale,
+                        const float* base, float* opd, cudaStream_t st) {
+  const size_t smem = sizeof(float) * B * (size_t)n_act_pad;
+  cudaError_t e = cudaFuncSetAttribute(dm_gemv_bf16<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int rows_per_cta = 8 * kGemvRowsPerWarp;
+  dm_gemv_bf16<B><<<ceil_div(n_pix, rows_per_cta), 256, smem, st>>>(
+      reinterpret_cast<const __nv_bfloat16*>(modes), n_act_pad, coefs, n_act, n_pix, scale, base, opd);
+  return cudaGetLastError();
+}
+
 // modes_t [n_act][n_pix] f32 -> modes [n_pix][n_act_pad] bf16, zero padded
 __global__ void dm_modes_to_bf16(const float* __restrict__ modes_t, int n_act, int n_pix, int n_act_pad,
                                  __nv_bfloat16* __restrict__ out) {
@@ -289,6 +374,23 @@ extern "C" int oopao_dm_opd_bf16(const void* modes, int n_act_pad, const float* 
   OOPAO_CHECK_ARG(workspace_bytes >= oopao_dm_bf16_workspace_bytes(n_act_pad, batch), "workspace too small");
   OOPAO_CHECK_ARG(ceil_div(n_pix, kBM) <= 65535, "n_pix above 65535 * 128");
   cudaStream_t st = (cudaStream_t)stream;
+  if (batch <= kGemvMaxBatch) {
+    OOPAO_CHECK_ARG((size_t)batch * n_act_pad * sizeof(float) <= 200 * 1024, "n_act_pad too large for the GEMV form");
+    OOPAO_CUDA_TRY(cudaMemsetAsync(workspace, 0, sizeof(int), st));
+    cudaError_t e = cudaSuccess;
+    switch (batch) {
+      case 1: e = launch_gemv<1>(modes, n_act_pad, coefs, n_act, n_pix, scale, base, opd, st); break;
+      case 2: e = launch_gemv<2>(modes, n_act_pad, coefs, n_act, n_pix, scale, base, opd, st); break;
+      case 3: e = launch_gemv<3>(modes, n_act_pad, coefs, n_act, n_pix, scale, base, opd, st); break;
+      default: e = launch_gemv<4>(modes, n_act_pad, coefs, n_act, n_pix, scale, base, opd, st); break;
+    }
+    if (e != cudaSuccess) {
+      oopao_set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+      return OOPAO_ERR_CUDA;
+    }
+    oopao_count_launches(1);
+    return OOPAO_OK;
+  }
   const int bn = batch <= 64 ? 64 : 128;
   const int batch_pad = ceil_div(batch, bn) * bn;
   int* err = reinterpret_cast<int*>(workspace);

@@ -1176,7 +1176,7 @@ extern "C" int oopao_pwfs_signal(const oopao_pwfs_plan* p, const float* frame, i
   a.n_valid = p->cam2;
   for (int q = 0; q < 4; q++) { a.q_r0[q] = p->q_r0[q]; a.q_c0[q] = p->q_c0[q]; }
   a.units = p->slopes_units; a.norma_const = p->norma_const;
-  pwfs_signal<<<batch, 256, 0, (cudaStream_t)stream>>>(a);
+  pwfs_signal<<<batch, 512, 0, (cudaStream_t)stream>>>(a);
   oopao_count_launches(1);
   OOPAO_CUDA_TRY(cudaGetLastError());
   return OOPAO_OK;
