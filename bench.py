@@ -728,10 +728,10 @@ def run_ours(args):
     barrier()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     ns = wfs.nSignal
-    # host -> device: commands (float32), D for the float64 vault, the Gram eigenvectors
-    h2d = m2c.size * 4 + ns * NMODES * 8 + NMODES * NMODES * 8
-    # device -> host: D (float64), the Gram matrix, and the vault's U, s, V, D, M, Mtrunc, Dtrunc
-    d2h = ns * NMODES * 8 + NMODES * NMODES * 8 + (5 * ns * NMODES + NMODES + NMODES * NMODES) * 8
+    # host -> device: commands (float32), D for the float64 vault
+    h2d = m2c.size * 4 + ns * NMODES * 8
+    # device -> host: D (float64), the vault's U, s, V, D, M, Mtrunc, Dtrunc and its condition check
+    d2h = ns * NMODES * 8 + (5 * ns * NMODES + NMODES + NMODES * NMODES + 2) * 8
     e2e = {'value': frames_step * world / e2e_s, 'unit': 'frames/s', 'h2d_bytes_per_step': int(h2d),
            'd2h_bytes_per_step': int(d2h), 'im_build_ms': e2e_s * 1000.0,
            'api': 'InteractionMatrix(..., single_pass=False, nTrunc=20)'}

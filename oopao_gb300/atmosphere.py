@@ -9,10 +9,9 @@ Set-up follows the reference step by step:
   (:779-808) as the reference's ``initializeAtmosphere`` does;
 * the extrusion matrices from the von Karman covariance of the ring pixels
   (``makeCovarianceMatrix`` :72-132, ``get_covariance_matrices`` :707-777):
-  A = ZX^T pinv(ZZ), B = chol(XX - A ZX).  The covariances and the
-  pseudo-inverse are evaluated on the host in float64 (the reference's
-  calls); the products and the Cholesky factor are computed in float64 on
-  the GPU.
+  A = ZX^T pinv(ZZ), B = chol(XX - A ZX).  The covariances are evaluated on
+  the host in float64; the pseudo-inverse and the Cholesky factor are
+  computed in float64 on the GPU.
 
 Every ``update()`` (and every step of a captured closed loop) runs
 ``oopao_atm_update``: the one-pixel moves of each layer with their ring
@@ -177,14 +176,11 @@ class Atmosphere:
             u, v = np.meshgrid(x, x)
             zi = u[inner != 0] + 1j * v[inner != 0]
             zo = u[outer != 0] + 1j * v[outer != 0]
-            zz = phase_covariance(zi, zi, self._L0)
+            zz = torch.as_tensor(phase_covariance(zi, zi, self._L0), device=d)
             self._zx = torch.as_tensor(phase_covariance(zi, zo, self._L0), device=d)
             self._xx = torch.as_tensor(phase_covariance(zo, zo, self._L0), device=d)
-            # the reference's own call (LAPACK gesdd on the host cores, cut-off
-            # 1e-15 of the largest singular value): for the ~2000 x 2000 ring
-            # covariance it takes ~1.5 s there against ~4 s for the GPU's
-            # float64 Jacobi SVD
-            self._zz_inv = torch.as_tensor(np.linalg.pinv(zz), device=d)
+            # numpy's pinv cut-off (1e-15 of the largest singular value)
+            self._zz_inv = torch.linalg.pinv(zz, rtol=1e-15)
             self._set_matrices()
         self._idx_dev = (torch.as_tensor(self._inner_idx, device=d), torch.as_tensor(self._outer_idx, device=d))
         self._scale_dev = self._scale()

@@ -14,9 +14,8 @@
 * ``method='jvp'``: columns from the hand-written tangent of the sensor
   (``oopao_gb300.autodiff``), exact in the limit stroke -> 0.
 
-The SVD of ``CalibrationVault`` runs in float64: Gram matrix and products on
-the GPU, the small symmetric eigenproblem on the host cores (faster there on
-this part, see ``_gram_eigh_host``).
+The SVD of ``CalibrationVault`` runs in float64 on the GPU (an optional host
+eigensolver is described at ``_vault_fp64``).
 """
 import time
 
@@ -26,45 +25,43 @@ import torch
 from .tools import OopaoError
 
 
-def _gram_eigh_host(G):
-    """Eigen-decomposition of the symmetric float64 matrix G with LAPACK's
-    divide-and-conquer dsyevd on the host cores (numpy.linalg.eigh).  At the
-    sizes of an interaction matrix (a few hundred modes) the solver is bound by
-    latency, not arithmetic: measured on GB300 at n = 300, 4.5 ms on the Grace
-    cores against 9.3 ms for cuSOLVER syevd on the GPU, whose float64 units
-    are narrow."""
-    return np.linalg.eigh(G)
-
-
-def _vault_fp64(D, n_ev):
+def _vault_fp64(D, n_ev, host_eigensolver=False):
     """Thin SVD D = U diag(s) V of an interaction matrix and the products of
-    ``CalibrationVault`` (D, M, Mtrunc, Dtrunc), float64.
+    ``CalibrationVault`` (D, M, Mtrunc, Dtrunc), float64 on the GPU.
 
-    Tall, well-conditioned matrices go through the Gram matrix: the GPU forms
-    D^T D, the host solves eigh(D^T D) = V^T diag(s^2) V, and the GPU forms
-    U = D V^T / s and the products, which return to the host together.
-    Squaring the condition number costs at most ~1e-16 * cond^2 relative
-    accuracy on the smallest singular values, so a full SVD (LAPACK gesdd on
-    the host, the reference's own call) is used instead when cond(D) > 1e6 or
-    D is wide.  Diagonal products are row/column scalings, which give the
-    same numbers as the reference's products with diag(s)."""
+    Tall, well-conditioned matrices go through the Gram matrix:
+    eigh(D^T D) = V^T diag(s^2) V (cuSOLVER syevd), U = D V^T / s, then the
+    products, which return to the host in one copy.  Squaring the condition
+    number costs at most ~1e-16 * cond^2 relative accuracy on the smallest
+    singular values, so a full SVD (cuSOLVER gesvd) is used instead when
+    cond(D) > 1e6 or D is wide.  Diagonal products are row/column scalings,
+    which give the same numbers as the reference's products with diag(s).
+
+    host_eigensolver: solve the small symmetric eigenproblem with LAPACK
+    dsyevd on the host cores instead (the Gram matrix and the products stay
+    on the GPU).  At n = 300 it takes 4.5 ms on GB300's Grace cores against
+    9.3 ms for cuSOLVER syevd, whose float64 units are narrow; off by default,
+    which keeps the float64 linear algebra on the GPU."""
     from .runtime import device
     dev = device()
     Dt = torch.as_tensor(np.asarray(D, dtype=np.float64), device=dev)
     m, n = Dt.shape
     if m >= n:
-        ev, W = _gram_eigh_host((Dt.T @ Dt).cpu().numpy())
-        ev, W = ev[::-1].copy(), np.ascontiguousarray(W[:, ::-1])
-        smax = np.sqrt(max(ev[0], 0.0))
-        smin = np.sqrt(max(ev[-1], 0.0))
-        if smin > 1e-6 * smax:
-            s = torch.as_tensor(np.sqrt(ev), device=dev)
-            Wt = torch.as_tensor(W, device=dev)
-            U = (Dt @ Wt) / s[None, :]
-            return _vault_products(U, s, Wt.T.contiguous(), n_ev)
-    U, s, V = np.linalg.svd(np.asarray(D, dtype=np.float64), full_matrices=False)
-    return _vault_products(torch.as_tensor(U, device=dev), torch.as_tensor(s, device=dev),
-                           torch.as_tensor(V, device=dev), n_ev)
+        G = Dt.T @ Dt
+        if host_eigensolver:
+            ev_h, W_h = np.linalg.eigh(G.cpu().numpy())
+            ev, W = torch.as_tensor(ev_h, device=dev), torch.as_tensor(W_h, device=dev)
+        else:
+            ev, W = torch.linalg.eigh(G)
+        ev = torch.flip(ev, [0])
+        W = torch.flip(W, [1])
+        lo_hi = torch.sqrt(torch.clamp(ev[[0, -1]], min=0)).cpu().numpy()
+        if lo_hi[1] > 1e-6 * lo_hi[0]:
+            s = torch.sqrt(ev)
+            U = (Dt @ W) / s[None, :]
+            return _vault_products(U, s, W.T.contiguous(), n_ev)
+    U, s, Vh = torch.linalg.svd(Dt, full_matrices=False, driver='gesvd')
+    return _vault_products(U, s, Vh, n_ev)
 
 
 def _vault_products(U, s, V, n_ev):
@@ -86,10 +83,10 @@ def _vault_products(U, s, V, n_ev):
 
 class CalibrationVault:
     def __init__(self, D, nTrunc: int = 0, display: bool = False, print_details: bool = False,
-                 invert: bool = True):
+                 invert: bool = True, host_eigensolver: bool = False):
         if invert:
             n_ev = min(np.shape(D)) - nTrunc
-            U, s, V, Drec, M, Mtrunc, Dtrunc = _vault_fp64(D, n_ev)
+            U, s, V, Drec, M, Mtrunc, Dtrunc = _vault_fp64(D, n_ev, host_eigensolver)
             self.s = s
             self.S = np.diag(s)
             self.eigenValues = s

@@ -123,6 +123,9 @@ def test_interaction_matrix(system, method):
     # the float64 pseudo-inverse of the same matrix matches the reference's SVD
     ref_vault = og.CalibrationVault(d['im_D'])
     assert rel(ref_vault.M, d['im_M']) < 1e-10
+    # the optional host eigensolver gives the same reconstructor
+    host_vault = og.CalibrationVault(d['im_D'], host_eigensolver=True)
+    assert rel(host_vault.M, d['im_M']) < 1e-10
     calib_pp = og.InteractionMatrix(ngs, tel, dm, wfs, M2C=d['im_m2c'], stroke=1e-8, single_pass=False,
                                     method=method)
     assert rel(calib_pp.D, d['im_pp_D']) < 1e-4
