@@ -5,6 +5,8 @@
 // A device step counter drives the time index, so a CUDA graph capturing one
 // step replays every later step without host involvement: the screen kernel
 // reads the counter, the integrator kernel advances it.
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 
 namespace {
@@ -118,41 +120,62 @@ __device__ float cta_sum_1024(float v, float* red) {
 }
 
 // RMS of (opd - mean) over the pupil pixels idx[0..npup) -> out[*step].
-// Two passes (mean, then the squared deviations) with compensated float32
-// sums; float64 is a narrow pipe on this part, and the two-pass form keeps
-// the variance free of the cancellation of sum(v^2)/n - mean^2.
-__global__ void __launch_bounds__(1024) cl_pupil_rms(const float* __restrict__ opd, const int* __restrict__ idx,
-                                                     int npup, const int* step, float* out, int out_len) {
+// A cluster of kRmsCtas CTAs splits the pixels into contiguous chunks; each
+// CTA takes its chunk's mean and sum of squared deviations in two passes with
+// compensated float32 sums (float64 is a narrow pipe on this part, and the
+// two-pass form avoids the cancellation of sum(v^2)/n - mean^2).  CTA 0 then
+// reads the chunk results through distributed shared memory and merges them
+// in rank order (Chan et al.: M2 = sum M2_c + sum n_c (mean_c - mean)^2).
+constexpr int kRmsCtas = 8;
+
+__global__ void __cluster_dims__(kRmsCtas, 1, 1) __launch_bounds__(1024)
+    cl_pupil_rms(const float* __restrict__ opd, const int* __restrict__ idx, int npup, const int* step, float* out,
+                 int out_len) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
   __shared__ float red[33];
+  __shared__ float part[3];  // n, mean, M2 of this CTA's chunk
+  const int rank = (int)cluster.block_rank();
+  const int chunk = (npup + kRmsCtas - 1) / kRmsCtas;
+  const int i0 = rank * chunk, i1 = min(npup, i0 + chunk);
+  const int cnt = max(0, i1 - i0);
   float s = 0.f, c = 0.f;
-  int i = threadIdx.x;
-  for (; i + 3 * 1024 < npup; i += 4 * 1024) {
-    float v[4];
-#pragma unroll
-    for (int u = 0; u < 4; u++) v[u] = opd[idx[i + u * 1024]];
-#pragma unroll
-    for (int u = 0; u < 4; u++) kahan_add(s, c, v[u]);
-  }
-  for (; i < npup; i += 1024) kahan_add(s, c, opd[idx[i]]);
-  const float mean = cta_sum_1024(s, red) / (float)npup;
+  for (int i = i0 + threadIdx.x; i < i1; i += 1024) kahan_add(s, c, opd[idx[i]]);
+  const float chunk_sum = cta_sum_1024(s, red);
+  const float mean = cnt > 0 ? chunk_sum / (float)cnt : 0.f;
   float q = 0.f, cq = 0.f;
-  i = threadIdx.x;
-  for (; i + 3 * 1024 < npup; i += 4 * 1024) {
-    float v[4];
-#pragma unroll
-    for (int u = 0; u < 4; u++) v[u] = opd[idx[i + u * 1024]] - mean;
-#pragma unroll
-    for (int u = 0; u < 4; u++) kahan_add(q, cq, v[u] * v[u]);
-  }
-  for (; i < npup; i += 1024) {
+  for (int i = i0 + threadIdx.x; i < i1; i += 1024) {
     const float d = opd[idx[i]] - mean;
     kahan_add(q, cq, d * d);
   }
-  const float var = cta_sum_1024(q, red) / (float)npup;
+  const float m2 = cta_sum_1024(q, red);
   if (threadIdx.x == 0) {
-    const int t = step ? *step : 0;
-    if (t >= 0 && t < out_len) out[t] = sqrtf(var);
+    part[0] = (float)cnt;
+    part[1] = mean;
+    part[2] = m2;
   }
+  cluster.sync();
+  if (rank == 0 && threadIdx.x == 0) {
+    float n_r[kRmsCtas], mean_r[kRmsCtas], m2_r[kRmsCtas];
+    float tot = 0.f, sum = 0.f;
+    for (int r = 0; r < kRmsCtas; r++) {
+      const float* pr = cluster.map_shared_rank(part, r);
+      n_r[r] = pr[0];
+      mean_r[r] = pr[1];
+      m2_r[r] = pr[2];
+      tot += n_r[r];
+      sum += n_r[r] * mean_r[r];
+    }
+    const float mu = sum / tot;
+    float m2t = 0.f;
+    for (int r = 0; r < kRmsCtas; r++) {
+      const float d = mean_r[r] - mu;
+      m2t += m2_r[r] + n_r[r] * d * d;
+    }
+    const int t = step ? *step : 0;
+    if (t >= 0 && t < out_len) out[t] = sqrtf(m2t / tot);
+  }
+  cluster.sync();  // the other CTAs' shared memory stays alive until CTA 0 has read it
 }
 
 }  // namespace
@@ -191,7 +214,7 @@ extern "C" int oopao_cl_integrate(const float* R, const float* s, int n_act, int
 extern "C" int oopao_cl_pupil_rms(const float* opd, const int* idx, int npup, const int* step, float* out,
                                   int out_len, void* stream) {
   OOPAO_CHECK_ARG(opd && idx && out && npup > 0, "bad argument");
-  cl_pupil_rms<<<1, 1024, 0, (cudaStream_t)stream>>>(opd, idx, npup, step, out, out_len);
+  cl_pupil_rms<<<kRmsCtas, 1024, 0, (cudaStream_t)stream>>>(opd, idx, npup, step, out, out_len);
   oopao_count_launches(1);
   OOPAO_CUDA_TRY(cudaGetLastError());
   return OOPAO_OK;

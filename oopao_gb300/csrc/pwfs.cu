@@ -429,6 +429,7 @@ struct SignalArgs {
   const unsigned char* valid;
   const float* ref2d;        // or null
   const int* sig_index;      // [n_signal]
+  const int* sig_inv;        // [n2d] signal entry of each 2-D cell, or -1
   float* signal_2d;          // [B][n2d]
   float* signal;             // [B][n_signal]
   float* norma;              // [B] or null
@@ -442,6 +443,7 @@ __global__ void pwfs_signal(SignalArgs a) {
   const int b = blockIdx.x;
   const float* fr = a.frame + (size_t)b * a.cam * a.cam;
   float* s2 = a.signal_2d + (size_t)b * a.n2d;
+  float* sg = a.signal + (size_t)b * a.n_signal;
   const bool slopes = a.mode <= 2;
   float part = 0.f;
   if (slopes) {
@@ -488,18 +490,23 @@ __global__ void pwfs_signal(SignalArgs a) {
       }
       const float rx = a.ref2d ? a.ref2d[idx] : 0.f;
       const float ry = a.ref2d ? a.ref2d[nq2 + idx] : 0.f;
-      s2[idx] = (sx / norma - rx) * a.units;
-      s2[nq2 + idx] = (sy / norma - ry) * a.units;
+      const float vx = (sx / norma - rx) * a.units, vy = (sy / norma - ry) * a.units;
+      s2[idx] = vx;
+      s2[nq2 + idx] = vy;
+      // signal = signal_2D[validSignal], written from the same registers
+      const int ex = a.sig_inv[idx], ey = a.sig_inv[nq2 + idx];
+      if (ex >= 0) sg[ex] = vx;
+      if (ey >= 0) sg[ey] = vy;
     }
   } else {
     for (int idx = threadIdx.x; idx < a.cam * a.cam; idx += blockDim.x) {
       const float rr = a.ref2d ? a.ref2d[idx] : 0.f;
-      s2[idx] = fr[idx] / norma - rr;
+      const float v = fr[idx] / norma - rr;
+      s2[idx] = v;
+      const int e = a.sig_inv[idx];
+      if (e >= 0) sg[e] = v;
     }
   }
-  __syncthreads();
-  float* sg = a.signal + (size_t)b * a.n_signal;
-  for (int t = threadIdx.x; t < a.n_signal; t += blockDim.x) sg[t] = s2[a.sig_index[t]];
   if (a.norma && threadIdx.x == 0) a.norma[b] = norma;
 }
 
@@ -1171,6 +1178,7 @@ extern "C" int oopao_pwfs_signal(const oopao_pwfs_plan* p, const float* frame, i
   OOPAO_CHECK_ARG(batch >= 1, "batch must be >= 1");
   SignalArgs a;
   a.frame = frame; a.valid = p->d_valid; a.ref2d = p->d_ref2d; a.sig_index = p->d_sig_index;
+  a.sig_inv = p->d_sig_inv;
   a.signal_2d = signal_2d; a.signal = signal; a.norma = norma;
   a.mode = p->sp_mode; a.cam = p->cam; a.nq = p->nq; a.n2d = p->n2d; a.n_signal = p->n_signal;
   a.n_valid = p->cam2;
