@@ -62,6 +62,16 @@ int oopao_pwfs_plan_destroy(oopao_pwfs_plan* plan);
 
 /* Pupil amplitude sqrt(src.intensity / nTheta) [res*res] (OOPAO/Pyramid.py:674). */
 int oopao_pwfs_set_amplitude(oopao_pwfs_plan* plan, const float* amp_host);
+/* Several Fourier masks measured together (the Bi-O Edge sensor's four,
+ * OOPAO/BioEdge.py:510-544): masks_host = [n_masks][n_fft][n_fft] complex64
+ * (1 to 8; mask 0 replaces the plan's mask).  The forward transforms of each
+ * modulation point are computed once; measure then writes frame
+ * [batch][n_masks][cam][cam] and raw [batch][n_masks][n_fft][n_fft].  With
+ * n_masks > 1 the plan needs a compile-time variant with one stage-B
+ * butterfly per thread (else OOPAO_ERR_UNSUPPORTED at measure) and the
+ * tangent/adjoint entry points return OOPAO_ERR_UNSUPPORTED. */
+int oopao_pwfs_set_masks(oopao_pwfs_plan* plan, int n_masks, const float* masks_host);
+int oopao_pwfs_n_masks(const oopao_pwfs_plan* plan);
 /* Optional per-point weights [n_theta] (Pyramid.weight_vector, :750-755);
  * NULL restores the plain sum. */
 int oopao_pwfs_set_weights(oopao_pwfs_plan* plan, const float* weights_host);

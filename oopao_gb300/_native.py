@@ -26,6 +26,8 @@ SIGNATURES = {
     'oopao_pwfs_plan_destroy': (c_int, [c_void_p]),
     'oopao_pwfs_set_amplitude': (c_int, [c_void_p, c_void_p]),
     'oopao_pwfs_set_weights': (c_int, [c_void_p, c_void_p]),
+    'oopao_pwfs_set_masks': (c_int, [c_void_p, c_int, c_void_p]),
+    'oopao_pwfs_n_masks': (c_int, [c_void_p]),
     'oopao_pwfs_set_launch': (c_int, [c_void_p, c_int, c_int, c_int, c_int]),
     'oopao_pwfs_set_pass_budget': (c_int, [c_void_p, c_size_t]),
     'oopao_pwfs_set_variant': (c_int, [c_void_p, c_int]),
@@ -124,7 +126,7 @@ def call(name, *args):
     memory cannot be released while the library reads it."""
     lib = load()
     st = getattr(lib, name)(*[_arg(a) for a in args])
-    if SIGNATURES[name][0] is c_int and name not in ('oopao_abi_version', 'oopao_pwfs_n_signal',
+    if SIGNATURES[name][0] is c_int and name not in ('oopao_abi_version', 'oopao_pwfs_n_signal', 'oopao_pwfs_n_masks',
                                                      'oopao_pwfs_get_variant', 'oopao_pwfs_num_variants'):
         check(st, name)
     return st

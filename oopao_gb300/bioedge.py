@@ -117,6 +117,7 @@ class BioEdge:
         self._dev = device()
         self._ws = Workspace()
         self._plans = None
+        self._shared_forward = False
         self._signal_configured = False
         self.mask_computation()
         self.slopesUnits = 1
@@ -139,10 +140,19 @@ class BioEdge:
 
     @property
     def plans(self):
+        """One plan holding the four masks (forward transforms shared), or,
+        for FFT sizes without a several-mask column pass, one plan per mask."""
         if self._plans is None:
             tel = self.telescope
-            self._plans = [_Plan(tel.resolution, self.resolution, self._cam_eff, m, self.modulation_path,
-                                 tel.resolution / tel.initial_resolution, True) for m in self.mask]
+            mk = lambda m: _Plan(tel.resolution, self.resolution, self._cam_eff, m, self.modulation_path,
+                                 tel.resolution / tel.initial_resolution, True)
+            p0 = mk(self.mask[0])
+            try:
+                N.call('oopao_pwfs_set_masks', p0.h, len(self.mask),
+                       np.ascontiguousarray(np.stack(self.mask), dtype=np.complex64))
+                self._plans, self._shared_forward = [p0], True
+            except OopaoError:
+                self._plans, self._shared_forward = [p0] + [mk(m) for m in self.mask[1:]], False
             if self.weight_vector is not None:
                 w = N.host(np.asarray(self.weight_vector, dtype=np.float64) / self.nTheta, np.float32)
                 for p in self._plans:
@@ -210,11 +220,25 @@ class BioEdge:
         x = opd_dev if opd_dev.ndim == 3 else opd_dev[None]
         x = x.contiguous()
         B, cam, n = x.shape[0], self._cam_eff, self.resolution
+        plans = self.plans
+        if self._shared_forward:
+            # one launch sequence; tiles [B][4][.][.] laid out 2 x 2
+            plan = plans[0]
+            plan.set_amplitude(half, self._amplitude_key())
+            tiles = torch.empty((B, 4, cam, cam), dtype=torch.float32, device=self._dev)
+            rtiles = torch.empty((B, 4, n, n), dtype=torch.float32, device=self._dev) if want_raw else None
+            nb = plan.workspace_bytes(min(B, self.max_batch))
+            ws = self._ws.get(nb)
+            N.call('oopao_pwfs_measure', plan.h, N.ptr(x), float(scale), B, N.ptr(tiles), N.ptr(rtiles), N.ptr(ws),
+                   nb, N.stream_handle())
+            frame = tiles.view(B, 2, 2, cam, cam).permute(0, 1, 3, 2, 4).reshape(B, 2 * cam, 2 * cam)
+            raw = rtiles.view(B, 2, 2, n, n).permute(0, 1, 3, 2, 4).reshape(B, 2 * n, 2 * n) if want_raw else None
+            return frame, raw
         frame = torch.empty((B, 2 * cam, 2 * cam), dtype=torch.float32, device=self._dev)
         raw = torch.empty((B, 2 * n, 2 * n), dtype=torch.float32, device=self._dev) if want_raw else None
         tile = torch.empty((B, cam, cam), dtype=torch.float32, device=self._dev)
         rtile = torch.empty((B, n, n), dtype=torch.float32, device=self._dev) if want_raw else None
-        for q, plan in enumerate(self.plans):
+        for q, plan in enumerate(plans):
             plan.set_amplitude(half, self._amplitude_key())
             nb = plan.workspace_bytes(min(B, self.max_batch))
             ws = self._ws.get(nb)

@@ -100,6 +100,8 @@ struct oopao_pwfs_plan {
   int variant;                    // 1 = use `fast` when available, 0 = generic
   int inv_target_ctas;            // row-inverse CTAs wanted per launch (2 resident waves)
   int cols3_ctas;                 // resident CTAs of the persistent column pass (0 = not used)
+  int n_masks;                    // Fourier masks measured together (1, or Bi-O Edge's 4)
+  float2* d_masks;                // [n_masks][n][n] when n_masks > 1
   int* d_err;                     // device error word (bounded waits of the persistent column pass)
   // signal processing
   int sp_mode, nq, n2d, n_signal, cam2;
@@ -183,6 +185,8 @@ struct ColsArgs {
   // persistent column pass (pwfs_cols3): items in this pass, error word
   int items;
   int* err;
+  // several masks (pwfs_cols2m): mask = [n_masks][n][n]
+  int n_masks;
 };
 
 __global__ void __launch_bounds__(kThreads) pwfs_cols(ColsArgs a) {
@@ -336,6 +340,8 @@ cudaError_t fast_attrs(const FastPasses* f, int res, int* inv_target, int* cols3
   cudaError_t e = cudaFuncSetAttribute(f->rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->smem_rows);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(f->cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->smem_cols);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(f->inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->smem_inv);
+  if (e == cudaSuccess && f->cols_m)
+    e = cudaFuncSetAttribute(f->cols_m, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f->smem_cols_m);
   int dev = 0, sms = 0, occ = 0;
   if (e == cudaSuccess) e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -546,6 +552,7 @@ void free_plan(oopao_pwfs_plan* p) {
   cudaFree(p->d_ref2d);
   cudaFree(p->d_sig_index);
   cudaFree(p->d_err);
+  cudaFree(p->d_masks);
   free(p);
 }
 
@@ -584,6 +591,7 @@ extern "C" int oopao_pwfs_plan_create(oopao_pwfs_plan** out, int res, int n, int
   p->cols_per_cta = std::min(16, max_lines(n, false));
   p->inv_rows_per_cta = std::min(8, max_lines(n, true));
   p->ksplit = 0;  // automatic
+  p->n_masks = 1;
   p->l2_budget = kDefaultPassBudget;
   p->slopes_units = 1.f;
   p->sp_mode = -1;
@@ -694,6 +702,49 @@ extern "C" int oopao_pwfs_set_amplitude(oopao_pwfs_plan* p, const float* amp_hos
   return OOPAO_OK;
 }
 
+extern "C" int oopao_pwfs_set_masks(oopao_pwfs_plan* p, int n_masks, const float* masks_host) {
+  OOPAO_CHECK_ARG(p && masks_host, "NULL argument");
+  OOPAO_CHECK_ARG(n_masks >= 1 && n_masks <= 8, "1 to 8 masks");
+  const size_t nn = (size_t)p->n * p->n;
+  if (n_masks > 1 && !(p->fast && p->variant >= 1 && p->fast->cols_m)) {
+    // move to the first compile-time variant that has the several-mask column pass
+    const FastPasses* c = nullptr;
+    const int cnt = fast_candidates(p->n, &c);
+    int v = 0;
+    for (int i = 0; i < cnt && !v; i++)
+      if (c[i].cols_m) v = i + 1;
+    if (!v) {
+      oopao_set_last_error("no compile-time plan with a several-mask column pass for this FFT size", __FILE__,
+                           __LINE__);
+      return OOPAO_ERR_UNSUPPORTED;
+    }
+    int target = kTargetCtas, c3 = 0;
+    OOPAO_CUDA_TRY(fast_attrs(c + (v - 1), p->res, &target, &c3));
+    p->fast = c + (v - 1);
+    p->variant = v;
+    p->inv_target_ctas = target;
+    p->cols3_ctas = c3;
+  }
+  // mask 0 is also the plan's single mask (spatial consumers, focal camera)
+  OOPAO_CUDA_TRY(cudaMemcpy(p->d_mask, masks_host, sizeof(float2) * nn, cudaMemcpyHostToDevice));
+  if (p->d_mask_conj) {
+    std::vector<float2> mc(nn);
+    const float2* m = reinterpret_cast<const float2*>(masks_host);
+    for (size_t i = 0; i < nn; i++) mc[i] = make_float2(m[i].x, -m[i].y);
+    OOPAO_CUDA_TRY(cudaMemcpy(p->d_mask_conj, mc.data(), sizeof(float2) * nn, cudaMemcpyHostToDevice));
+  }
+  cudaFree(p->d_masks);
+  p->d_masks = nullptr;
+  if (n_masks > 1) {
+    OOPAO_CUDA_TRY(cudaMalloc((void**)&p->d_masks, sizeof(float2) * nn * n_masks));
+    OOPAO_CUDA_TRY(cudaMemcpy(p->d_masks, masks_host, sizeof(float2) * nn * n_masks, cudaMemcpyHostToDevice));
+  }
+  p->n_masks = n_masks;
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_pwfs_n_masks(const oopao_pwfs_plan* p) { return p ? p->n_masks : -1; }
+
 extern "C" int oopao_pwfs_set_weights(oopao_pwfs_plan* p, const float* w) {
   OOPAO_CHECK_ARG(p, "NULL plan");
   if (!w) {
@@ -755,7 +806,8 @@ PassPlan plan_passes(const oopao_pwfs_plan* p, int batch, bool want_raw, size_t 
   pp.fast = f != nullptr;
   pp.fused = pp.fast && !want_raw && (f->l_inv % p->bin == 0);
   const int k = p->k;
-  pp.unit_bytes = ((size_t)p->res * p->n + (size_t)p->n * p->n) * sizeof(float2);
+  const int nm = p->n_masks;
+  pp.unit_bytes = ((size_t)p->res * p->n + (size_t)nm * p->n * p->n) * sizeof(float2);
   if (units < 1) units = 1;
   if (units >= (size_t)k) {
     pp.bc = (int)std::min<size_t>((size_t)batch, units / k);
@@ -769,7 +821,7 @@ PassPlan plan_passes(const oopao_pwfs_plan* p, int batch, bool want_raw, size_t 
     pp.ksplit = p->ksplit;
   } else {
     const int row_blocks = ceil_div(p->n, pp.fast ? f->l_inv : p->inv_rows_per_cta);
-    const int want = ceil_div(pp.fast ? p->inv_target_ctas : kTargetCtas, row_blocks * pp.bc);
+    const int want = ceil_div(pp.fast ? p->inv_target_ctas : kTargetCtas, row_blocks * pp.bc * nm);
     int best = 1;
     for (int d = 1; d <= k && d <= cap; d++) {
       if (k % d) continue;
@@ -786,13 +838,13 @@ PassPlan plan_passes(const oopao_pwfs_plan* p, int batch, bool want_raw, size_t 
   pp.slot_pts = k / pp.ksplit;
   if (pp.kp < k) pp.kp = std::max(pp.slot_pts, (pp.kp / pp.slot_pts) * pp.slot_pts);
   const size_t part = pp.fused ? (size_t)p->cam * p->cam : (size_t)p->n * p->n;
-  pp.bytes = (size_t)pp.bc * pp.kp * pp.unit_bytes + (size_t)pp.bc * pp.ksplit * part * sizeof(float) +
+  pp.bytes = (size_t)pp.bc * pp.kp * pp.unit_bytes + (size_t)pp.bc * nm * pp.ksplit * part * sizeof(float) +
              (size_t)pp.bc * p->res * p->res * sizeof(float2) + 1024;
   return pp;
 }
 
 size_t default_units(const oopao_pwfs_plan* p, int batch) {
-  const size_t unit = ((size_t)p->res * p->n + (size_t)p->n * p->n) * sizeof(float2);
+  const size_t unit = ((size_t)p->res * p->n + (size_t)p->n_masks * p->n * p->n) * sizeof(float2);
   size_t u = std::max<size_t>(1, p->l2_budget / unit);
   return std::min<size_t>(u, (size_t)batch * p->k);
 }
@@ -854,12 +906,17 @@ int measure_impl(const oopao_pwfs_plan* p, const float* opd, double phase_scale,
     oopao_set_last_error("workspace smaller than one pass needs", __FILE__, __LINE__);
     return OOPAO_ERR_WORKSPACE;
   }
-  const int n = p->n, res = p->res, k = p->k, cam = p->cam;
+  const int n = p->n, res = p->res, k = p->k, cam = p->cam, nm = p->n_masks;
   float2* y = (float2*)base;
   float2* z = y + (size_t)pp.bc * pp.kp * res * n;
-  float2* field = z + (size_t)pp.bc * pp.kp * n * n;
+  float2* field = z + (size_t)pp.bc * nm * pp.kp * n * n;
   float* part = (float*)(field + (size_t)pp.bc * res * res);
   const FastPasses* f = pp.fast ? p->fast : nullptr;
+  if (nm > 1 && (!f || !f->cols_m)) {
+    oopao_set_last_error("several masks need a compile-time plan with one stage-B butterfly per thread",
+                         __FILE__, __LINE__);
+    return OOPAO_ERR_UNSUPPORTED;
+  }
   PwfsProfile* prof = p->prof->enabled ? p->prof : nullptr;
   auto mark = [&](int stage) {
     if (prof) prof->mark(stage, st);
@@ -895,7 +952,12 @@ int measure_impl(const oopao_pwfs_plan* p, const float* opd, double phase_scale,
                   res, n, k0, kc, ng, p->off, p->cols_per_cta,
                   focal ? focal + (size_t)b0 * n * n : nullptr, (float)((double)n * n)};
       mark(1);
-      if (f && p->cols3_ctas > 0) {
+      if (nm > 1) {
+        ca.mask = p->d_masks;
+        ca.n_masks = nm;
+        dim3 g2(ceil_div(n, f->l_cols), kc, bc);
+        f->cols_m<<<g2, f->t * f->l_cols, f->smem_cols_m, st>>>(ca);
+      } else if (f && p->cols3_ctas > 0) {
         // persistent column pass: each CTA keeps one column block's mask and
         // streams its Y tiles with TMA over the (item, point) units
         CUtensorMap ymap;
@@ -918,7 +980,7 @@ int measure_impl(const oopao_pwfs_plan* p, const float* opd, double phase_scale,
                      n, k0, kc, k0 / pp.slot_pts, pp.slot_pts, pp.ksplit, p->inv_rows_per_cta, p->bin, cam};
       mark(2);
       if (f) {
-        dim3 g3(ceil_div(n, f->l_inv), kc / pp.slot_pts, bc);
+        dim3 g3(ceil_div(n, f->l_inv), kc / pp.slot_pts, bc * nm);
         f->inv<<<g3, f->t * f->l_inv, f->smem_inv, st>>>(ia);
       } else {
         dim3 g3(ceil_div(n, p->inv_rows_per_cta), kc / pp.slot_pts, bc);
@@ -929,12 +991,12 @@ int measure_impl(const oopao_pwfs_plan* p, const float* opd, double phase_scale,
     }
     mark(3);
     if (pp.fused) {
-      dim3 g4(ceil_div(cam * cam, 256), bc);
-      pwfs_reduce_binned<<<g4, 256, 0, st>>>(part, frame + (size_t)b0 * cam * cam, cam * cam, pp.ksplit);
+      dim3 g4(ceil_div(cam * cam, 256), bc * nm);
+      pwfs_reduce_binned<<<g4, 256, 0, st>>>(part, frame + (size_t)b0 * nm * cam * cam, cam * cam, pp.ksplit);
     } else {
-      dim3 g4(cam, bc);
-      pwfs_bin<<<g4, 128, 0, st>>>(part, frame + (size_t)b0 * cam * cam, raw ? raw + (size_t)b0 * n * n : nullptr,
-                                   n, cam, p->bin, pp.ksplit);
+      dim3 g4(cam, bc * nm);
+      pwfs_bin<<<g4, 128, 0, st>>>(part, frame + (size_t)b0 * nm * cam * cam,
+                                   raw ? raw + (size_t)b0 * nm * n * n : nullptr, n, cam, p->bin, pp.ksplit);
     }
     mark(3);
     launches += 1;
@@ -1243,6 +1305,10 @@ const AdPasses* ad_passes(int n) {
 
 int ad_setup(const oopao_pwfs_plan* p, const AdPasses** out) {
   const AdPasses* a = ad_passes(p->n);
+  if (p->n_masks != 1) {
+    oopao_set_last_error("tangent/adjoint passes take a plan with one mask", __FILE__, __LINE__);
+    return OOPAO_ERR_UNSUPPORTED;
+  }
   if (!a || !p->fast || p->variant < 1) {
     oopao_set_last_error("tangent/adjoint passes exist for n_fft in {72,112,128,264,504} only", __FILE__, __LINE__);
     return OOPAO_ERR_UNSUPPORTED;
@@ -1450,6 +1516,10 @@ extern "C" int oopao_pwfs_set_variant(oopao_pwfs_plan* p, int variant) {
   OOPAO_CHECK_ARG(variant >= 0, "variant must be 0 (generic) or a compile-time plan index >= 1");
   if (variant > cnt) {
     oopao_set_last_error("no such compile-time plan for this FFT size", __FILE__, __LINE__);
+    return OOPAO_ERR_UNSUPPORTED;
+  }
+  if (p->n_masks > 1 && (variant == 0 || !c[variant - 1].cols_m)) {
+    oopao_set_last_error("this variant has no several-mask column pass", __FILE__, __LINE__);
     return OOPAO_ERR_UNSUPPORTED;
   }
   if (variant >= 1) {

@@ -240,6 +240,107 @@ __global__ void __launch_bounds__(T* L) pwfs_cols2(ColsArgs a) {
   }
 }
 
+// ---- pass 2 for several Fourier masks (Bi-O Edge) ----
+// The forward column transform is computed once; for each of the n_masks
+// masks the spectrum is multiplied by that mask and transformed back, giving
+// one Z per mask ([B][n_masks][kp][N][N]).  Variants with one stage-B
+// butterfly per thread only (the spectrum stays in registers across masks).
+template <int N, int R1, int R2, int T, int L>
+__global__ void __launch_bounds__(T* L) pwfs_cols2m(ColsArgs a) {
+  constexpr int LAY1 = cols_layout(R1, R2, T, L), LAY2 = cols_layout(R2, R1, T, L);
+  constexpr int R1P = LAY1 >> 16, LS1 = LAY1 & 0xFFFF;
+  constexpr int R2P = LAY2 >> 16, LS2 = LAY2 & 0xFFFF;
+  constexpr int PBA = (R2 + T - 1) / T;
+  static_assert((R1 + T - 1) / T == 1, "one stage-B butterfly per thread");
+  extern __shared__ float2 sm[];
+  float2* tw = sm;
+  float2* twi = sm + N;
+  float2* b1 = sm + 2 * N;   // forward exchange, reused by the inverse exchange
+  const int tid = threadIdx.x;
+  const int l = tid % L, t = tid / L;
+  for (int i = tid; i < N; i += T * L) {
+    tw[i] = a.tw[(i % R1) * (i / R1)];
+    const float2 w = a.tw[(i % R2) * (i / R2)];
+    twi[i] = make_float2(w.x, -w.y);
+  }
+  const int b = blockIdx.z, kk = blockIdx.y, c = blockIdx.x * L + l;
+  const int kabs = a.k0 + kk;
+  const int g = a.group ? a.group[kabs] : kk;
+  const bool active = c < N;
+  const int res = a.res, off = a.off, nm = a.n_masks;
+  const float2* y = a.y + ((size_t)b * a.ng + g) * res * N + c;
+  const float2* cf = a.colfac + (size_t)kabs * res;
+  float2* x1 = b1 + l * LS1;
+  float2* x2 = b1 + l * LS2;
+#pragma unroll
+  for (int p = 0; p < PBA; p++) {
+    const int j = t + p * T;
+    if (j < R2) {
+      float2 v[R1];
+#pragma unroll
+      for (int m = 0; m < R1; m++) {
+        const int i = j + m * R2 - off;
+        v[m] = (active && i >= 0 && i < res) ? cmul(y[(size_t)i * N], cf[i]) : make_float2(0.f, 0.f);
+      }
+      dft<R1, false>(v);
+#pragma unroll
+      for (int q = 0; q < R1; q++) x1[j * R1P + q] = v[q];
+    }
+  }
+  __syncthreads();
+  const int j = t;
+  float2 spec[R2];  // forward spectrum of column c, rows j + q*R1
+  if (j < R1) {
+#pragma unroll
+    for (int m = 0; m < R2; m++) {
+      const float2 u = x1[m * R1P + j];
+      spec[m] = (m == 0) ? u : cmul(u, tw[m * R1 + j]);
+    }
+    dft<R2, false>(spec);
+    if (a.focal && active) {
+      float* fo = a.focal + (size_t)b * N * N + c;
+#pragma unroll
+      for (int q = 0; q < R2; q++) atomicAdd(fo + (size_t)(j + q * R1) * N, a.focal_scale * cabs2(spec[q]));
+    }
+  }
+  for (int mi = 0; mi < nm; mi++) {
+    float2 v[R2];
+    if (j < R1) {
+      const float2* mk = a.mask + (size_t)mi * N * N + c;
+#pragma unroll
+      for (int q = 0; q < R2; q++) {
+        const float2 mq = active ? mk[(size_t)(j + q * R1) * N] : make_float2(0.f, 0.f);
+        v[q] = cmul(spec[q], mq);
+      }
+      dft<R2, true>(v);
+    }
+    __syncthreads();  // earlier reads of the exchange buffer are done
+    if (j < R1) {
+#pragma unroll
+      for (int q = 0; q < R2; q++) x2[j * R2P + q] = v[q];
+    }
+    __syncthreads();
+    float2* z = a.z + (((size_t)b * nm + mi) * a.kp + kk) * N * N + c;
+#pragma unroll
+    for (int p = 0; p < PBA; p++) {
+      const int jj = t + p * T;
+      if (jj < R2) {
+        float2 w[R1];
+#pragma unroll
+        for (int m = 0; m < R1; m++) {
+          const float2 u = x2[m * R2P + jj];
+          w[m] = (m == 0) ? u : cmul(u, twi[m * R2 + jj]);
+        }
+        dft<R1, true>(w);
+        if (active) {
+#pragma unroll
+          for (int q = 0; q < R1; q++) z[(size_t)(jj + q * R2) * N] = w[q];
+        }
+      }
+    }
+  }
+}
+
 // ---- pass 2, persistent form ----
 // A CTA owns a block of L columns for the whole pass: it loads that block of
 // the mask into shared memory once, then loops over (item, point) units,
@@ -519,6 +620,9 @@ struct FastPasses {
   int l_cols3;
   void (*cols3)(const CUtensorMap, ColsArgs);
   size_t (*smem_cols3)(int res);
+  // column pass over several masks (null unless one stage-B butterfly per thread)
+  void (*cols_m)(ColsArgs);
+  size_t smem_cols_m;
 };
 
 template <int N, int R1, int R2, int T, int LR, int LC, int LI>
@@ -540,6 +644,12 @@ FastPasses make_fast() {
   f.l_cols3 = 0;
   f.cols3 = nullptr;
   f.smem_cols3 = nullptr;
+  f.cols_m = nullptr;
+  f.smem_cols_m = 0;
+  if constexpr ((R1 + T - 1) / T == 1) {
+    f.cols_m = pwfs_cols2m<N, R1, R2, T, LC>;
+    f.smem_cols_m = sizeof(float2) * (2 * N + (size_t)LC * imax(LS1C, LS2C));
+  }
   return f;
 }
 

@@ -74,3 +74,38 @@ def test_interaction_matrix(system):
     with _quiet():
         calib = og.InteractionMatrix(ngs, tel, dm, wfs, d['im_m2c'], 1e-8, single_pass=False, invert=False)
     assert O.rel_l2(np.asarray(calib.D), d['im_pp_D']) < 1e-4
+
+
+def test_shared_forward_matches_per_mask_plans(system):
+    """One plan with the four masks (forward transforms shared) gives the
+    frames of four single-mask plans.  bioedge_tiny (N = 72) takes the
+    shared path; bioedge_grey (N = 128, two stage-B butterflies per thread)
+    keeps one plan per mask; both are checked against the goldens above."""
+    import torch
+    from oopao_gb300 import _native as N
+    from oopao_gb300.pyramid import _Plan
+    d, tel, ngs, dm, wfs = system
+    plans = wfs.plans
+    assert wfs._shared_forward == (wfs.resolution == 72)
+    rng = np.random.default_rng(9)
+    opd = torch.as_tensor(rng.standard_normal((3, tel.resolution, tel.resolution)) * 50e-9, dtype=torch.float32,
+                          device='cuda')
+    scale = 2 * np.pi / ngs.wavelength
+    ngs ** tel
+    frame, raw = wfs._measure_frames(opd, scale, want_raw=True)
+    cam, n = wfs._cam_eff, wfs.resolution
+    half = 0.5 * np.asarray(ngs.intensity, dtype=np.float64)
+    for q, m in enumerate(wfs.mask):
+        p = _Plan(tel.resolution, n, cam, m, wfs.modulation_path, 1.0, True)
+        p.set_amplitude(half, None)
+        nb = p.workspace_bytes(3)
+        ws = torch.empty(nb, dtype=torch.uint8, device='cuda')
+        tile = torch.empty((3, cam, cam), device='cuda')
+        rt = torch.empty((3, n, n), device='cuda')
+        N.call('oopao_pwfs_measure', p.h, N.ptr(opd), float(scale), 3, N.ptr(tile), N.ptr(rt), N.ptr(ws), nb,
+               N.stream_handle())
+        i, j = divmod(q, 2)
+        ft = frame[:, i * cam:(i + 1) * cam, j * cam:(j + 1) * cam].double().cpu().numpy()
+        rr = raw[:, i * n:(i + 1) * n, j * n:(j + 1) * n].double().cpu().numpy()
+        assert O.rel_l2(ft, tile.double().cpu().numpy()) < 1e-6, q
+        assert O.rel_l2(rr, rt.double().cpu().numpy()) < 1e-6, q
