@@ -277,8 +277,8 @@ int oopao_dm_vjp_f32(const float* modes_t, const float* g, int n_act, int n_pix,
  * Tangent (JVP) and adjoint (VJP) of the propagation.  No reference
  * counterpart: the reference obtains derivatives only by finite push-pull
  * differences (OOPAO/calibration/InteractionMatrix.py:117-158).  Available
- * for n_fft in {72, 112, 128, 264, 504} (compile-time plans), otherwise
- * OOPAO_ERR_UNSUPPORTED.  Workspace: oopao_pwfs_ad_workspace_bytes.
+ * for n_fft in {72, 112, 128, 264, 504, 1920} (compile-time plans) on plans
+ * with one mask, otherwise OOPAO_ERR_UNSUPPORTED.  Workspace: oopao_pwfs_ad_workspace_bytes.
  * ------------------------------------------------------------------------ */
 size_t oopao_pwfs_ad_workspace_bytes(const oopao_pwfs_plan* plan, int batch);
 /* dframe[b] = d frame / d opd at opd0 applied to dopd[b].

@@ -1310,7 +1310,8 @@ int ad_setup(const oopao_pwfs_plan* p, const AdPasses** out) {
     return OOPAO_ERR_UNSUPPORTED;
   }
   if (!a || !p->fast || p->variant < 1) {
-    oopao_set_last_error("tangent/adjoint passes exist for n_fft in {72,112,128,264,504} only", __FILE__, __LINE__);
+    oopao_set_last_error("tangent/adjoint passes exist for n_fft in {72,112,128,264,504,1920} only", __FILE__,
+                         __LINE__);
     return OOPAO_ERR_UNSUPPORTED;
   }
   cudaError_t e = cudaFuncSetAttribute(a->field, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a->smem_field);
