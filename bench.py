@@ -382,6 +382,57 @@ def gsc_leg(peaks):
     return out
 
 
+def cl_gsc(n_steps=500, og_start=30):
+    """The reference's GSC tutorial loop on the 20x20 configuration: 300-mode
+    KL modal reconstructor (push-pull IM, full FP64 pseudo-inverse), one
+    infinite-screen layer (r0 0.10 m, L0 25 m, 10 m/s), gain 0.4, frame delay
+    2; a GainSensingCamera on the 300 KL modes (basis = tel.OPD of the modes),
+    calibrated on the flat-wavefront focal-plane frame; from step `og_start`
+    the commands are M2C @ diag(1/og) @ M @ s.  Every step also forms the
+    full-resolution focal-plane frame and its optical gains (captured in the
+    same CUDA graph).  Reports us per step and the long-exposure Strehl with
+    and without the compensation on the same turbulence."""
+    import torch
+    import oopao_gb300 as og
+    from oopao_gb300.calibration import InteractionMatrix
+    from oopao_gb300.closed_loop import ClosedLoop
+    tel, ngs, dm, wfs = build_system(0)
+    m2c = kl_like_basis(dm.modes, tel.pupil, NMODES)
+    with _quiet():
+        calib = InteractionMatrix(ngs, tel, dm, wfs, m2c, STROKE, single_pass=False)
+        dm.coefs = m2c
+        ngs ** tel * dm
+        basis = np.array(tel.OPD)
+        dm.coefs = 0
+        gsc = og.GainSensingCamera(wfs.mask, basis)
+        wfs.focal_plane_camera.resolution = wfs.nRes
+        ngs ** tel * wfs
+        wfs * wfs.focal_plane_camera
+        wfs.focal_plane_camera * gsc
+        atm = og.Atmosphere(telescope=tel, r0=0.10, L0=25, fractionalR0=[1.0], windSpeed=[10.], windDirection=[0.],
+                            altitude=[0.])
+        atm.initializeAtmosphere(tel)
+    M = np.asarray(calib.M)
+    out = {'config': '20x20 PWFS, 300 KL modes, 1 layer r0 0.10 m, gain 0.4, delay 2, %d frames, OG compensation '
+                     'from frame %d' % (n_steps, og_start)}
+    for key, start in (('with_og', og_start), ('without_og', 10 ** 9)):
+        cl = ClosedLoop(tel, ngs, dm, wfs, M, gain=0.4, frame_delay=2, layers=atm, max_steps=n_steps + 10,
+                        science=True, gsc=gsc, M2C=m2c, og_start=start)
+        cl.capture()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        cl.run(n_steps)
+        e1.record()
+        torch.cuda.synchronize()
+        ogv = cl.og[0].cpu().numpy()
+        out[key] = {'us_per_step': e0.elapsed_time(e1) / n_steps * 1e3,
+                    'strehl_le_pct': cl.long_exposure_strehl(),
+                    'wfe_mean_last_100_nm': float(cl.residual_wfe[-100:].mean() * 1e9),
+                    'og_first_modes': [float(v) for v in ogv[:5]], 'og_mean': float(ogv.mean())}
+        del cl
+    return out
+
+
 def _event_ms(fn, reps, warm=3):
     import torch
     for _ in range(warm):
@@ -773,6 +824,7 @@ def run_ours(args):
         extra['dm_projection'] = dm_projection(pk)
         extra['gsc'] = gsc_leg(pk)
         extra['next_rows'] = next_rows_leg()
+        extra['cl_gsc_20x20'] = cl_gsc()
 
     if rank == 0:
         line = {
@@ -853,6 +905,8 @@ def run_case(args):
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_pop()
         out = {'case': args.case, 'batch': args.batch, 'reps': args.reps, 'tc_status': dm.tensor_core_status()}
+    elif args.case == 'clgsc':
+        out = {'case': args.case, 'cl_gsc_20x20': cl_gsc()}
     elif args.case == 'next':
         out = {'case': args.case, 'next_rows': next_rows_leg()}
     elif args.case == 'gsc':
@@ -873,7 +927,7 @@ def main():
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline and accuracy legs')
     ap.add_argument('--no-extra', action='store_true',
                     help='skip the interaction-matrix comparisons and the closed-loop rate')
-    ap.add_argument('--case', default=None, help='run a small profiling workload (%s, dm40, gsc, next) instead'
+    ap.add_argument('--case', default=None, help='run a small profiling workload (%s, dm40, gsc, next, clgsc) instead'
                     % ', '.join(CASES))
     ap.add_argument('--batch', type=int, default=16)
     ap.add_argument('--reps', type=int, default=3)

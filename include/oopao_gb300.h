@@ -236,6 +236,14 @@ int oopao_cl_screen(int n_layers, const float* const* screens, const int* height
  * *step by one when step is not NULL. */
 int oopao_cl_integrate(const float* R, const float* s, int n_act, int n_sig, float gain, float* coefs,
                        int* step, void* stream);
+/* Modal commands with optical-gain compensation (the reference's GSC
+ * tutorial, M2C @ diag(1/og) @ M @ s): y[m] = (M @ s)[m] / og[m] once
+ * *step >= og_start, (M @ s)[m] before or when og is NULL.  M device
+ * [n_modes][n_sig] float32, og device float64 [n_modes] (the gains of
+ * oopao_gsc_optical_gains), y device [n_modes]; step may be NULL (always
+ * compensated). */
+int oopao_cl_modal(const float* M, const float* s, int n_modes, int n_sig, const double* og, int og_start,
+                   const int* step, float* y, void* stream);
 /* Residual wavefront RMS over pupil pixels idx[npup] (device) written to
  * out[*step] (device, out_len entries). */
 int oopao_cl_pupil_rms(const float* opd, const int* idx, int npup, const int* step, float* out, int out_len,

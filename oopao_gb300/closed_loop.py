@@ -17,10 +17,16 @@ Every operation is a launch of ``liboopao_gb300`` on preallocated buffers; a
 device step counter carries the time index, so the captured graph is
 replayed as is for every later step (``ClosedLoop.run``).
 
-The turbulence is a set of periodic von Karman layers translated by frozen
-flow (``VonKarmanLayers``).  It stands in for the reference's infinite
-phase screens (``OOPAO/Atmosphere.py:410-531``), whose extrusion and
-sub-pixel shift (skimage ``warp``) are not reproduced here.
+The turbulence is either the reference's infinite phase screens
+(``oopao_gb300.Atmosphere``, updated on the device inside the captured step)
+or a set of periodic von Karman layers translated by frozen flow
+(``VonKarmanLayers``, a lighter stand-in).
+
+With a calibrated ``GainSensingCamera`` the loop follows the reference's GSC
+tutorial (``tutorials/AO_closed_loop_Pyramid_WFS_GSC.py``): every step also
+forms the full-resolution focal-plane (modulation) camera frame, computes the
+optical gains from it and, from step ``og_start`` on, applies
+coefs -= gain * M2C @ diag(1/og) @ M @ s with the modal reconstructor M.
 """
 import numpy as np
 import torch
@@ -97,8 +103,11 @@ def strehl_meter(psf, psf_ref):
 
 
 class ClosedLoop:
+    """reconstructor: [nValidAct, nSignal] (M2C @ M), or, with ``gsc``, the
+    modal reconstructor M [n_modes, nSignal] and ``M2C`` [nValidAct, n_modes]."""
+
     def __init__(self, tel, ngs, dm, wfs, reconstructor, gain=0.4, frame_delay=1, layers=None,
-                 max_steps=100000, science=False):
+                 max_steps=100000, science=False, gsc=None, M2C=None, og_start=0):
         if frame_delay not in (1, 2):
             raise OopaoError('frame_delay must be 1 or 2')
         self.tel, self.ngs, self.dm, self.wfs = tel, ngs, dm, wfs
@@ -107,11 +116,35 @@ class ClosedLoop:
         self.frame_delay = frame_delay
         res = tel.resolution
         self.res = res
-        R = np.asarray(reconstructor, dtype=np.float32)
-        if R.shape != (dm.nValidAct, wfs.nSignal):
-            raise OopaoError('reconstructor must be [nValidAct, nSignal]')
         d = self.dev
-        self.R = torch.as_tensor(np.ascontiguousarray(R), device=d)
+        self.gsc = gsc
+        if gsc is not None:
+            if M2C is None:
+                raise OopaoError('optical-gain compensation needs M2C and the modal reconstructor M')
+            Mr = np.asarray(reconstructor, dtype=np.float32)
+            m2c = np.asarray(M2C, dtype=np.float32)
+            if Mr.shape != (gsc.n_modes, wfs.nSignal) or m2c.shape != (dm.nValidAct, gsc.n_modes):
+                raise OopaoError('with gsc: reconstructor [n_modes, nSignal] and M2C [nValidAct, n_modes]')
+            if not gsc.calibration_ready:
+                raise OopaoError('the GainSensingCamera must be calibrated first')
+            if gsc.n != wfs.resolution:
+                raise OopaoError('the GainSensingCamera mask must be the pyramid mask (N x N)')
+            if not wfs.psfCentering and wfs.spatialFilter is not None:
+                raise OopaoError('optical-gain compensation in the loop takes a pyramid without spatial filter '
+                                 'in the 1-pixel-centred branch')
+            self.M = torch.as_tensor(np.ascontiguousarray(Mr), device=d)
+            self.R = torch.as_tensor(np.ascontiguousarray(m2c), device=d)   # M2C
+            self.y = torch.zeros(gsc.n_modes, dtype=torch.float32, device=d)
+            self.og = torch.ones((1, gsc.n_modes), dtype=torch.float64, device=d)
+            self.focal = torch.zeros((1, wfs.resolution, wfs.resolution), dtype=torch.float32, device=d)
+            self.og_start = int(og_start)
+            self._gsc_nb = N.load().oopao_gsc_workspace_bytes(gsc._plan, 1)
+            self._gsc_ws = torch.empty(self._gsc_nb, dtype=torch.uint8, device=d)
+        else:
+            R = np.asarray(reconstructor, dtype=np.float32)
+            if R.shape != (dm.nValidAct, wfs.nSignal):
+                raise OopaoError('reconstructor must be [nValidAct, nSignal]')
+            self.R = torch.as_tensor(np.ascontiguousarray(R), device=d)
         self.coefs = torch.zeros(dm.nValidAct, dtype=torch.float32, device=d)
         self.step_counter = torch.zeros(1, dtype=torch.int32, device=d)
         self.opd_atm = torch.zeros((1, res, res), dtype=torch.float32, device=d)
@@ -180,6 +213,8 @@ class ClosedLoop:
 
     def reset(self):
         self.coefs.zero_()
+        if self.gsc is not None:
+            self.og.fill_(1.0)
         self.step_counter.zero_()
         self.s_prev.zero_()
         self.wfe.zero_()
@@ -226,10 +261,25 @@ class ClosedLoop:
                self.wfe, self.max_steps, st)
         if self.science:
             self._science()
-        N.call('oopao_pwfs_measure', self.plan.h, self.opd, self.scale, 1, self.frame, None, self.ws,
-               self.ws_bytes, st)
+        if self.gsc is not None:
+            # frame + full-resolution focal-plane camera, then the optical gains
+            N.call('oopao_pwfs_measure_focal', self.plan.h, self.opd, self.scale, 1, self.frame, None, self.focal,
+                   self.ws, self.ws_bytes, st)
+            N.call('oopao_gsc_optical_gains', self.gsc._plan, self.focal, 1, self.og, None, None, self._gsc_ws,
+                   self._gsc_nb, st)
+        else:
+            N.call('oopao_pwfs_measure', self.plan.h, self.opd, self.scale, 1, self.frame, None, self.ws,
+                   self.ws_bytes, st)
         N.call('oopao_pwfs_signal', self.plan.h, self.frame, 1, self.s2d, self.s, None, st)
-        if self.frame_delay == 1:
+        if self.gsc is not None:
+            s_in = self.s if self.frame_delay == 1 else self.s_prev
+            N.call('oopao_cl_modal', self.M, s_in, self.M.shape[0], self.M.shape[1], self.og, self.og_start,
+                   self.step_counter, self.y, st)
+            N.call('oopao_cl_integrate', self.R, self.y, self.R.shape[0], self.R.shape[1], self.gain, self.coefs,
+                   self.step_counter, st)
+            if self.frame_delay == 2:
+                self.s_prev.copy_(self.s)
+        elif self.frame_delay == 1:
             N.call('oopao_cl_integrate', self.R, self.s, self.R.shape[0], self.R.shape[1], self.gain, self.coefs,
                    self.step_counter, st)
         else:

@@ -95,6 +95,46 @@ __global__ void __launch_bounds__(256) cl_integrate(const float* __restrict__ R,
   if (blockIdx.x == 0 && threadIdx.x == 0 && step) *step += 1;
 }
 
+// Modal commands with optical-gain compensation (the GSC tutorial,
+// tutorials/AO_closed_loop_Pyramid_WFS_GSC.py: M2C @ diag(1/og) @ M @ s):
+// y[m] = (M[m] . s) / og[m] from step og_start on (og = 1 before).  Same
+// layout and load pattern as cl_integrate.
+__global__ void __launch_bounds__(256) cl_modal(const float* __restrict__ M, const float* __restrict__ s,
+                                                int n_modes, int n_sig, const double* __restrict__ og, int og_start,
+                                                const int* __restrict__ step, float* __restrict__ y) {
+  __shared__ float red[8];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int mode = blockIdx.x * kIntActPerBlock + (w >> 2), part = w & 3;
+  float acc = 0.f;
+  if (mode < n_modes) {
+    const float* r = M + (size_t)mode * n_sig;
+    int j = part * 32 + lane;
+    for (; j + 7 * 128 < n_sig; j += 8 * 128) {
+      float rv[8], sv[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        rv[u] = r[j + u * 128];
+        sv[u] = s[j + u * 128];
+      }
+#pragma unroll
+      for (int u = 0; u < 8; u++) acc = fmaf(rv[u], sv[u], acc);
+    }
+    for (; j < n_sig; j += 128) acc = fmaf(r[j], s[j], acc);
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) red[w] = acc;
+  __syncthreads();
+  if (threadIdx.x < kIntActPerBlock) {
+    const int m = blockIdx.x * kIntActPerBlock + threadIdx.x;
+    if (m < n_modes) {
+      const float* q = red + 4 * threadIdx.x;
+      const float v = (q[0] + q[1]) + (q[2] + q[3]);
+      const bool comp = og != nullptr && (step == nullptr || *step >= og_start);
+      y[m] = comp ? v / (float)og[m] : v;
+    }
+  }
+}
+
 __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
   const float y = x - c;
   const float t = s + y;
@@ -206,6 +246,17 @@ extern "C" int oopao_cl_integrate(const float* R, const float* s, int n_act, int
   OOPAO_CHECK_ARG(n_act > 0 && n_sig > 0, "sizes must be positive");
   cl_integrate<<<ceil_div(n_act, kIntActPerBlock), 256, 0, (cudaStream_t)stream>>>(R, s, n_act, n_sig, gain, coefs,
                                                                                   step);
+  oopao_count_launches(1);
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_cl_modal(const float* M, const float* s, int n_modes, int n_sig, const double* og,
+                              int og_start, const int* step, float* y, void* stream) {
+  OOPAO_CHECK_ARG(M && s && y, "NULL argument");
+  OOPAO_CHECK_ARG(n_modes > 0 && n_sig > 0, "sizes must be positive");
+  cl_modal<<<ceil_div(n_modes, kIntActPerBlock), 256, 0, (cudaStream_t)stream>>>(M, s, n_modes, n_sig, og, og_start,
+                                                                                step, y);
   oopao_count_launches(1);
   OOPAO_CUDA_TRY(cudaGetLastError());
   return OOPAO_OK;

@@ -118,3 +118,65 @@ def test_long_exposure_strehl_vs_fp64_oracle(system):
     assert O.rel_l2(wfe, ref['wfe']) < 1e-4
     assert O.rel_l2(psf, ref['psf_le']) < 1e-4
     assert abs(sr - ref['strehl_le']) < 1e-4 * ref['strehl_le']
+
+
+@pytest.fixture(scope='module')
+def gsc_system(system):
+    """Modal loop of 20 modes (zonal M2C slice) with a GainSensingCamera
+    calibrated on the flat-wavefront focal-plane frame."""
+    import oopao_gb300 as og
+    tel, ngs, dm, wfs, _ = system
+    rng = np.random.default_rng(3)
+    m2c = rng.standard_normal((dm.nValidAct, 20))
+    with _quiet():
+        calib = og.InteractionMatrix(ngs, tel, dm, wfs, M2C=m2c, stroke=1e-8, method='jvp')
+        dm.coefs = m2c
+        ngs ** tel * dm
+        basis = np.array(tel.OPD)
+        dm.coefs = 0
+        gsc = og.GainSensingCamera(wfs.mask, basis)
+        wfs.focal_plane_camera.resolution = wfs.nRes
+        ngs ** tel * wfs
+        wfs * wfs.focal_plane_camera
+        wfs.focal_plane_camera * gsc
+    return m2c, np.asarray(calib.M), gsc
+
+
+def test_gsc_loop_graph_equals_eager(system, gsc_system):
+    import torch
+    from oopao_gb300.closed_loop import ClosedLoop, VonKarmanLayers
+    tel, ngs, dm, wfs, _ = system
+    m2c, M, gsc = gsc_system
+    layers = VonKarmanLayers(tel, r0=0.15, L0=25, windSpeed=(10.,), seed=4)
+    cl = ClosedLoop(tel, ngs, dm, wfs, M, gain=0.3, layers=layers, gsc=gsc, M2C=m2c, og_start=3, max_steps=40)
+    cl.reset()
+    cl.run(8, graph=False)
+    eager = cl.coefs.clone()
+    og_eager = cl.og.clone()
+    cl.capture()
+    cl.run(8)
+    # the focal-plane frame is summed over modulation points with float
+    # atomics, so the gains (and the commands after og_start) agree to
+    # round-off rather than bit for bit
+    assert O.rel_l2(cl.coefs.double().cpu().numpy(), eager.double().cpu().numpy()) < 1e-5
+    assert O.rel_l2(cl.og.cpu().numpy(), og_eager.cpu().numpy()) < 1e-6
+    # the gains inside the loop are the camera's gains of the loop's focal frame
+    gsc.compute_optical_gains(cl.focal[0])
+    assert O.rel_l2(cl.og[0].cpu().numpy(), gsc.og) < 1e-6
+    assert np.all(np.isfinite(gsc.og)) and not np.allclose(gsc.og, 1.0)
+
+
+def test_gsc_loop_without_compensation_is_the_plain_loop(system, gsc_system):
+    """og_start beyond the run: M2C @ (M @ s) in two GEMVs equals the plain
+    loop with R = M2C @ M (float32 summation order only)."""
+    from oopao_gb300.closed_loop import ClosedLoop, VonKarmanLayers
+    tel, ngs, dm, wfs, _ = system
+    m2c, M, gsc = gsc_system
+    layers = VonKarmanLayers(tel, r0=0.15, L0=25, windSpeed=(10.,), seed=4)
+    a = ClosedLoop(tel, ngs, dm, wfs, M, gain=0.3, layers=layers, gsc=gsc, M2C=m2c, og_start=10 ** 6, max_steps=40)
+    a.reset()
+    a.run(10, graph=False)
+    b = ClosedLoop(tel, ngs, dm, wfs, m2c @ M, gain=0.3, layers=layers, max_steps=40)
+    b.reset()
+    b.run(10, graph=False)
+    assert O.rel_l2(a.coefs.double().cpu().numpy(), b.coefs.double().cpu().numpy()) < 1e-4
