@@ -760,7 +760,9 @@ def run_ours(args):
     byts = kernel_bytes(top, RES, n, cam, units, items, nl)
     achieved = byts / (totals[top] / 1000.0) / 1e9
     peak, peak_kind = load_peaks()
-    tr = load_traffic(top)
+    variant = int(N_variant(wfs))
+    # per-variant capture when the variant's kernel differs (persistent column pass)
+    tr = load_traffic('%s@v%d' % (top, variant)) or load_traffic(top)
     traffic = None
     if tr is not None:
         # committed ncu capture: DRAM bytes per (item, point) unit, scaled to one launch here
@@ -836,7 +838,7 @@ def run_ours(args):
                        'fft_grid': n, 'camera': cam, 'batch_per_launch': wfs.max_batch,
                        'l2': 'intermediates (>=2.4 GB per launch) exceed L2; no flush needed',
                        'im_rel_fro_err_vs_fp64_oracle_2cols': err},
-            'roofline': {'bound': 'hbm', 'kernel': top, 'achieved': achieved, 'peak': peak,
+            'roofline': {'bound': 'hbm', 'kernel': top, 'variant': variant, 'achieved': achieved, 'peak': peak,
                          'unit': 'GB/s', 'frac': achieved / peak, 'peak_kind': peak_kind,
                          'traffic': traffic, 'kernel_share': share,
                          'kernel_ms': {kk: totals[kk] for kk in KERNELS},
