@@ -2,7 +2,7 @@
 and I/O dependencies.
 
 Used only by ``make_golden.py`` (fixture generation) where the reference
-source tree is present.  Nothing here runs on a GPU machine.
+source tree is present.  The tests never import it: they read the fixtures.
 
 Recipe:
   * the package writes ``precision_oopao.npy`` into the shortest ``sys.path``
