@@ -174,7 +174,8 @@ class ClosedLoop:
             # device update is one more part of the captured step
             self._atm = layers
             layers.reset_state()
-            layers.prepare(max_steps + 1)
+            layers.prepare(max_steps + 2)
+            layers._launch(advance=True)         # the first step's turbulence (one update)
             self._atm_opd = layers.device_opd().view(1, res, res)
         elif layers is not None:
             self._scr = [torch.as_tensor(s, device=d) for s in layers.screens]
@@ -210,6 +211,7 @@ class ClosedLoop:
             self.psf_ref = (f.real.double() ** 2 + f.imag.double() ** 2).cpu().numpy()
             self._sci_pad.zero_()
         self.graph = None
+        self._side = torch.cuda.Stream(device=d)
 
     def reset(self):
         self.coefs.zero_()
@@ -221,7 +223,11 @@ class ClosedLoop:
         if self.science:
             self.psf_le.zero_()
         if self._atm is not None:
+            # step t sees the atmosphere after t + 1 updates (the reference
+            # tutorial updates it first in every iteration); each step then
+            # prepares the next step's turbulence while the sensor runs
             self._atm.reset_state()
+            self._atm._launch(advance=True)
 
     def _science(self):
         lo, res = self._sci_lo, self.res
@@ -241,12 +247,16 @@ class ClosedLoop:
         return strehl_meter(self.long_exposure_psf(), self.psf_ref)
 
     def _launch_step(self):
-        st = N.stream_handle()
+        """One step.  With the infinite-screen Atmosphere, the next step's
+        turbulence, this step's pupil RMS and the optional science PSF run on
+        a side stream while the sensor runs; the integrator (which advances
+        the step counter) waits for them."""
+        main = torch.cuda.current_stream()
+        st = N.stream_handle(main)
         dm, wfs = self.dm, self.wfs
         base = None
         if self._atm is not None:
-            self._atm._launch(advance=True)
-            base = self._atm_opd
+            base = self._atm_opd                 # prepared by the previous step (or reset)
         elif self.layers is not None:
             N.call('oopao_cl_screen', len(self._scr), self._scr_ptr, self._h, self._w, self._y0, self._x0,
                    self._vy, self._vx, self.res, self.step_counter, self.opd_atm, st)
@@ -257,10 +267,20 @@ class ClosedLoop:
         else:
             N.call('oopao_dm_opd_acc_f32', dm._modes_t, self.coefs, dm.nValidAct, self.res * self.res, 1, 1.0,
                    base, self.opd, st)
-        N.call('oopao_cl_pupil_rms', self.opd, self.pupil_idx, self.pupil_idx.numel(), self.step_counter,
-               self.wfe, self.max_steps, st)
-        if self.science:
-            self._science()
+        fork = torch.cuda.Event()
+        fork.record(main)
+        side = self._side
+        side.wait_event(fork)
+        with torch.cuda.stream(side):
+            ss = N.stream_handle(side)
+            if self._atm is not None:
+                self._atm._launch(advance=True, stream=side)
+            N.call('oopao_cl_pupil_rms', self.opd, self.pupil_idx, self.pupil_idx.numel(), self.step_counter,
+                   self.wfe, self.max_steps, ss)
+            if self.science:
+                self._science()
+        join = torch.cuda.Event()
+        join.record(side)
         if self.gsc is not None:
             # frame + full-resolution focal-plane camera, then the optical gains
             N.call('oopao_pwfs_measure_focal', self.plan.h, self.opd, self.scale, 1, self.frame, None, self.focal,
@@ -271,6 +291,7 @@ class ClosedLoop:
             N.call('oopao_pwfs_measure', self.plan.h, self.opd, self.scale, 1, self.frame, None, self.ws,
                    self.ws_bytes, st)
         N.call('oopao_pwfs_signal', self.plan.h, self.frame, 1, self.s2d, self.s, None, st)
+        main.wait_event(join)
         if self.gsc is not None:
             s_in = self.s if self.frame_delay == 1 else self.s_prev
             N.call('oopao_cl_modal', self.M, s_in, self.M.shape[0], self.M.shape[1], self.og, self.og_start,

@@ -83,8 +83,10 @@ def test_graph_replay_equals_eager_and_horizon_guard():
     torch.cuda.synchronize()
     opd_graph = atm.OPD.copy()
     wfe_graph = cl.residual_wfe.copy()
+    # step t of the loop sees the atmosphere after t + 1 updates, and each
+    # step prepares the next one's: after n steps it has been updated n + 1 times
     atm.reset_state()
-    for _ in range(n):
+    for _ in range(n + 1):
         atm.update()
     np.testing.assert_array_equal(atm.OPD, opd_graph)
     assert atm.status() == 0
