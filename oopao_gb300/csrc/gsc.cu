@@ -32,7 +32,8 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kSumThreads = 1024;
-constexpr int kModeGroup = 8;        // modes per contraction CTA
+constexpr int kModeGroup = 8;        // modes per contraction CTA, one frame per CTA
+constexpr int kModeGroupBatch = 4;   // modes per contraction CTA, four frames per CTA
 constexpr int kMaxChunks = 64;       // pixel chunks of the contraction
 constexpr size_t kSmemBudget = 96 * 1024;
 
@@ -260,14 +261,13 @@ __global__ void __launch_bounds__(kSumThreads) gsc_mode_power(const float* __res
 }
 
 // part[chunk][b][m] = sum over the chunk's pixels p of v[b][p] * bp[m][p]
-// (complex v, real bp).  A CTA covers BT frames, kModeGroup modes and one
+// (complex v, real bp).  A CTA covers BT frames, MG modes and one
 // pixel chunk; a thread handles 4 consecutive pixels per step (float4 loads).
 // Out-of-range modes and frames are clamped on load and dropped on store.
-template <int BT>
-__global__ void __launch_bounds__(kThreads, 2) gsc_contract(const float* __restrict__ bp, const float2* __restrict__ v,
+template <int BT, int MG>
+__global__ void __launch_bounds__(kThreads, BT == 4 ? 3 : 2) gsc_contract(const float* __restrict__ bp, const float2* __restrict__ v,
                                                          int n_modes, int n2, int batch, int chunk,
                                                          float2* __restrict__ part) {
-  constexpr int MG = kModeGroup;
   const int b0 = blockIdx.x * BT;  // frame groups vary fastest: CTAs that read
   const int m0 = blockIdx.y * MG;  // the same basis-product rows run together
   const int p0 = blockIdx.z * chunk;
@@ -508,17 +508,17 @@ int pick_chunks(int ctas_per_chunk, int slots) {
 void contract(const oopao_gsc_plan* P, const float2* v, int batch, float2* part, bool calibrating, double2* s_out,
               double* og, cudaStream_t st) {
   const int n2 = P->n * P->n;
-  const int groups = ceil_div(P->n_modes, kModeGroup);
   const int bt = batch >= 4 ? 4 : 1;
+  const int groups = ceil_div(P->n_modes, bt == 4 ? kModeGroupBatch : kModeGroup);
   const int zg = ceil_div(batch, bt);
   int chunks = pick_chunks(groups * zg, P->contract_slots[bt == 4 ? 1 : 0]);
   const int chunk = ceil_div(ceil_div(n2, chunks), 4) * 4;
   chunks = ceil_div(n2, chunk);
   const dim3 g((unsigned)zg, (unsigned)groups, (unsigned)chunks);
   if (bt == 4)
-    gsc_contract<4><<<g, kThreads, 0, st>>>(P->bp, v, P->n_modes, n2, batch, chunk, part);
+    gsc_contract<4, kModeGroupBatch><<<g, kThreads, 0, st>>>(P->bp, v, P->n_modes, n2, batch, chunk, part);
   else
-    gsc_contract<1><<<g, kThreads, 0, st>>>(P->bp, v, P->n_modes, n2, batch, chunk, part);
+    gsc_contract<1, kModeGroup><<<g, kThreads, 0, st>>>(P->bp, v, P->n_modes, n2, batch, chunk, part);
   gsc_finish<<<ceil_div(batch * P->n_modes, 256), 256, 0, st>>>(part, chunks, batch, P->n_modes, P->mode_norm,
                                                               P->s_ref, P->s_inv, calibrating ? nullptr : P->s_inv,
                                                               s_out, og);
@@ -565,8 +565,8 @@ extern "C" int oopao_gsc_plan_create(oopao_gsc_plan** plan, int n, int n_modes, 
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&P->n_sm, cudaDevAttrMultiProcessorCount, dev);
   int occ1 = 1, occ4 = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ1, gsc_contract<1>, kThreads, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ4, gsc_contract<4>, kThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ1, gsc_contract<1, kModeGroup>, kThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ4, gsc_contract<4, kModeGroupBatch>, kThreads, 0);
   P->contract_slots[0] = (occ1 < 1 ? 1 : occ1) * P->n_sm;
   P->contract_slots[1] = (occ4 < 1 ? 1 : occ4) * P->n_sm;
   const size_t nn = (size_t)n * n;
