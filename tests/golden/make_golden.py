@@ -293,6 +293,37 @@ def case_kl(OOPAO, name, res, n_subap, r0=0.15, L0=25.0):
     print(name, 'M2C', rec['m2c'].shape)
 
 
+POSTPROCESSING_MODES = ['slopesMaps', 'slopesMaps_incidence_flux', 'slopesMaps_camera_flux', 'fullFrame_camera_flux',
+                        'fullFrame_incidence_flux', 'fullFrame_sum_flux', 'fullFrame']
+
+
+def case_modes(OOPAO, name='modes_tiny', res=24, n_subap=4, modulation=3, light_ratio=0.5, seed=5):
+    """Every postProcessing normalisation of signalProcessing (OOPAO/Pyramid.py
+    :835-926) on one DM shape, plus the detector binning (binning=2, the
+    Pyramid.__mul__ rebin, :1195-1201) with slopesMaps."""
+    import json
+    rng = np.random.default_rng(seed)
+    rec = {}
+    coefs = None
+    for mode in POSTPROCESSING_MODES + ['binning2']:
+        kw = dict(binning=2) if mode == 'binning2' else dict(postProcessing=mode)
+        tel, ngs, dm, wfs = build(OOPAO, res, n_subap, modulation, light_ratio, **kw)
+        if coefs is None:
+            coefs = rng.standard_normal(dm.nValidAct) * 60e-9
+        with _quiet():
+            dm.coefs = coefs
+            ngs ** tel * dm * wfs
+        rec[mode + '_signal'] = np.array(wfs.signal)
+        rec[mode + '_signal_2D'] = np.array(wfs.signal_2D)
+        rec[mode + '_frame'] = np.array(wfs.cam.frame)
+        rec[mode + '_n_signal'] = wfs.nSignal
+    rec['coefs'] = coefs
+    rec['params'] = json.dumps(dict(res=res, n_subap=n_subap, modulation=modulation, light_ratio=light_ratio,
+                                    modes=POSTPROCESSING_MODES))
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **rec)
+    print(name, [(m, int(rec[m + '_n_signal'])) for m in POSTPROCESSING_MODES + ['binning2']])
+
+
 GSC_CASES = [('gsc_tiny', dict(res=24, n_subap=4, modulation=3, n_modes=12)),
              ('gsc_small', dict(res=40, n_subap=10, modulation=2, n_modes=40))]
 
@@ -373,6 +404,8 @@ def main():
     for name, kw in GSC_CASES:
         if not only or name in only:
             case_gsc(OOPAO, name, **kw)
+    if not only or 'modes_tiny' in only:
+        case_modes(OOPAO)
     if not only or any(n in only for n, _ in KL_CASES):
         from refimport import install_kl_shims
         install_kl_shims()
