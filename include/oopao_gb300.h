@@ -73,7 +73,9 @@ int oopao_pwfs_set_amplitude(oopao_pwfs_plan* plan, const float* amp_host);
 int oopao_pwfs_set_masks(oopao_pwfs_plan* plan, int n_masks, const float* masks_host);
 int oopao_pwfs_n_masks(const oopao_pwfs_plan* plan);
 /* Optional per-point weights [n_theta] (Pyramid.weight_vector, :750-755);
- * NULL restores the plain sum. */
+ * NULL restores the plain sum.  The device copy stays allocated until the
+ * plan is destroyed, so a captured graph may keep its address; switching
+ * the weights off or on does not free or move it. */
 int oopao_pwfs_set_weights(oopao_pwfs_plan* plan, const float* weights_host);
 /* Launch shape (autotuner hook, no reference counterpart): lines per CTA of
  * the generic FFT passes (0 keeps a value) and the number of partial sums

@@ -30,8 +30,14 @@ def _scale(wfs):
     return 2 * np.pi / wfs.src.wavelength
 
 
+def _plan(wfs):
+    """The sensor's plan as the interaction matrix sees it: a batch
+    measurement, whose sum over modulation points is unweighted."""
+    return wfs._weighted_plan(False) if hasattr(wfs, '_weighted_plan') else wfs.plan
+
+
 def _ws(wfs, batch, ad=True):
-    plan = wfs.plan
+    plan = _plan(wfs)
     nb = N.load().oopao_pwfs_ad_workspace_bytes(plan.h, batch) if ad else plan.workspace_bytes(batch)
     return wfs._ws.get(nb), nb
 
@@ -46,7 +52,7 @@ def frames(wfs, opd, scale=None):
 def frame_jvp(wfs, opd0, dopd, scale=None):
     """Tangent of the camera frames at opd0 ([1 or B, res, res]) along dopd [B, res, res]."""
     scale = _scale(wfs) if scale is None else scale
-    plan = wfs.plan
+    plan = _plan(wfs)
     dopd = dopd.contiguous()
     opd0 = opd0.contiguous()
     B = dopd.shape[0]
@@ -61,7 +67,7 @@ def frame_jvp(wfs, opd0, dopd, scale=None):
 def frame_vjp(wfs, opd, fbar, scale=None):
     """Adjoint of the camera frames at opd [B, res, res] applied to fbar [B, cam, cam]."""
     scale = _scale(wfs) if scale is None else scale
-    plan = wfs.plan
+    plan = _plan(wfs)
     opd = opd.contiguous()
     fbar = fbar.contiguous()
     B = opd.shape[0]
@@ -73,7 +79,7 @@ def frame_vjp(wfs, opd, fbar, scale=None):
 
 
 def signal_jvp(wfs, frame0, dframe):
-    plan = wfs.plan
+    plan = _plan(wfs)
     if not getattr(wfs, '_signal_configured', False):
         wfs._configure_signal(plan)
     frame0 = frame0.contiguous()
@@ -89,7 +95,7 @@ def signal_jvp(wfs, frame0, dframe):
 
 
 def signal_vjp(wfs, frame0, sbar):
-    plan = wfs.plan
+    plan = _plan(wfs)
     if not getattr(wfs, '_signal_configured', False):
         wfs._configure_signal(plan)
     frame0 = frame0.contiguous()
@@ -183,7 +189,7 @@ def jvp_interaction_matrix(ngs, tel, dm, wfs, M2C, phase_offset=None, chunk=256)
     if phase_offset is not None:
         opd0 = torch.as_tensor(np.asarray(phase_offset) / scale, dtype=torch.float32, device=dev)[None]
     ngs ** tel
-    wfs.plan.set_amplitude(ngs.intensity, wfs._amplitude_key())
+    _plan(wfs).set_amplitude(ngs.intensity, wfs._amplitude_key())
     frame0 = frames(wfs, opd0)
     m2c = torch.as_tensor(np.ascontiguousarray(M2C, dtype=np.float32), device=dev)
     cols = []

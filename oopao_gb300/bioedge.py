@@ -153,16 +153,76 @@ class BioEdge:
                 self._plans, self._shared_forward = [p0], True
             except OopaoError:
                 self._plans, self._shared_forward = [p0] + [mk(m) for m in self.mask[1:]], False
-            if self.weight_vector is not None:
-                w = N.host(np.asarray(self.weight_vector, dtype=np.float64) / self.nTheta, np.float32)
-                for p in self._plans:
-                    N.call('oopao_pwfs_set_weights', p.h, w)
             self._signal_configured = False
         return self._plans
 
     @property
     def plan(self):
         return self.plans[0]
+
+    def _weighted_plans(self, single):
+        """The plans with the weights of a single-wavefront (True) or a batch
+        (False) measurement in place (BioEdge.py:643-648 weights one 2-D
+        phase only)."""
+        plans = self.plans
+        w = self._weight_vector
+        for p in plans:
+            p.set_weights(w / self.nTheta if single and w is not None else None)
+        return plans
+
+    @property
+    def weight_vector(self):
+        return self._weight_vector
+
+    @weight_vector.setter
+    def weight_vector(self, val):
+        self._weight_vector = None if val is None else np.asarray(val, dtype=np.float64).ravel()
+
+    @property
+    def mask(self):
+        return self._mask
+
+    @mask.setter
+    def mask(self, val):
+        """The four complex masks; a new list takes effect at the next
+        measurement."""
+        self._mask = val
+        self._plans = None
+
+    def apply_shift_wfs(self, sx=None, sy=None, mis_reg=None, units='pixels'):
+        """Moves the four pupil images by a tip/tilt on each mask
+        (BioEdge.py:394-433).  As in the reference, the masks are rebuilt
+        from sx, sy as given (one value or four); units only scales the
+        shifts recorded in self.sx / self.sy and the range warning.  The
+        reference slopes are measured again."""
+        sx = 0 if sx is None else sx
+        sy = 0 if sy is None else sy
+        if mis_reg is not None:
+            sx = [mis_reg.dX_1, mis_reg.dX_2, mis_reg.dX_3, mis_reg.dX_4]
+            sy = [mis_reg.dY_1, mis_reg.dY_2, mis_reg.dY_3, mis_reg.dY_4]
+        f = 2
+        if units == 'pixels':
+            factor = f
+        elif units == 'm':
+            factor = f / (self.telescope.D / self.nSubap)
+        else:
+            raise OopaoError("units must be 'pixels' or 'm'")
+        if np.isscalar(sx) and np.isscalar(sy):
+            shift_x, shift_y = [factor * sx] * 4, [factor * sy] * 4
+        elif len(sx) == 4 and len(sy) == 4:
+            shift_x, shift_y = [factor * v for v in sx], [factor * v for v in sy]
+        else:
+            raise OopaoError('Wrong size for sx and/or sy, a list of 4 values is expected.')
+        if np.max(np.abs(shift_x) / factor) > self.n_pix_edge or np.max(np.abs(shift_y) / factor) > self.n_pix_edge:
+            warning('The Bi-O Edge pupils have been shifted outside of the detector!'
+                    'Wrapping of the signal is currently occuring!!')
+        self.mask_computation(sx=sx, sy=sy)
+        self.sx = np.asarray(shift_x) / factor
+        self.sy = np.asarray(shift_y) / factor
+        self.slopesUnits = 1
+        self.referenceSignal = 0
+        self.referenceSignal_2D = 0
+        self.wfs_calibration()
 
     # ------------------------------------------------------------------ modulation (BioEdge.py:963-1009)
     @property
@@ -199,6 +259,28 @@ class BioEdge:
             self.wfs_calibration()
 
     @property
+    def delta_Tip(self):
+        return self._delta_Tip
+
+    @delta_Tip.setter
+    def delta_Tip(self, val):
+        """Offset of the modulation circle along x (BioEdge.py:933-941); a
+        calibrated sensor rebuilds its path and reference slopes."""
+        self._delta_Tip = val
+        if self.isCalibrated:
+            self.modulation = self.modulation
+
+    @property
+    def delta_Tilt(self):
+        return self._delta_Tilt
+
+    @delta_Tilt.setter
+    def delta_Tilt(self, val):
+        self._delta_Tilt = val
+        if self.isCalibrated:
+            self.modulation = self.modulation
+
+    @property
     def lightRatio(self):
         return self._lightRatio
 
@@ -220,7 +302,7 @@ class BioEdge:
         x = opd_dev if opd_dev.ndim == 3 else opd_dev[None]
         x = x.contiguous()
         B, cam, n = x.shape[0], self._cam_eff, self.resolution
-        plans = self.plans
+        plans = self._weighted_plans(opd_dev.ndim == 2)
         if self._shared_forward:
             # one launch sequence; tiles [B][4][.][.] laid out 2 x 2
             plan = plans[0]

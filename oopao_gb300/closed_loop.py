@@ -161,7 +161,8 @@ class ClosedLoop:
         self.scale = 2 * np.pi / ngs.wavelength
         # static configuration: amplitude, signal processing, workspace
         ngs ** tel
-        plan = wfs.plan
+        # one wavefront per step: the weights of a single measurement apply
+        plan = wfs._weighted_plan(True) if hasattr(wfs, '_weighted_plan') else wfs.plan
         plan.set_amplitude(ngs.intensity, wfs._amplitude_key())
         wfs._configure_signal(plan)
         self.plan = plan

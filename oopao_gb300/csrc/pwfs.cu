@@ -91,7 +91,8 @@ struct oopao_pwfs_plan {
   float2* d_mask_conj;
   float2* d_ones;
   float* d_amp;      // [res*res]
-  float* d_weights;  // [k] or null
+  float* d_weights;  // [k] or null; allocated once, freed with the plan
+  bool weights_on;   // launches read d_weights (else the plain sum)
   // launch shape
   int rows_per_cta, cols_per_cta, inv_rows_per_cta;
   int ksplit;        // partial slots over modulation points (divides k; 0 = automatic)
@@ -112,6 +113,8 @@ struct oopao_pwfs_plan {
   int* d_sig_index;
   int* d_sig_inv;  // [n2d] signal entry of each 2-D map cell, or -1
 };
+
+static const float* weights_of(const oopao_pwfs_plan* p) { return p->weights_on ? p->d_weights : nullptr; }
 
 // ---------------------------------------------------------------------------
 // Kernels
@@ -747,13 +750,15 @@ extern "C" int oopao_pwfs_n_masks(const oopao_pwfs_plan* p) { return p ? p->n_ma
 
 extern "C" int oopao_pwfs_set_weights(oopao_pwfs_plan* p, const float* w) {
   OOPAO_CHECK_ARG(p, "NULL plan");
+  // The buffer outlives every switch: a graph captured with the weights on
+  // keeps its address.
   if (!w) {
-    cudaFree(p->d_weights);
-    p->d_weights = nullptr;
+    p->weights_on = false;
     return OOPAO_OK;
   }
   if (!p->d_weights) OOPAO_CUDA_TRY(cudaMalloc((void**)&p->d_weights, sizeof(float) * p->k));
   OOPAO_CUDA_TRY(cudaMemcpy(p->d_weights, w, sizeof(float) * p->k, cudaMemcpyHostToDevice));
+  p->weights_on = true;
   return OOPAO_OK;
 }
 
@@ -976,7 +981,7 @@ int measure_impl(const oopao_pwfs_plan* p, const float* opd, double phase_scale,
         pwfs_cols<<<g2, kThreads, rows_smem(n, p->cols_per_cta), st>>>(ca);
       }
       mark(1);
-      RowsInvArgs ia{p->fft, p->d_tw, z, p->d_weights, pp.fused ? nullptr : part, pp.fused ? part : nullptr,
+      RowsInvArgs ia{p->fft, p->d_tw, z, weights_of(p), pp.fused ? nullptr : part, pp.fused ? part : nullptr,
                      n, k0, kc, k0 / pp.slot_pts, pp.slot_pts, pp.ksplit, p->inv_rows_per_cta, p->bin, cam};
       mark(2);
       if (f) {
@@ -1445,7 +1450,7 @@ extern "C" int oopao_pwfs_jvp(const oopao_pwfs_plan* p, const float* opd0, int o
     pwfs_field_tangent<<<dim3(ceil_div(res * res, 256), nb), 256, 0, st>>>(
         o0, dopd + (size_t)b0 * res * res, (float)phase_scale, p->d_amp, fld, res * res, 0);
     forward_to_z(fld, nb);
-    AdJvpArgs ja{p->d_tw, z, g, p->d_weights, part, 0, k, 0, slot_pts, ks, p->bin, cam};
+    AdJvpArgs ja{p->d_tw, z, g, weights_of(p), part, 0, k, 0, slot_pts, ks, p->bin, cam};
     ad->jvp<<<dim3(ceil_div(n, ad->l), ks, nb), ad->t * ad->l, ad->smem_jvp, st>>>(ja);
     pwfs_reduce_binned<<<dim3(ceil_div(cam * cam, 256), nb), 256, 0, st>>>(part, dframe + (size_t)b0 * cam * cam,
                                                                            cam * cam, ks);
@@ -1493,7 +1498,7 @@ extern "C" int oopao_pwfs_vjp(const oopao_pwfs_plan* p, const float* opd, const 
     ColsArgs ca{p->fft, p->d_tw, p->d_mask, y, p->d_group, p->d_colfac, z, res, n, 0, k, p->ngroups, p->off, 0};
     f->cols<<<dim3(ceil_div(n, f->l_cols), k, nb), f->t * f->l_cols, f->smem_cols, st>>>(ca);
     // Gbar and its row FFT, in place over z
-    AdVjpAArgs va{p->d_tw, z, z, fbar + (size_t)b0 * cam * cam, p->d_weights, 0, k, p->bin, cam};
+    AdVjpAArgs va{p->d_tw, z, z, fbar + (size_t)b0 * cam * cam, weights_of(p), 0, k, p->bin, cam};
     ad->vjp_a<<<dim3(ceil_div(n, ad->l), k, nb), ad->t * ad->l, ad->smem_vjp_a, st>>>(va);
     // column FFT, conj(mask), column IFFT over full columns, in place
     ColsArgs cb{p->fft, p->d_tw, p->d_mask_conj, z, nullptr, p->d_ones, z, n, n, 0, k, k, 0, 0};

@@ -37,6 +37,7 @@ class _Plan:
                float(tt_scale), int(bool(psf_centering)))
         self.h = h
         self._amp_key = None
+        self._weights = None
 
     def __del__(self):
         try:
@@ -52,6 +53,20 @@ class _Plan:
         amp = N.host(np.sqrt(np.asarray(intensity, dtype=np.float64) / self.k), np.float32)
         N.call('oopao_pwfs_set_amplitude', self.h, amp)
         self._amp_key = key
+
+    def set_weights(self, w):
+        """Per-point factors of the sum over modulation points (None: the
+        plain sum); uploaded only when they change."""
+        if w is None and self._weights is None:
+            return
+        if w is not None:
+            w = np.asarray(w, dtype=np.float64).ravel()
+            if w.size != self.k:
+                raise OopaoError('weight_vector has %d entries for %d modulation points' % (w.size, self.k))
+            if self._weights is not None and np.array_equal(w, self._weights):
+                return
+        N.call('oopao_pwfs_set_weights', self.h, None if w is None else N.host(w, np.float32))
+        self._weights = w
 
     def workspace_bytes(self, batch):
         return N.load().oopao_pwfs_workspace_bytes(self.h, batch)
@@ -219,6 +234,46 @@ class Pyramid:
         self.initial_mask = np.copy(self.mask)
         self._plan = None
 
+    def apply_shift_wfs(self, sx=None, sy=None, mis_reg=None, units='pixels'):
+        """Moves the four pupil images by tilting the faces of the mask
+        (OOPAO/Pyramid.py:400-451).  sx, sy: one shift for every face or four,
+        in detector pixels or, with units='m', in metres at the pupil; a
+        MisRegistration object gives them as dX_1..4 / dY_1..4.  The
+        quadrant-tilt mask of old_mask takes twice the value for the same
+        shift.  The new mask carries no spatial filter (initial_mask keeps the
+        unshifted one) and the reference slopes are measured again."""
+        sx = 0 if sx is None else sx
+        sy = 0 if sy is None else sy
+        if mis_reg is not None:
+            sx = [mis_reg.dX_1, mis_reg.dX_2, mis_reg.dX_3, mis_reg.dX_4]
+            sy = [mis_reg.dY_1, mis_reg.dY_2, mis_reg.dY_3, mis_reg.dY_4]
+        f = 2 if self.old_mask else 1
+        if units == 'pixels':
+            factor = f
+        elif units == 'm':
+            factor = f / (self.telescope.D / self.nSubap)
+        else:
+            raise OopaoError("units must be 'pixels' or 'm'")
+        if np.isscalar(sx) and np.isscalar(sy):
+            shift_x, shift_y = [factor * sx] * 4, [factor * sy] * 4
+        elif len(sx) == 4 and len(sy) == 4:
+            shift_x, shift_y = [factor * v for v in sx], [factor * v for v in sy]
+        else:
+            raise OopaoError('Wrong size for sx and/or sy, a list of 4 values is expected.')
+        if np.max(np.abs(shift_x)) > self.n_pix_edge or np.max(np.abs(shift_y)) > self.n_pix_edge:
+            warning('The Pyramid pupils have been shifted outside of the detector!'
+                    'Wrapping of the signal is currently occuring!!')
+        self.sx = np.asarray(shift_x) / factor
+        self.sy = np.asarray(shift_y) / factor
+        fn = self.get_phase_mask_old if self.old_mask else self.get_phase_mask
+        self.m = fn(resolution=self.resolution, n_subap=self.nSubap, n_pix_separation=self.n_pix_separation,
+                    n_pix_edge=self.n_pix_edge, psf_centering=self.psfCentering, sx=shift_x, sy=shift_y)
+        self.mask = np.complex64(np.exp(1j * self.m))
+        self.slopesUnits = 1
+        self.referenceSignal = 0
+        self.referenceSignal_2D = 0
+        self.wfs_calibration()
+
     @property
     def phasor(self):
         n = self.resolution
@@ -365,11 +420,39 @@ class Pyramid:
     def plan(self):
         if self._plan is None:
             self._plan = self._make_plan(self.modulation_path)
-            if self.weight_vector is not None:
-                w = N.host(np.asarray(self.weight_vector, dtype=np.float64) / self.nTheta, np.float32)
-                N.call('oopao_pwfs_set_weights', self._plan.h, w)
             self._signal_configured = False
         return self._plan
+
+    @property
+    def weight_vector(self):
+        return self._weight_vector
+
+    @weight_vector.setter
+    def weight_vector(self, val):
+        """Weights of the modulation points in the measurement of one
+        wavefront: raw = sum_k w_k I_k / nTheta (OOPAO/Pyramid.py:750-755).
+        As in the reference, a batch of wavefronts (its 3-D phase path, the
+        one the interaction matrix takes) sums the points unweighted."""
+        self._weight_vector = None if val is None else np.asarray(val, dtype=np.float64).ravel()
+
+    def _weighted_plan(self, single):
+        """The plan with the weights of a single-wavefront (True) or a batch
+        (False) measurement in place."""
+        plan = self.plan
+        w = self._weight_vector
+        plan.set_weights(w / self.nTheta if single and w is not None else None)
+        return plan
+
+    @property
+    def mask(self):
+        return self._mask
+
+    @mask.setter
+    def mask(self, val):
+        """The complex focal-plane mask; assigning a new one takes effect at
+        the next measurement, as the reference's attribute does."""
+        self._mask = val
+        self._plan = None
 
     # ------------------------------------------------------------------ geometry of quadrants
     def _quadrant_origins(self):
@@ -395,7 +478,7 @@ class Pyramid:
         return (id(self.src), self.src._intensity_version)
 
     def _measure_frames(self, opd_dev, scale, plan=None, want_raw=False, want_focal=False):
-        plan = plan or self.plan
+        plan = plan or self._weighted_plan(opd_dev.ndim == 2)
         if self.src.intensity is None:
             raise OopaoError('No flux: propagate the source through the telescope first (src**tel)')
         plan.set_amplitude(self.src.intensity, self._amplitude_key())

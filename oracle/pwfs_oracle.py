@@ -192,14 +192,68 @@ def phase_mask(res: int, n_subap: int, n_pix_separation: float, n_pix_edge: floa
     return -np.max(stacked, axis=0)
 
 
+def phase_mask_old(res: int, n_subap: int, n_pix_separation: float, n_pix_edge: float,
+                   psf_centering: bool, sx=(0, 0, 0, 0), sy=(0, 0, 0, 0)) -> np.ndarray:
+    """Quadrant tip/tilt pyramid phase (``old_mask``), ``OOPAO/Pyramid.py:482-539``.
+
+    Each quadrant holds a zero-mean plane ±tip·(s ± sx_q) ± tilt·(s ± sy_q),
+    s = n_subap + n_pix_separation, scaled by (res/n_subap)/4.  Centred on
+    four pixels the quadrants are n/2 square with grids linspace(-pi, pi,
+    n/2, endpoint=False); centred on one pixel they are n/2+1 or n/2-1 wide
+    (grids over ±pi with the endpoint, or ±(pi - 2pi/n) without), the later
+    quadrants overwriting the shared row and column in the order 1, 2, 3, 4.
+    """
+    n = int((n_subap * 2 + n_pix_separation + n_pix_edge * 2) * res / n_subap)
+    h = n // 2
+    s = n_subap + n_pix_separation
+    scale = res / n_subap / 4
+    m = np.zeros((n, n))
+
+    def grid(x_len, x_full, y_len, y_full):
+        # zero-mean tip (along x) and tilt (along y) planes of one quadrant
+        def axis(length, full):
+            if psf_centering:
+                return np.linspace(-np.pi, np.pi, length, endpoint=False)
+            if full:
+                return np.linspace(-np.pi, np.pi, length, endpoint=True)
+            lim = np.pi - 2 * np.pi / n
+            return np.linspace(-lim, lim, length, endpoint=False)
+        tip, tilt = np.meshgrid(axis(x_len, x_full), axis(y_len, y_full))
+        return tip - tip.mean(), tilt - tilt.mean()
+
+    if psf_centering:
+        g = grid(h, True, h, True)
+        quads = [((slice(0, h), slice(0, h)), g, (+1, +1, +1, -1)),
+                 ((slice(0, h), slice(n - h, n)), g, (-1, -1, +1, -1)),
+                 ((slice(n - h, n), slice(n - h, n)), g, (-1, -1, -1, +1)),
+                 ((slice(n - h, n), slice(0, h)), g, (+1, +1, -1, +1))]
+    else:
+        big, small = h + 1, h - 1
+        g1 = grid(big, True, big, True)
+        g2 = grid(big, True, small, False)
+        g3 = grid(small, False, small, False)
+        g4 = grid(small, False, big, True)
+        quads = [((slice(0, big), slice(0, big)), g1, (+1, +1, +1, -1)),
+                 ((slice(0, big), slice(n - small, n)), g4, (-1, -1, +1, -1)),
+                 ((slice(n - small, n), slice(n - small, n)), g3, (-1, -1, -1, +1)),
+                 ((slice(n - small, n), slice(0, big)), g2, (+1, +1, -1, +1))]
+    for q, ((rows, cols), (tip, tilt), (a, b, c, d)) in enumerate(quads):
+        # a*tip*(s + b*sx) + c*tilt*(s + d*sy)
+        m[rows, cols] = (a * tip * (s + b * sx[q]) + c * tilt * (s + d * sy[q])) * scale
+    return -m
+
+
 def pyramid_geometry(res: int, n_subap: int, n_pix_separation: float = 2,
                      n_pix_edge: float | None = None, psf_centering: bool = True,
                      rooftop: float = 0.0, theta_rotation: float = 0.0,
-                     initial_res: int | None = None) -> PyramidGeometry:
+                     initial_res: int | None = None, old_mask: bool = False,
+                     sx=(0, 0, 0, 0), sy=(0, 0, 0, 0)) -> PyramidGeometry:
     """FFT grid, camera size, tip/tilt grids, centring phasor and mask.
 
     ``OOPAO/Pyramid.py:276-285`` (N, zero padding, camera), ``:334-344``
-    (Tip/Tilt, phasor), ``:368-391`` (mask, complex64).
+    (Tip/Tilt, phasor), ``:368-391`` (mask, complex64; ``old_mask`` picks the
+    quadrant tip/tilt mask, sx/sy the face shifts as ``apply_shift_wfs``
+    hands them to the mask, ``:400-451``).
     """
     if n_pix_edge is None:
         n_pix_edge = n_pix_separation // 2
@@ -213,7 +267,10 @@ def pyramid_geometry(res: int, n_subap: int, n_pix_separation: float = 2,
     tip = tip * (res / initial_res)
     xx, yy = np.meshgrid(np.linspace(0, N - 1, N), np.linspace(0, N - 1, N))
     phasor = np.exp(-(1j * np.pi * (N + 1) / N) * (xx + yy))
-    m = phase_mask(res, n_subap, n_pix_separation, n_pix_edge, psf_centering, rooftop, theta_rotation)
+    if old_mask:
+        m = phase_mask_old(res, n_subap, n_pix_separation, n_pix_edge, psf_centering, sx, sy)
+    else:
+        m = phase_mask(res, n_subap, n_pix_separation, n_pix_edge, psf_centering, rooftop, theta_rotation, sx, sy)
     mask = np.complex64(np.exp(1j * m))
     return PyramidGeometry(res=res, n_subap=n_subap, n_pix_separation=n_pix_separation,
                            n_pix_edge=n_pix_edge, psf_centering=psf_centering, N=N, cam=cam,
@@ -460,7 +517,8 @@ def build_pyramid(res: int, n_subap: int, modulation: float, light_ratio: float,
                   n_pix_edge=None, psf_centering: bool = True, calib_modulation: float = 50.,
                   n_theta_user: int | None = None, extra: int = 0, delta_theta: float = 0.,
                   rooftop: float = 0., theta_rotation: float = 0., user_path=None,
-                  workers: int = 1, spatial_filter=None) -> OraclePyramid:
+                  workers: int = 1, spatial_filter=None, old_mask: bool = False,
+                  user_valid=None) -> OraclePyramid:
     """Construction sequence of ``Pyramid.__init__`` (``OOPAO/Pyramid.py:26-366``):
     geometry, calibration modulation clamp (``:292-296``), valid pixels at
     ``calibModulation`` (``initialization`` ``:541-589``), flat-wavefront
@@ -468,20 +526,24 @@ def build_pyramid(res: int, n_subap: int, modulation: float, light_ratio: float,
     ``spatial_filter``, the filter is then attached as the ``spatialFilter``
     setter does (``:1051-1085``): the mask is filtered and the reference
     slopes are measured again; the valid pixels stay those of the
-    unfiltered initialization."""
+    unfiltered initialization.  ``user_valid`` (``userValidSignal``,
+    slopes maps) replaces the flux selection (``:574-580``)."""
     geom = pyramid_geometry(res, n_subap, n_pix_separation, n_pix_edge, psf_centering,
-                            rooftop, theta_rotation)
+                            rooftop, theta_rotation, old_mask=old_mask)
     if calib_modulation >= res / 2:
         calib_modulation = res / 2 - 1
     flat = np.zeros((res, res))
     cpath, _ = modulation_path(calib_modulation, n_theta_user, extra, delta_theta, user_path=user_path)
     ctt = tt_buffers(cpath, geom)
-    if light_ratio == 0:
-        frame0 = np.ones((geom.cam, geom.cam))
+    if user_valid is not None:
+        valid = np.asarray(user_valid, dtype=bool)
     else:
-        raw0 = wfs_raw(flat, intensity, ctt, geom, workers=workers)
-        frame0 = camera_frame(raw0, geom)
-    valid, _ = valid_pixels(frame0, geom, light_ratio)
+        if light_ratio == 0:
+            frame0 = np.ones((geom.cam, geom.cam))
+        else:
+            raw0 = wfs_raw(flat, intensity, ctt, geom, workers=workers)
+            frame0 = camera_frame(raw0, geom)
+        valid, _ = valid_pixels(frame0, geom, light_ratio)
     path, n_theta = modulation_path(modulation, n_theta_user, extra, delta_theta, user_path=user_path)
     tt = tt_buffers(path, geom)
     if spatial_filter is not None:

@@ -324,6 +324,126 @@ def case_modes(OOPAO, name='modes_tiny', res=24, n_subap=4, modulation=3, light_
     print(name, [(m, int(rec[m + '_n_signal'])) for m in POSTPROCESSING_MODES + ['binning2']])
 
 
+# Constructor options and post-construction calls of the Pyramid and Bi-O Edge
+# operators: (name, sensor, constructor keywords, calls).  A call is
+# ('call', method, keywords) or ('set', attribute, value); the values
+# 'corner' (userValidSignal) and 'ramp' (weight_vector) are arrays the
+# generator and the test build the same way (options_array below).
+OPTION_CASES = [
+    ('old_mask', 'pyramid', dict(old_mask=True), []),
+    ('old_mask_nocenter', 'pyramid', dict(old_mask=True, psfCentering=False, modulation=2), []),
+    ('shift', 'pyramid', {}, [('call', 'apply_shift_wfs', dict(sx=[1, -1, 0.5, 0], sy=[0, 0.5, -1, 1]))]),
+    ('shift_old_metres', 'pyramid', dict(old_mask=True),
+     [('call', 'apply_shift_wfs', dict(sx=0.5, sy=-0.25, units='m'))]),
+    ('shift_nocenter', 'pyramid', dict(psfCentering=False),
+     [('call', 'apply_shift_wfs', dict(sx=[0.5, 0, -0.5, 1], sy=[1, -1, 0, 0.5]))]),
+    # a grid of points as in the reference's closed-loop tutorial, with the
+    # modulation radius non-zero (with modulation 0 the reference's
+    # single-wavefront path drops the source phase, Pyramid.py:617-618)
+    ('user_path', 'pyramid', dict(user_modulation_path=[[x, y] for x in (-2, 0, 2) for y in (-2, 0, 2)] + [[1, 0.5]]),
+     []),
+    ('delta_extra', 'pyramid', dict(delta_theta=0.3, extraModulationFactor=1), []),
+    ('user_valid', 'pyramid', dict(userValidSignal='corner'), []),
+    ('user_valid_fullframe', 'pyramid', dict(userValidSignal='corner', postProcessing='fullFrame'), []),
+    ('setters', 'pyramid', {}, [('set', 'modulation', 2), ('set', 'lightRatio', 0.2), ('set', 'delta_Tip', 0.5),
+                                ('set', 'delta_Tilt', -0.25)]),
+    ('weights', 'pyramid', {}, [('set', 'weight_vector', 'ramp')]),
+    ('bioedge_shift', 'bioedge', {}, [('call', 'apply_shift_wfs', dict(sx=[1, 0, -1, 0.5], sy=[0, 1, 0.5, -1]))]),
+    ('bioedge_path_tip', 'bioedge', dict(delta_theta=0.2, extraModulationFactor=1),
+     [('set', 'delta_Tip', 0.5), ('set', 'delta_Tilt', 0.25)]),
+]
+
+
+def options_array(tag, wfs=None, shape=None):
+    """The arrays named in OPTION_CASES: 'corner' is a user valid-pixel map
+    (every pixel but a 2-pixel corner block, of the valid-pixel map's shape),
+    'ramp' a weight per modulation point, 0.5 .. 1.5."""
+    if tag == 'corner':
+        v = np.ones(shape, dtype=bool)
+        v[0, 0] = False
+        v[1, 2] = False
+        return v
+    if tag == 'ramp':
+        return np.linspace(0.5, 1.5, wfs.nTheta)
+    raise ValueError(tag)
+
+
+def build_option_sensor(OOPAO, sensor, res, n_subap, modulation, light_ratio, kw):
+    """Telescope, source, DM and the sensor of one OPTION_CASES entry."""
+    from OOPAO.Telescope import Telescope
+    from OOPAO.Source import Source
+    from OOPAO.DeformableMirror import DeformableMirror
+    kw = dict(kw)
+    modulation = kw.pop('modulation', modulation)
+    with _quiet():
+        tel = Telescope(resolution=res, diameter=8.0, samplingTime=1e-3)
+        ngs = Source(optBand='V0', magnitude=8)
+        ngs * tel
+        dm = DeformableMirror(tel, nSubap=n_subap, mechCoupling=0.35)
+        if sensor == 'pyramid':
+            from OOPAO.Pyramid import Pyramid as cls
+        else:
+            from OOPAO.BioEdge import BioEdge as cls
+        if kw.get('userValidSignal') == 'corner':
+            # the valid-pixel map's shape: one quadrant (slopes maps) or the
+            # whole detector (full frame)
+            probe = cls(nSubap=n_subap, telescope=tel, modulation=modulation, lightRatio=light_ratio,
+                        postProcessing=kw.get('postProcessing', 'slopesMaps'))
+            shape = np.shape(probe.validI4Q if kw.get('postProcessing', 'slopesMaps')[:10] == 'slopesMaps'
+                             else probe.validSignal)
+            kw['userValidSignal'] = options_array('corner', shape=shape)
+        wfs = cls(nSubap=n_subap, telescope=tel, modulation=modulation, lightRatio=light_ratio, **kw)
+    return tel, ngs, dm, wfs
+
+
+def apply_option_calls(wfs, calls):
+    with _quiet():
+        for kind, name, val in calls:
+            if kind == 'call':
+                getattr(wfs, name)(**val)
+            else:
+                setattr(wfs, name, options_array(val, wfs) if isinstance(val, str) else val)
+
+
+def case_options(OOPAO, name='options_tiny', res=24, n_subap=4, modulation=3, light_ratio=0.5, seed=9):
+    """Constructor options (old_mask, psfCentering with the old mask,
+    user_modulation_path, delta_theta, extraModulationFactor, userValidSignal)
+    and post-construction calls (apply_shift_wfs in pixels and metres, the
+    modulation / lightRatio / delta_Tip / delta_Tilt setters, weight_vector) of
+    OOPAO/Pyramid.py and OOPAO/BioEdge.py, each with one DM shape and a batch
+    of two DM shapes (the reference's 3-D phase path)."""
+    import json
+    rng = np.random.default_rng(seed)
+    rec, coefs, coefs2 = {}, None, None
+    for case, sensor, kw, calls in OPTION_CASES:
+        tel, ngs, dm, wfs = build_option_sensor(OOPAO, sensor, res, n_subap, modulation, light_ratio, kw)
+        apply_option_calls(wfs, calls)
+        if coefs is None:
+            coefs = rng.standard_normal(dm.nValidAct) * 60e-9
+            coefs2 = rng.standard_normal((dm.nValidAct, 2)) * 60e-9
+        with _quiet():
+            dm.coefs = coefs
+            ngs ** tel * dm * wfs
+            rec[case + '_frame'] = np.array(wfs.cam.frame)
+            rec[case + '_signal'] = np.array(wfs.signal)
+            rec[case + '_signal_2D'] = np.array(wfs.signal_2D)
+            dm.coefs = coefs2
+            ngs ** tel * dm * wfs
+            rec[case + '_batch_signal'] = np.array(wfs.signal)
+        if 'userValidSignal' in kw:
+            rec[case + '_user_valid'] = np.array(wfs.userValidSignal)
+        rec[case + '_n_signal'] = int(wfs.nSignal)
+        rec[case + '_n_theta'] = int(wfs.nTheta)
+        rec[case + '_reference_2D'] = np.array(wfs.referenceSignal_2D)
+        if wfs.modulation != 0 or wfs.user_modulation_path is not None:
+            rec[case + '_modulation_path'] = np.array(wfs.modulation_path, dtype=np.float64)
+    rec['coefs'], rec['coefs2'] = coefs, coefs2
+    rec['params'] = json.dumps(dict(res=res, n_subap=n_subap, modulation=modulation, light_ratio=light_ratio,
+                                    cases=OPTION_CASES))
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **rec)
+    print(name, [(c, int(rec[c + '_n_signal']), int(rec[c + '_n_theta'])) for c, *_ in OPTION_CASES])
+
+
 GSC_CASES = [('gsc_tiny', dict(res=24, n_subap=4, modulation=3, n_modes=12)),
              ('gsc_small', dict(res=40, n_subap=10, modulation=2, n_modes=40))]
 
@@ -406,6 +526,8 @@ def main():
             case_gsc(OOPAO, name, **kw)
     if not only or 'modes_tiny' in only:
         case_modes(OOPAO)
+    if not only or 'options_tiny' in only:
+        case_options(OOPAO)
     if not only or any(n in only for n, _ in KL_CASES):
         from refimport import install_kl_shims
         install_kl_shims()
