@@ -18,6 +18,7 @@ from .source import Source
 from .telescope import Telescope
 from .detector import Detector
 from .deformable_mirror import DeformableMirror
+from .mis_registration import MisRegistration
 from .pyramid import Pyramid
 from .calibration import InteractionMatrix, CalibrationVault
 from .atmosphere import Atmosphere
@@ -25,4 +26,5 @@ from .bioedge import BioEdge
 from .gain_sensing import GainSensingCamera
 
 __all__ = ['OopaoError', 'warning', 'Source', 'Telescope', 'Detector', 'DeformableMirror', 'Pyramid',
-           'InteractionMatrix', 'CalibrationVault', 'Atmosphere', 'BioEdge', 'GainSensingCamera']
+           'InteractionMatrix', 'CalibrationVault', 'Atmosphere', 'BioEdge', 'GainSensingCamera',
+           'MisRegistration']

@@ -3,7 +3,9 @@
 
 Construction builds the Gaussian influence functions on the host in float64
 exactly as the reference (Fried grid and radial actuator selection
-:306-340, ``modesComputation`` :572-600), or takes user ``modes``.  The IF
+:306-340, mis-registration of the grid :359-386, ``modesComputation``
+:572-600), or takes user ``modes`` (the grid is still mis-registered, the
+modes are not, as in the reference).  The IF
 matrix is then kept on the GPU, transposed ([n_act][n_pix]), and every
 ``dm.coefs = ...`` runs the projection OPD = modes @ coefs on the device
 through ``oopao_dm_opd_f32`` (FP32) or, with ``if_dtype='bf16'``, the
@@ -13,6 +15,7 @@ import numpy as np
 import torch
 
 from . import _native as N
+from .mis_registration import MisRegistration
 from .runtime import device
 from .tools import OopaoError, print_
 
@@ -27,8 +30,6 @@ class DeformableMirror:
             raise OopaoError('M4 influence functions are not supported by oopao_gb300')
         if altitude is not None:
             raise OopaoError('Altitude-conjugated DMs are not supported by oopao_gb300')
-        if misReg is not None:
-            raise OopaoError('Mis-registered DMs are not supported by oopao_gb300 (pass modes=)')
         if mechCoupling <= 0:
             raise OopaoError('The value of mechanical coupling should be positive.')
         self.telescope = telescope
@@ -47,6 +48,7 @@ class DeformableMirror:
         self.precision = np.float64
         self.pitch = self.D / nSubap if pitch is None else pitch
         self.if_dtype = if_dtype
+        self.misReg = MisRegistration() if misReg is None else misReg
         if coordinates is None:
             self.nAct = nSubap + 1
             self.nActAlongDiameter = self.nAct - 1
@@ -78,9 +80,17 @@ class DeformableMirror:
             self.nActAlongDiameter = self.D / self.pitch
             self.validAct = np.arange(self.nAct)
             self.nValidAct = self.nAct
-        xIF = self.xIF0[self.validAct]
-        yIF = self.yIF0[self.validAct]
-        self.nIF = len(xIF)
+        xIF0 = self.xIF0[self.validAct]
+        yIF0 = self.yIF0[self.validAct]
+        self.nIF = len(xIF0)
+        self.initial_coordinates = np.stack([xIF0, yIF0], axis=1)
+        # mis-registration of the grid (:359-386): anamorphosis, rotation, shift
+        mr = self.misReg
+        x3, y3 = self.anamorphosis_coordinates(xIF0, yIF0, mr.anamorphosisAngle * np.pi / 180,
+                                               mr.tangentialScaling, mr.radialScaling)
+        x4, y4 = self.rotate_coordinates(x3, y3, mr.rotationAngle * np.pi / 180)
+        xIF = x4 - mr.shiftX
+        yIF = y4 - mr.shiftY
         self.coordinates = np.stack([xIF, yIF], axis=1)
         self.xIF, self.yIF = xIF, yIF
         if modes is None:
@@ -113,12 +123,32 @@ class DeformableMirror:
         print_(self, print_dm_properties)
 
     # ------------------------------------------------------------ IF build
+    @staticmethod
+    def rotate_coordinates(x, y, angle):
+        """Rotation of the actuator grid by `angle` radians (:559-562)."""
+        return x * np.cos(angle) - y * np.sin(angle), y * np.cos(angle) + x * np.sin(angle)
+
+    @staticmethod
+    def anamorphosis_coordinates(x, y, angle, mRad, mNorm):
+        """Stretch of the grid by 1+mRad along direction `angle` and 1+mNorm
+        across it (:564-570).  The reference passes the tangential scaling as
+        mRad and the radial one as mNorm; the same order is kept."""
+        mRad = mRad + 1
+        mNorm = mNorm + 1
+        s2 = np.sin(2 * angle) / 2
+        x_out = x * (mRad * np.cos(angle) ** 2 + mNorm * np.sin(angle) ** 2) + y * (mNorm * s2 - mRad * s2)
+        y_out = y * (mRad * np.sin(angle) ** 2 + mNorm * np.cos(angle) ** 2) + x * (mNorm * s2 - mRad * s2)
+        return x_out, y_out
+
     def _gaussian_modes(self, u0x, u0y):
-        """``modesComputation`` (OOPAO/DeformableMirror.py:572-600), zero mis-registration."""
+        """``modesComputation`` (OOPAO/DeformableMirror.py:572-600): Gaussian
+        IFs whose widths are scaled by 1+radialScaling along the anamorphosis
+        direction and 1+tangentialScaling across it."""
         res = self.resolution
-        cx = (self.resolution / self.nActAlongDiameter) / np.sqrt(2 * np.log(1. / self.mechCoupling))
-        cy = cx
-        theta = 0.0
+        w = (self.resolution / self.nActAlongDiameter) / np.sqrt(2 * np.log(1. / self.mechCoupling))
+        cx = (1 + self.misReg.radialScaling) * w
+        cy = (1 + self.misReg.tangentialScaling) * w
+        theta = self.misReg.anamorphosisAngle * np.pi / 180
         x = np.linspace(0, 1, res) * res
         X, Y = np.meshgrid(x, x)
         a = np.cos(theta) ** 2 / (2 * cx ** 2) + np.sin(theta) ** 2 / (2 * cy ** 2)

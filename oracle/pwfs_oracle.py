@@ -78,13 +78,27 @@ def source_intensity(pupil: np.ndarray, nphoton: float, sampling_time: float,
 # Deformable mirror
 # ---------------------------------------------------------------------------
 
+MISREG_FIELDS = ('rotationAngle', 'shiftX', 'shiftY', 'anamorphosisAngle', 'tangentialScaling', 'radialScaling')
+
+
+def _misreg(misreg):
+    m = dict.fromkeys(MISREG_FIELDS, 0.0)
+    m.update(misreg or {})
+    return m
+
+
 def dm_actuator_pixels(res: int, diameter: float, n_subap: int,
-                       central_obstruction: float = 0.0):
+                       central_obstruction: float = 0.0, misreg=None):
     """Fried-geometry actuator grid and radial selection, then pixel centres.
 
     ``OOPAO/DeformableMirror.py:306-340`` (grid, r_in/r_out selection) and
-    ``:366-386`` (identity mis-registration, pixel coordinates u0x/u0y).
+    ``:359-386`` (mis-registration, pixel coordinates u0x/u0y): the valid
+    actuators are stretched along the anamorphosis direction (``:564-570``,
+    by 1+tangentialScaling along it and 1+radialScaling across it, the
+    order in which the reference passes them), rotated (``:559-562``), then
+    shifted by -shiftX, -shiftY metres.
     """
+    mr = _misreg(misreg)
     pitch = diameter / n_subap
     n_act = n_subap + 1
     x = np.linspace(-diameter / 2, diameter / 2, n_act)
@@ -95,25 +109,36 @@ def dm_actuator_pixels(res: int, diameter: float, n_subap: int,
     r_in = central_obstruction * diameter / 2 - 0.5 * pitch
     r_out = diameter / 2 + 0.7533 * pitch
     valid = (r >= r_in) * (r <= r_out)
-    xIF = xIF0[valid]
-    yIF = yIF0[valid]
+    x0 = xIF0[valid]
+    y0 = yIF0[valid]
+    ang = mr['anamorphosisAngle'] * np.pi / 180
+    along, across = 1 + mr['tangentialScaling'], 1 + mr['radialScaling']
+    c2, s2, cs = np.cos(ang) ** 2, np.sin(ang) ** 2, np.sin(2 * ang) / 2
+    x3 = x0 * (along * c2 + across * s2) + y0 * (across - along) * cs
+    y3 = y0 * (along * s2 + across * c2) + x0 * (across - along) * cs
+    rot = mr['rotationAngle'] * np.pi / 180
+    xIF = x3 * np.cos(rot) - y3 * np.sin(rot) - mr['shiftX']
+    yIF = y3 * np.cos(rot) + x3 * np.sin(rot) - mr['shiftY']
     u0x = res / 2 + xIF * res / diameter
     u0y = res / 2 + yIF * res / diameter
     return u0x, u0y, valid
 
 
 def dm_modes(res: int, diameter: float, n_subap: int, mech_coupling: float = 0.35,
-             central_obstruction: float = 0.0) -> np.ndarray:
+             central_obstruction: float = 0.0, misreg=None) -> np.ndarray:
     """Gaussian influence functions [res*res, nAct] (row-major pixel index).
 
-    ``OOPAO/DeformableMirror.py:572-600`` (modesComputation with zero
-    mis-registration: theta=0, b=0) stacked as in ``:389-394``.
+    ``OOPAO/DeformableMirror.py:572-600`` (modesComputation: widths scaled by
+    1+radialScaling and 1+tangentialScaling, Gaussian axes along the
+    anamorphosis angle) stacked as in ``:389-394``.
     """
-    u0x, u0y, _ = dm_actuator_pixels(res, diameter, n_subap, central_obstruction)
+    mr = _misreg(misreg)
+    u0x, u0y, _ = dm_actuator_pixels(res, diameter, n_subap, central_obstruction, misreg)
     n_along = n_subap
-    cx = (res / n_along) / np.sqrt(2 * np.log(1. / mech_coupling))
-    cy = cx
-    theta = 0.0
+    w = (res / n_along) / np.sqrt(2 * np.log(1. / mech_coupling))
+    cx = (1 + mr['radialScaling']) * w
+    cy = (1 + mr['tangentialScaling']) * w
+    theta = mr['anamorphosisAngle'] * np.pi / 180
     xg = np.linspace(0, 1, res) * res
     X, Y = np.meshgrid(xg, xg)
     a = np.cos(theta) ** 2 / (2 * cx ** 2) + np.sin(theta) ** 2 / (2 * cy ** 2)

@@ -444,6 +444,40 @@ def case_options(OOPAO, name='options_tiny', res=24, n_subap=4, modulation=3, li
     print(name, [(c, int(rec[c + '_n_signal']), int(rec[c + '_n_theta'])) for c, *_ in OPTION_CASES])
 
 
+MISREG_CASES = {
+    'rot_shift': dict(rotationAngle=3.0, shiftX=0.12, shiftY=-0.07, anamorphosisAngle=0.0, tangentialScaling=0.0,
+                      radialScaling=0.0),
+    'anamorphosis': dict(rotationAngle=-1.5, shiftX=-0.05, shiftY=0.03, anamorphosisAngle=30.0,
+                         tangentialScaling=0.04, radialScaling=-0.03),
+}
+
+
+def case_misreg(OOPAO, name='misreg_tiny', res=24, n_subap=4, modulation=3, light_ratio=0.5, seed=11):
+    """DeformableMirror with a MisRegistration (OOPAO/DeformableMirror.py
+    :359-386, :559-600): actuator coordinates, influence functions and the
+    pyramid measurement of one DM shape through the mis-registered mirror."""
+    import json
+    from OOPAO.DeformableMirror import DeformableMirror
+    from OOPAO.MisRegistration import MisRegistration
+    tel, ngs, dm0, wfs = build(OOPAO, res, n_subap, modulation, light_ratio)
+    coefs = np.random.default_rng(seed).standard_normal(dm0.nValidAct) * 60e-9
+    rec = dict(coefs=coefs)
+    for tag, mr in MISREG_CASES.items():
+        with _quiet():
+            dm = DeformableMirror(tel, nSubap=n_subap, mechCoupling=0.35, misReg=MisRegistration(mr))
+            dm.coefs = coefs
+            ngs ** tel * dm * wfs
+        rec[tag + '_coordinates'] = np.array(dm.coordinates)
+        rec[tag + '_modes'] = np.array(dm.modes)
+        rec[tag + '_frame'] = np.array(wfs.cam.frame)
+        rec[tag + '_signal'] = np.array(wfs.signal)
+        rec[tag + '_name'] = MisRegistration(mr).misRegName
+    rec['params'] = json.dumps(dict(res=res, n_subap=n_subap, modulation=modulation, light_ratio=light_ratio,
+                                    misreg=MISREG_CASES))
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **rec)
+    print(name, {t: rec[t + '_modes'].shape for t in MISREG_CASES})
+
+
 GSC_CASES = [('gsc_tiny', dict(res=24, n_subap=4, modulation=3, n_modes=12)),
              ('gsc_small', dict(res=40, n_subap=10, modulation=2, n_modes=40))]
 
@@ -528,6 +562,8 @@ def main():
         case_modes(OOPAO)
     if not only or 'options_tiny' in only:
         case_options(OOPAO)
+    if not only or 'misreg_tiny' in only:
+        case_misreg(OOPAO)
     if not only or any(n in only for n, _ in KL_CASES):
         from refimport import install_kl_shims
         install_kl_shims()
