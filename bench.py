@@ -143,23 +143,34 @@ def cl_rate(n_steps=2000):
         atm = Atmosphere(telescope=tel, r0=0.12, L0=30, fractionalR0=[1 / 3, 1 / 3, 1 / 3],
                          windSpeed=[10., 15., 20.], windDirection=[0., 72., 144.], altitude=[0., 5000., 10000.])
         atm.initializeAtmosphere(tel)
-    cl = ClosedLoop(tel, ngs, dm, wfs, R, gain=0.4, layers=atm, max_steps=n_steps + 30)
-    cl.capture()
-    cl.run(20)
-    torch.cuda.synchronize()
-    cl.reset()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    cl.run(n_steps)
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / n_steps
-    wfe = cl.residual_wfe
+
+    def timed_loop():
+        cl = ClosedLoop(tel, ngs, dm, wfs, R, gain=0.4, layers=atm, max_steps=n_steps + 30)
+        cl.capture()
+        cl.run(20)
+        torch.cuda.synchronize()
+        cl.reset()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        cl.run(n_steps)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n_steps, cl.residual_wfe
+
+    # the DM's default projection (separable Gaussian IFs), then the dense
+    # BF16 tensor-core GEMV over the same IFs for comparison
+    path = dm.projection_path()
+    ms, wfe = timed_loop()
+    dm.separable_projection = False
+    ms_dense, wfe_dense = timed_loop()
+    dm.separable_projection = path == 'separable'
     return {'config': '40x40 PWFS, 240 px, N=504, 96 points, 41x41 DM (%d act), 3 infinite-screen layers, '
                       '1000 KL modes'
                       % dm.nValidAct,
             'steps': n_steps, 'us_per_step': ms * 1000.0, 'khz': 1.0 / ms,
-            'graph': True, 'variant': int(N_variant(wfs)), 'dm': 'bf16 tcgen05',
+            'graph': True, 'variant': int(N_variant(wfs)), 'dm': path,
+            'us_per_step_dense_bf16_dm': ms_dense * 1000.0,
+            'wfe_rel_diff_dense_vs_default': float(np.linalg.norm(wfe_dense - wfe) / np.linalg.norm(wfe)),
             'tc_status': dm.tensor_core_status(), 'wfe_first_nm': float(wfe[0] * 1e9),
             'wfe_mean_last_500_nm': float(wfe[-500:].mean() * 1e9)}
 
@@ -896,6 +907,8 @@ def run_case(args):
             import oopao_gb300 as og
             tel = og.Telescope(resolution=240, diameter=8.0, samplingTime=1e-3)
             dm = og.DeformableMirror(tel, nSubap=40, if_dtype='bf16')
+        # profile the dense tensor-core GEMM, not the separable default
+        dm.separable_projection = False
         c = torch.randn((dm.nValidAct, args.batch), device='cuda', generator=g) * 50e-9
         o = torch.empty((args.batch, 240, 240), device='cuda')
         torch.cuda.synchronize()
@@ -909,6 +922,8 @@ def run_case(args):
         out = {'case': args.case, 'batch': args.batch, 'reps': args.reps, 'tc_status': dm.tensor_core_status()}
     elif args.case == 'clgsc':
         out = {'case': args.case, 'cl_gsc_20x20': cl_gsc()}
+    elif args.case == 'cl':
+        out = {'case': args.case, 'cl_step': cl_rate()}
     elif args.case == 'next':
         out = {'case': args.case, 'next_rows': next_rows_leg()}
     elif args.case == 'gsc':
@@ -929,7 +944,7 @@ def main():
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline and accuracy legs')
     ap.add_argument('--no-extra', action='store_true',
                     help='skip the interaction-matrix comparisons and the closed-loop rate')
-    ap.add_argument('--case', default=None, help='run a small profiling workload (%s, dm40, gsc, next, clgsc) instead'
+    ap.add_argument('--case', default=None, help='run a small profiling workload (%s, dm40, gsc, next, clgsc, cl) instead'
                     % ', '.join(CASES))
     ap.add_argument('--batch', type=int, default=16)
     ap.add_argument('--reps', type=int, default=3)

@@ -215,6 +215,19 @@ int oopao_dm_opd_bf16(const void* modes, int n_act_pad, const float* coefs, int 
                       float scale, const float* base, float* opd, void* workspace, size_t workspace_bytes,
                       void* stream);
 
+/* Separable influence functions (DeformableMirror.modesComputation,
+ * OOPAO/DeformableMirror.py:572-600, with anamorphosisAngle = 0 on a
+ * Cartesian actuator grid): modes[y*res + x][a] = gx[i_a][x] * gy[j_a][y].
+ * opd[b][y][x] = scale * sum_j gy[j][y] sum_i C_b[j][i] gx[i][x] + base,
+ * C_b[j][i] = coefs[grid_act[j*nx + i]][b] (grid_act < 0: no actuator).
+ * gx device [nx][res], gy [ny][res], grid_act [ny*nx] int32, coefs
+ * [n_act][batch]; same output layout as oopao_dm_opd_f32.  ws: at least
+ * oopao_dm_sep_workspace_bytes(ny, res, batch) bytes.  Two launches. */
+size_t oopao_dm_sep_workspace_bytes(int ny, int res, int batch);
+int oopao_dm_opd_sep_f32(const float* gx, const float* gy, const int* grid_act, int nx, int ny, const float* coefs,
+                         int n_act, int res, int batch, float scale, const float* base, float* opd, void* ws,
+                         size_t ws_bytes, void* stream);
+
 /* opd = (modes @ coefs)^T * scale + base: the DM shape added to an incoming
  * OPD in one pass (DeformableMirror.relay, OOPAO/DeformableMirror.py:441-447:
  * src.OPD_no_pupil += dm.OPD).  base: device [batch][n_pix] or NULL. */

@@ -52,6 +52,9 @@ SIGNATURES = {
     'oopao_dm_opd_acc_f32': (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_float, c_void_p, c_void_p,
                                      c_void_p]),
     'oopao_dm_modes_bf16': (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p]),
+    'oopao_dm_sep_workspace_bytes': (c_size_t, [c_int, c_int, c_int]),
+    'oopao_dm_opd_sep_f32': (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_int,
+                                     c_float, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     'oopao_dm_bf16_workspace_bytes': (c_size_t, [c_int, c_int]),
     'oopao_dm_opd_bf16': (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_float, c_void_p, c_void_p,
                                   c_void_p, c_size_t, c_void_p]),

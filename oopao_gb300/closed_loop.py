@@ -189,11 +189,10 @@ class ClosedLoop:
             self._x0 = (N.ctypes.c_float * nl)(*c)
             self._vy = (N.ctypes.c_float * nl)(*np.float32(layers.vy))
             self._vx = (N.ctypes.c_float * nl)(*np.float32(layers.vx))
-        self._tc_ws = None
-        if getattr(dm, '_modes_bf16', None) is not None:
-            nb = N.load().oopao_dm_bf16_workspace_bytes(dm._n_act_pad, 1)
-            self._tc_ws = torch.zeros(nb, dtype=torch.uint8, device=d)
-            self._tc_nb = nb
+        # the loop owns its projection workspace: the graph keeps its address
+        nb = dm.projection_workspace_bytes(1)
+        self._dm_ws = torch.zeros(nb, dtype=torch.uint8, device=d) if nb else None
+        self._tc_ws = self._dm_ws if dm.projection_path() == 'bf16' else None
         self.science = bool(science)
         if self.science:
             # science camera of the NGS: zero padding 2 (N = 2 res), centring
@@ -262,12 +261,7 @@ class ClosedLoop:
             N.call('oopao_cl_screen', len(self._scr), self._scr_ptr, self._h, self._w, self._y0, self._x0,
                    self._vy, self._vx, self.res, self.step_counter, self.opd_atm, st)
             base = self.opd_atm
-        if self._tc_ws is not None:
-            N.call('oopao_dm_opd_bf16', dm._modes_bf16, dm._n_act_pad, self.coefs, dm.nValidAct, self.res * self.res,
-                   1, 1.0, base, self.opd, self._tc_ws, self._tc_nb, st)
-        else:
-            N.call('oopao_dm_opd_acc_f32', dm._modes_t, self.coefs, dm.nValidAct, self.res * self.res, 1, 1.0,
-                   base, self.opd, st)
+        dm._launch_projection(self.coefs, 1, 1.0, base, self.opd, st, ws=self._dm_ws)
         fork = torch.cuda.Event()
         fork.record(main)
         side = self._side

@@ -7,9 +7,12 @@ exactly as the reference (Fried grid and radial actuator selection
 :572-600), or takes user ``modes`` (the grid is still mis-registered, the
 modes are not, as in the reference).  The IF
 matrix is then kept on the GPU, transposed ([n_act][n_pix]), and every
-``dm.coefs = ...`` runs the projection OPD = modes @ coefs on the device
-through ``oopao_dm_opd_f32`` (FP32) or, with ``if_dtype='bf16'``, the
-tensor-core path.  ``dm.OPD`` is materialised on the host only when read.
+``dm.coefs = ...`` runs the projection OPD = modes @ coefs on the device.
+Gaussian IFs on a Cartesian grid without rotation or anamorphosis angle
+factorise as gx(x) gy(y): they are projected exactly by two small
+contractions (``oopao_dm_opd_sep_f32``).  Other IFs go through
+``oopao_dm_opd_f32`` (FP32) or, with ``if_dtype='bf16'``, the tensor-core
+GEMM.  ``dm.OPD`` is materialised on the host only when read.
 """
 import numpy as np
 import torch
@@ -93,6 +96,7 @@ class DeformableMirror:
         yIF = y4 - mr.shiftY
         self.coordinates = np.stack([xIF, yIF], axis=1)
         self.xIF, self.yIF = xIF, yIF
+        self._sep_host = None
         if modes is None:
             u0x = self.resolution / 2 + xIF * self.resolution / self.D
             u0y = self.resolution / 2 + yIF * self.resolution / self.D
@@ -107,6 +111,8 @@ class DeformableMirror:
                 self.nIF = self.nValidAct
                 self.xIF, self.yIF = self.xIF[keep], self.yIF[keep]
                 self.coordinates = self.coordinates[keep]
+                u0x, u0y = u0x[keep], u0y[keep]
+            self._sep_host = self._separable_factors(u0x, u0y)
         else:
             self.modes = np.asarray(modes) * self.sign
             self.nValidAct = self.modes.shape[1]
@@ -115,6 +121,14 @@ class DeformableMirror:
         self._dev = device()
         self._modes_t = None
         self._upload_modes()
+        # the separable projection serves every batch when the IFs factorise
+        self.separable_projection = self._sep_host is not None
+        self._sep = None
+        self._sep_ws = None
+        if self._sep_host is not None:
+            gx, gy, cells = self._sep_host
+            self._sep = (torch.as_tensor(gx, device=self._dev), torch.as_tensor(gy, device=self._dev),
+                         torch.as_tensor(cells, device=self._dev), gx.shape[0], gy.shape[0])
         self._opd_dev = None
         self._opd_host = None
         self._coefs = None
@@ -166,6 +180,45 @@ class DeformableMirror:
             out = np.float32(out)
         return out
 
+    def _separable_factors(self, u0x, u0y):
+        """(gx [nx,res], gy [ny,res] float32, grid cell -> actuator [ny*nx]
+        int32) with modes[y*res+x, a] = gx[i_a, x] * gy[j_a, y], or None when
+        the IFs do not factorise that way: an anamorphosis angle couples x and
+        y, a rotated grid has no common columns, and a grid with a cell shared
+        by two actuators has no cell map.  The factors are checked against
+        the float64 modes before use."""
+        if self.misReg.anamorphosisAngle != 0:
+            return None
+        xs, ix = np.unique(u0x, return_inverse=True)
+        ys, iy = np.unique(u0y, return_inverse=True)
+        nx, ny = len(xs), len(ys)
+        if nx * ny > 4 * len(u0x) + 64:
+            return None
+        cells = np.full(nx * ny, -1, dtype=np.int32)
+        flat = iy * nx + ix
+        if len(np.unique(flat)) != len(flat):
+            return None
+        cells[flat] = np.arange(len(flat), dtype=np.int32)
+        res = self.resolution
+        w = (res / self.nActAlongDiameter) / np.sqrt(2 * np.log(1. / self.mechCoupling))
+        a = 1 / (2 * ((1 + self.misReg.radialScaling) * w) ** 2)
+        c = 1 / (2 * ((1 + self.misReg.tangentialScaling) * w) ** 2)
+        X = np.linspace(0, 1, res) * res
+        gx = self.sign * np.exp(-a * (X[None, :] - xs[:, None]) ** 2)
+        gy = np.exp(-c * (X[None, :] - ys[:, None]) ** 2)
+        if self.flip_lr:
+            gx = gx[:, ::-1]
+        if self.flip_:
+            gx, gy = gx[:, ::-1], gy[:, ::-1]
+        # the dense modes are the reference: the factors must reproduce them
+        scale = np.max(np.abs(self.modes))
+        for k in range(0, len(u0x), 64):
+            cols = np.arange(k, min(k + 64, len(u0x)))
+            rebuilt = (gy[iy[cols]][:, :, None] * gx[ix[cols]][:, None, :]).reshape(len(cols), res * res)
+            if np.max(np.abs(rebuilt.T - self.modes[:, cols])) > 1e-12 * scale:
+                return None
+        return (np.ascontiguousarray(gx, dtype=np.float32), np.ascontiguousarray(gy, dtype=np.float32), cells)
+
     def _upload_modes(self):
         mt = np.ascontiguousarray(np.asarray(self.modes, dtype=np.float32).T)
         self._modes_t = torch.as_tensor(mt, device=self._dev)
@@ -183,24 +236,65 @@ class DeformableMirror:
     # ------------------------------------------------------------ projection
     def opd_device(self, coefs_dev, scale=1.0, out=None, base=None):
         """Device projection: coefs [n_act] or [n_act, B] float32 -> opd
-        [B, res, res] float32 (= (modes @ coefs)^T * scale [+ base]); FP32
-        CUDA-core path, or the BF16 tensor-core path for if_dtype='bf16'."""
+        [B, res, res] float32 (= (modes @ coefs)^T * scale [+ base]) by the
+        path projection_path() names."""
         c = coefs_dev if coefs_dev.ndim == 2 else coefs_dev[:, None]
         c = c.contiguous()
         B = c.shape[1]
         res = self.resolution
         if out is None:
             out = torch.empty((B, res, res), dtype=torch.float32, device=self._dev)
-        if self._modes_bf16 is not None:
-            nb = N.load().oopao_dm_bf16_workspace_bytes(self._n_act_pad, B)
-            if self._tc_ws is None or self._tc_ws.numel() < nb:
-                self._tc_ws = torch.empty(nb, dtype=torch.uint8, device=self._dev)
+        self._launch_projection(c, B, scale, base, out, N.stream_handle())
+        return out
+
+    def projection_path(self):
+        """'separable', 'bf16' (tensor cores) or 'fp32' (dense CUDA cores)."""
+        if self._sep is not None and self.separable_projection:
+            return 'separable'
+        return 'bf16' if self._modes_bf16 is not None else 'fp32'
+
+    def projection_workspace_bytes(self, B):
+        """Device workspace bytes the projection of B coefficient vectors needs."""
+        path = self.projection_path()
+        if path == 'separable':
+            return N.load().oopao_dm_sep_workspace_bytes(self._sep[4], self.resolution, B)
+        if path == 'bf16':
+            return N.load().oopao_dm_bf16_workspace_bytes(self._n_act_pad, B)
+        return 0
+
+    def _projection_workspace(self, B):
+        """The DM's own projection workspace, grown on demand (a captured
+        graph must hold its own buffer instead: this one may be replaced)."""
+        nb = self.projection_workspace_bytes(B)
+        if nb == 0:
+            return None
+        if self.projection_path() == 'separable':
+            if self._sep_ws is None or self._sep_ws.numel() < nb:
+                self._sep_ws = torch.empty(nb, dtype=torch.uint8, device=self._dev)
+            return self._sep_ws
+        if self._tc_ws is None or self._tc_ws.numel() < nb:
+            self._tc_ws = torch.empty(nb, dtype=torch.uint8, device=self._dev)
+        return self._tc_ws
+
+    def _launch_projection(self, c, B, scale, base, out, stream, ws=None):
+        """out = (modes @ c)^T * scale + base on `stream`: the separable
+        factors when the IFs factorise (exact, 2*ny*res*(nx+res) flops per
+        frame), else the BF16 tensor-core GEMM (if_dtype='bf16') or the FP32
+        GEMV/SGEMM over the dense IF matrix.  ws: a caller-owned workspace of
+        projection_workspace_bytes(B) bytes, or None for the DM's own."""
+        res = self.resolution
+        if ws is None:
+            ws = self._projection_workspace(B)
+        if self._sep is not None and self.separable_projection:
+            gx, gy, cells, nx, ny = self._sep
+            N.call('oopao_dm_opd_sep_f32', gx, gy, cells, nx, ny, c, self.nValidAct, res, B, float(scale), base, out,
+                   ws, ws.numel(), stream)
+        elif self._modes_bf16 is not None:
             N.call('oopao_dm_opd_bf16', self._modes_bf16, self._n_act_pad, c, self.nValidAct, res * res, B,
-                   float(scale), base, out, self._tc_ws, nb, N.stream_handle())
+                   float(scale), base, out, ws, ws.numel(), stream)
         else:
             N.call('oopao_dm_opd_acc_f32', self._modes_t, c, self.nValidAct, res * res, B, float(scale), base, out,
-                   N.stream_handle())
-        return out
+                   stream)
 
     def tensor_core_status(self):
         """0, or the code of a timed-out pipeline wait of the last BF16 projection."""

@@ -82,3 +82,37 @@ def test_dm_host_geometry(golden, tag):
     u0y = res / 2 + coords[:, 1] * res / 8.0
     modes = DM._gaussian_modes(fake, u0x, u0y)
     np.testing.assert_allclose(modes, d[tag + '_modes'], rtol=1e-12, atol=1e-300)
+
+
+@pytest.mark.parametrize('kw', [dict(), dict(flip_lr=True), dict(flip_=True), dict(flip_lr=True, flip_=True),
+                                dict(sign=-1), dict(mr=dict(shiftX=0.1, radialScaling=0.05, tangentialScaling=-0.02))],
+                         ids=['plain', 'flip_lr', 'flip', 'both_flips', 'sign', 'shift_scalings'])
+def test_separable_factors_rebuild_the_modes(kw):
+    """The drop-in DM's separable factors (gx, gy, cell map) reproduce its
+    dense float64 Gaussian IFs, and a rotated or anamorphic grid is refused
+    (host only)."""
+    import types
+    from oopao_gb300.deformable_mirror import DeformableMirror as DM
+    from oopao_gb300.mis_registration import MisRegistration
+    res, ns = 48, 8
+    mr = MisRegistration(dict(dict.fromkeys(O.MISREG_FIELDS, 0.0), **kw.get('mr', {})))
+    fake = types.SimpleNamespace(resolution=res, nActAlongDiameter=ns, mechCoupling=0.35, misReg=mr,
+                                 sign=kw.get('sign', 1), flip_lr=kw.get('flip_lr', False),
+                                 flip_=kw.get('flip_', False), floating_precision=64)
+    u0x, u0y, _ = O.dm_actuator_pixels(res, 8.0, ns, 0.0, mr.__dict__)
+    fake.modes = DM._gaussian_modes(fake, u0x, u0y)
+    gx, gy, cells = DM._separable_factors(fake, u0x, u0y)
+    ny, nx = gy.shape[0], gx.shape[0]
+    assert (cells >= 0).sum() == len(u0x)
+    coefs = np.random.default_rng(0).standard_normal(len(u0x))
+    C = np.zeros(ny * nx)
+    C[cells >= 0] = coefs[cells[cells >= 0]]
+    opd = gy.astype(np.float64).T @ C.reshape(ny, nx) @ gx.astype(np.float64)
+    dense = (fake.modes @ coefs).reshape(res, res)
+    assert np.max(np.abs(opd - dense)) < 1e-6 * np.max(np.abs(dense))
+    for bad in (dict(rotationAngle=2.0), dict(anamorphosisAngle=20.0)):
+        mr2 = MisRegistration(dict(dict.fromkeys(O.MISREG_FIELDS, 0.0), **bad))
+        fake.misReg = mr2
+        ux, uy, _ = O.dm_actuator_pixels(res, 8.0, ns, 0.0, mr2.__dict__)
+        fake.modes = DM._gaussian_modes(fake, ux, uy)
+        assert DM._separable_factors(fake, ux, uy) is None
