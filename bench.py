@@ -144,25 +144,29 @@ def cl_rate(n_steps=2000):
                          windSpeed=[10., 15., 20.], windDirection=[0., 72., 144.], altitude=[0., 5000., 10000.])
         atm.initializeAtmosphere(tel)
 
-    def timed_loop():
+    def timed_loop(nvtx=None):
         cl = ClosedLoop(tel, ngs, dm, wfs, R, gain=0.4, layers=atm, max_steps=n_steps + 30)
         cl.capture()
         cl.run(20)
         torch.cuda.synchronize()
         cl.reset()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if nvtx:
+            torch.cuda.nvtx.range_push(nvtx)
         e0.record()
         cl.run(n_steps)
         e1.record()
+        if nvtx:
+            torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / n_steps, cl.residual_wfe
 
     # the DM's default projection (separable Gaussian IFs), then the dense
     # BF16 tensor-core GEMV over the same IFs for comparison
     path = dm.projection_path()
-    ms, wfe = timed_loop()
+    ms, wfe = timed_loop('cl_steps')
     dm.separable_projection = False
-    ms_dense, wfe_dense = timed_loop()
+    ms_dense, wfe_dense = timed_loop('cl_steps_dense_dm')
     dm.separable_projection = path == 'separable'
     return {'config': '40x40 PWFS, 240 px, N=504, 96 points, 41x41 DM (%d act), 3 infinite-screen layers, '
                       '1000 KL modes'

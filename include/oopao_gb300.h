@@ -222,7 +222,9 @@ int oopao_dm_opd_bf16(const void* modes, int n_act_pad, const float* coefs, int 
  * C_b[j][i] = coefs[grid_act[j*nx + i]][b] (grid_act < 0: no actuator).
  * gx device [nx][res], gy [ny][res], grid_act [ny*nx] int32, coefs
  * [n_act][batch]; same output layout as oopao_dm_opd_f32.  ws: at least
- * oopao_dm_sep_workspace_bytes(ny, res, batch) bytes.  Two launches. */
+ * oopao_dm_sep_workspace_bytes(ny, res, batch) bytes.  One launch when
+ * nx*ny + 16*nx + 80*ny <= 24576 (the coefficient grid and one block of the
+ * factors fit in shared memory), two otherwise. */
 size_t oopao_dm_sep_workspace_bytes(int ny, int res, int batch);
 int oopao_dm_opd_sep_f32(const float* gx, const float* gy, const int* grid_act, int nx, int ny, const float* coefs,
                          int n_act, int res, int batch, float scale, const float* base, float* opd, void* ws,

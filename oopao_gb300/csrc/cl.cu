@@ -55,21 +55,47 @@ __global__ void cl_screen(ScreenArgs a) {
 }
 
 // coefs[a] -= gain * sum_j R[a][j] s[j].  Four warps per actuator, each over
-// an interleaved quarter of the signals with eight loads per lane in flight
-// (enough bytes in flight to stream R at HBM rate); block 0 thread 0
-// advances the step counter.
+// an interleaved quarter of the signals; block 0 thread 0 advances the step
+// counter.
 constexpr int kIntActPerBlock = 2;  // 256 threads = 2 actuators x 4 warps
 
-__global__ void __launch_bounds__(256) cl_integrate(const float* __restrict__ R, const float* __restrict__ s,
-                                                    int n_act, int n_sig, float gain, float* __restrict__ coefs,
-                                                    int* step) {
-  __shared__ float red[8];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int act = blockIdx.x * kIntActPerBlock + (w >> 2), part = w & 3;
+// One lane's share of row . s (the 128 lanes of an actuator interleave).
+// VEC4: 16-byte loads (row and s 16-byte aligned, n_sig % 4 == 0), four of
+// each in flight, so a 2.5k-signal row is read in about one round trip;
+// otherwise eight scalar loads in flight.
+template <bool VEC4>
+__device__ __forceinline__ float row_dot_part(const float* __restrict__ r, const float* __restrict__ s, int n_sig,
+                                              int lane128) {
   float acc = 0.f;
-  if (act < n_act) {
-    const float* r = R + (size_t)act * n_sig;
-    int j = part * 32 + lane;
+  if constexpr (VEC4) {
+    const float4* r4 = reinterpret_cast<const float4*>(r);
+    const float4* s4 = reinterpret_cast<const float4*>(s);
+    const int n4 = n_sig >> 2;
+    int j = lane128;
+    for (; j + 3 * 128 < n4; j += 4 * 128) {
+      float4 rv[4], sv[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        rv[u] = r4[j + u * 128];
+        sv[u] = s4[j + u * 128];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        acc = fmaf(rv[u].x, sv[u].x, acc);
+        acc = fmaf(rv[u].y, sv[u].y, acc);
+        acc = fmaf(rv[u].z, sv[u].z, acc);
+        acc = fmaf(rv[u].w, sv[u].w, acc);
+      }
+    }
+    for (; j < n4; j += 128) {
+      const float4 rv = r4[j], sv = s4[j];
+      acc = fmaf(rv.x, sv.x, acc);
+      acc = fmaf(rv.y, sv.y, acc);
+      acc = fmaf(rv.z, sv.z, acc);
+      acc = fmaf(rv.w, sv.w, acc);
+    }
+  } else {
+    int j = lane128;
     for (; j + 7 * 128 < n_sig; j += 8 * 128) {
       float rv[8], sv[8];
 #pragma unroll
@@ -82,6 +108,18 @@ __global__ void __launch_bounds__(256) cl_integrate(const float* __restrict__ R,
     }
     for (; j < n_sig; j += 128) acc = fmaf(r[j], s[j], acc);
   }
+  return acc;
+}
+
+template <bool VEC4>
+__global__ void __launch_bounds__(256) cl_integrate(const float* __restrict__ R, const float* __restrict__ s,
+                                                    int n_act, int n_sig, float gain, float* __restrict__ coefs,
+                                                    int* step) {
+  __shared__ float red[8];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int act = blockIdx.x * kIntActPerBlock + (w >> 2), part = w & 3;
+  float acc = 0.f;
+  if (act < n_act) acc = row_dot_part<VEC4>(R + (size_t)act * n_sig, s, n_sig, part * 32 + lane);
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   if (lane == 0) red[w] = acc;
   __syncthreads();
@@ -99,6 +137,7 @@ __global__ void __launch_bounds__(256) cl_integrate(const float* __restrict__ R,
 // tutorials/AO_closed_loop_Pyramid_WFS_GSC.py: M2C @ diag(1/og) @ M @ s):
 // y[m] = (M[m] . s) / og[m] from step og_start on (og = 1 before).  Same
 // layout and load pattern as cl_integrate.
+template <bool VEC4>
 __global__ void __launch_bounds__(256) cl_modal(const float* __restrict__ M, const float* __restrict__ s,
                                                 int n_modes, int n_sig, const double* __restrict__ og, int og_start,
                                                 const int* __restrict__ step, float* __restrict__ y) {
@@ -106,21 +145,7 @@ __global__ void __launch_bounds__(256) cl_modal(const float* __restrict__ M, con
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int mode = blockIdx.x * kIntActPerBlock + (w >> 2), part = w & 3;
   float acc = 0.f;
-  if (mode < n_modes) {
-    const float* r = M + (size_t)mode * n_sig;
-    int j = part * 32 + lane;
-    for (; j + 7 * 128 < n_sig; j += 8 * 128) {
-      float rv[8], sv[8];
-#pragma unroll
-      for (int u = 0; u < 8; u++) {
-        rv[u] = r[j + u * 128];
-        sv[u] = s[j + u * 128];
-      }
-#pragma unroll
-      for (int u = 0; u < 8; u++) acc = fmaf(rv[u], sv[u], acc);
-    }
-    for (; j < n_sig; j += 128) acc = fmaf(r[j], s[j], acc);
-  }
+  if (mode < n_modes) acc = row_dot_part<VEC4>(M + (size_t)mode * n_sig, s, n_sig, part * 32 + lane);
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   if (lane == 0) red[w] = acc;
   __syncthreads();
@@ -240,12 +265,22 @@ extern "C" int oopao_cl_screen(int n_layers, const float* const* screens, const 
   return OOPAO_OK;
 }
 
+namespace {
+// 16-byte loads of every row of a row-major [rows][n_sig] matrix and of s.
+bool vec4_ok(const float* m, const float* s, int n_sig) {
+  return n_sig % 4 == 0 && reinterpret_cast<uintptr_t>(m) % 16 == 0 && reinterpret_cast<uintptr_t>(s) % 16 == 0;
+}
+}  // namespace
+
 extern "C" int oopao_cl_integrate(const float* R, const float* s, int n_act, int n_sig, float gain, float* coefs,
                                   int* step, void* stream) {
   OOPAO_CHECK_ARG(R && s && coefs, "NULL argument");
   OOPAO_CHECK_ARG(n_act > 0 && n_sig > 0, "sizes must be positive");
-  cl_integrate<<<ceil_div(n_act, kIntActPerBlock), 256, 0, (cudaStream_t)stream>>>(R, s, n_act, n_sig, gain, coefs,
-                                                                                  step);
+  const int g = ceil_div(n_act, kIntActPerBlock);
+  if (vec4_ok(R, s, n_sig))
+    cl_integrate<true><<<g, 256, 0, (cudaStream_t)stream>>>(R, s, n_act, n_sig, gain, coefs, step);
+  else
+    cl_integrate<false><<<g, 256, 0, (cudaStream_t)stream>>>(R, s, n_act, n_sig, gain, coefs, step);
   oopao_count_launches(1);
   OOPAO_CUDA_TRY(cudaGetLastError());
   return OOPAO_OK;
@@ -255,8 +290,11 @@ extern "C" int oopao_cl_modal(const float* M, const float* s, int n_modes, int n
                               int og_start, const int* step, float* y, void* stream) {
   OOPAO_CHECK_ARG(M && s && y, "NULL argument");
   OOPAO_CHECK_ARG(n_modes > 0 && n_sig > 0, "sizes must be positive");
-  cl_modal<<<ceil_div(n_modes, kIntActPerBlock), 256, 0, (cudaStream_t)stream>>>(M, s, n_modes, n_sig, og, og_start,
-                                                                                step, y);
+  const int g = ceil_div(n_modes, kIntActPerBlock);
+  if (vec4_ok(M, s, n_sig))
+    cl_modal<true><<<g, 256, 0, (cudaStream_t)stream>>>(M, s, n_modes, n_sig, og, og_start, step, y);
+  else
+    cl_modal<false><<<g, 256, 0, (cudaStream_t)stream>>>(M, s, n_modes, n_sig, og, og_start, step, y);
   oopao_count_launches(1);
   OOPAO_CUDA_TRY(cudaGetLastError());
   return OOPAO_OK;

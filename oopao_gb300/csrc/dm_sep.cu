@@ -56,6 +56,78 @@ __global__ void __launch_bounds__(kSepThreads) dm_sep_cols(const float* __restri
   }
 }
 
+// Both contractions in one launch for grids whose operands fit in shared
+// memory.  A CTA owns kSepTile columns x kSepRows rows of the OPD.  It first
+// issues every global load it needs at once (the gathered coefficient grid
+// C_b, the kSepTile columns of gx and the kSepRows columns of gy), then forms
+// the kSepTile columns of T and the output block from shared memory, so its
+// path holds about two memory round trips.  The projection is ~2.5 MFLOP per
+// 240 x 240 frame; latency, not arithmetic, sets its time.
+constexpr int kSepTile = 16;
+constexpr int kSepRows = 64;
+constexpr int kSepPerThread = kSepRows * kSepTile / 256;  // 4 rows per thread
+
+__host__ __device__ constexpr size_t sep_fused_floats(int nx, int ny) {
+  return (size_t)nx * ny + (size_t)nx * kSepTile + (size_t)ny * kSepRows + (size_t)ny * kSepTile;
+}
+constexpr size_t kSepFusedFloats = 24576;  // 96 KB of dynamic shared memory
+
+__global__ void __launch_bounds__(256) dm_sep_fused(const float* __restrict__ gx, const float* __restrict__ gy,
+                                                    const int* __restrict__ grid_act,
+                                                    const float* __restrict__ coefs, int n_act, int nx, int ny,
+                                                    int res, int batch, float scale,
+                                                    const float* __restrict__ base, float* __restrict__ opd) {
+  extern __shared__ float sm[];
+  float* cm = sm;                          // [ny][nx]   C_b
+  float* gxb = cm + nx * ny;               // [nx][kSepTile]
+  float* gyb = gxb + nx * kSepTile;        // [ny][kSepRows]
+  float* tb = gyb + ny * kSepRows;         // [ny][kSepTile]
+  const int x0 = blockIdx.x * kSepTile, y0 = blockIdx.y * kSepRows, b = blockIdx.z;
+  const int tid = threadIdx.x;
+#pragma unroll 4
+  for (int e = tid; e < nx * ny; e += 256) {
+    const int a = grid_act[e];
+    cm[e] = (a >= 0 && a < n_act) ? coefs[(size_t)a * batch + b] : 0.f;
+  }
+#pragma unroll 4
+  for (int e = tid; e < nx * kSepTile; e += 256) {
+    const int x = x0 + e % kSepTile;
+    gxb[e] = x < res ? __ldg(gx + (size_t)(e / kSepTile) * res + x) : 0.f;
+  }
+#pragma unroll 4
+  for (int e = tid; e < ny * kSepRows; e += 256) {
+    const int y = y0 + e % kSepRows;
+    gyb[e] = y < res ? __ldg(gy + (size_t)(e / kSepRows) * res + y) : 0.f;
+  }
+  __syncthreads();
+  for (int e = tid; e < ny * kSepTile; e += 256) {
+    const int j = e / kSepTile, xx = e % kSepTile;
+    float acc = 0.f;
+    for (int i = 0; i < nx; i++) acc = fmaf(cm[j * nx + i], gxb[i * kSepTile + xx], acc);
+    tb[e] = acc;
+  }
+  __syncthreads();
+  const int xx = tid % kSepTile, r0 = tid / kSepTile, x = x0 + xx;
+  float acc[kSepPerThread];
+#pragma unroll
+  for (int k = 0; k < kSepPerThread; k++) acc[k] = 0.f;
+  for (int j = 0; j < ny; j++) {
+    const float t = tb[j * kSepTile + xx];
+#pragma unroll
+    for (int k = 0; k < kSepPerThread; k++) acc[k] = fmaf(gyb[j * kSepRows + r0 + 16 * k], t, acc[k]);
+  }
+  if (x < res) {
+#pragma unroll
+    for (int k = 0; k < kSepPerThread; k++) {
+      const int y = y0 + r0 + 16 * k;
+      if (y < res) {
+        const size_t o = ((size_t)b * res + y) * res + x;
+        opd[o] = acc[k] * scale + (base ? base[o] : 0.f);
+      }
+    }
+  }
+}
+
 }  // namespace
 
 extern "C" size_t oopao_dm_sep_workspace_bytes(int ny, int res, int batch) {
@@ -72,6 +144,16 @@ extern "C" int oopao_dm_opd_sep_f32(const float* gx, const float* gy, const int*
   OOPAO_CHECK_ARG(ws_bytes >= oopao_dm_sep_workspace_bytes(ny, res, batch), "workspace too small");
   OOPAO_CHECK_ARG(batch <= 65535, "batch larger than 65535");
   cudaStream_t st = (cudaStream_t)stream;
+  if (sep_fused_floats(nx, ny) <= kSepFusedFloats) {
+    const dim3 grid(ceil_div(res, kSepTile), ceil_div(res, kSepRows), batch);
+    const size_t smem = sizeof(float) * sep_fused_floats(nx, ny);
+    if (smem > 48 * 1024)
+      OOPAO_CUDA_TRY(cudaFuncSetAttribute(dm_sep_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dm_sep_fused<<<grid, 256, smem, st>>>(gx, gy, grid_act, coefs, n_act, nx, ny, res, batch, scale, base, opd);
+    oopao_count_launches(1);
+    OOPAO_CUDA_TRY(cudaGetLastError());
+    return OOPAO_OK;
+  }
   float* t = (float*)ws;
   dm_sep_rows<<<dim3(ny, batch), kSepThreads, sizeof(float) * nx, st>>>(gx, grid_act, coefs, n_act, nx, ny, res,
                                                                          batch, t);

@@ -447,6 +447,10 @@ struct SignalArgs {
   float units, norma_const;
 };
 
+// Quadrant cells per thread that the slopes path keeps in registers between
+// the flux reduction and the output (nq^2 <= kSigCells * blockDim).
+constexpr int kSigCells = 8;
+
 __global__ void pwfs_signal(SignalArgs a) {
   __shared__ float red[33];
   const int b = blockIdx.x;
@@ -454,6 +458,58 @@ __global__ void pwfs_signal(SignalArgs a) {
   float* s2 = a.signal_2d + (size_t)b * a.n2d;
   float* sg = a.signal + (size_t)b * a.n_signal;
   const bool slopes = a.mode <= 2;
+  const int nq2s = a.nq * a.nq;
+  if (slopes && nq2s <= kSigCells * (int)blockDim.x) {
+    // one read of the frame: every load of a cell (four quadrant pixels, its
+    // reference slopes and signal slots) is issued before the reduction; the
+    // per-thread flux sums run over the same cells in the same order as the
+    // general path below, so both give the same bits
+    float sx[kSigCells], sy[kSigCells], rx[kSigCells], ry[kSigCells];
+    int ex[kSigCells], ey[kSigCells];
+    float part = 0.f;
+#pragma unroll
+    for (int k = 0; k < kSigCells; k++) {
+      const int idx = threadIdx.x + k * blockDim.x;
+      sx[k] = sy[k] = rx[k] = ry[k] = 0.f;
+      ex[k] = ey[k] = -1;
+      if (idx < nq2s) {
+        const int r = idx / a.nq, c = idx % a.nq;
+        const float i1 = fr[(a.q_r0[0] + r) * a.cam + a.q_c0[0] + c];
+        const float i2 = fr[(a.q_r0[1] + r) * a.cam + a.q_c0[1] + c];
+        const float i3 = fr[(a.q_r0[2] + r) * a.cam + a.q_c0[2] + c];
+        const float i4 = fr[(a.q_r0[3] + r) * a.cam + a.q_c0[3] + c];
+        if (a.ref2d) {
+          rx[k] = a.ref2d[idx];
+          ry[k] = a.ref2d[nq2s + idx];
+        }
+        ex[k] = a.sig_inv[idx];
+        ey[k] = a.sig_inv[nq2s + idx];
+        if (a.valid[idx]) {
+          sx[k] = ((i1 - i2) + i4) - i3;
+          sy[k] = ((i1 - i4) + i2) - i3;
+          if (a.mode == 0) part += ((i1 + i2) + i3) + i4;
+        }
+      }
+    }
+    if (a.mode == 2)
+      for (int idx = threadIdx.x; idx < a.cam * a.cam; idx += blockDim.x) part += fr[idx];
+    const float tot = block_sum(part, red);
+    const float norma = a.mode == 0 ? tot / (float)a.n_valid
+                      : a.mode == 2 ? tot / (float)(a.cam * a.cam) : a.norma_const;
+#pragma unroll
+    for (int k = 0; k < kSigCells; k++) {
+      const int idx = threadIdx.x + k * blockDim.x;
+      if (idx < nq2s) {
+        const float vx = (sx[k] / norma - rx[k]) * a.units, vy = (sy[k] / norma - ry[k]) * a.units;
+        s2[idx] = vx;
+        s2[nq2s + idx] = vy;
+        if (ex[k] >= 0) sg[ex[k]] = vx;
+        if (ey[k] >= 0) sg[ey[k]] = vy;
+      }
+    }
+    if (a.norma && threadIdx.x == 0) a.norma[b] = norma;
+    return;
+  }
   float part = 0.f;
   if (slopes) {
     const int nq2 = a.nq * a.nq;

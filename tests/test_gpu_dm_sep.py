@@ -73,3 +73,32 @@ def test_misregistered_projection_path(mr, path):
     out = dm.opd_device(torch.as_tensor(coefs, dtype=torch.float32, device='cuda')).cpu().double().numpy()
     ref = (dm.modes @ coefs).T.reshape(4, tel.resolution, tel.resolution)
     assert _rel(out, ref) < 1e-6
+
+
+@pytest.mark.parametrize('nx, ny, batch', [(12, 9, 2), (150, 60, 2), (300, 70, 3)],
+                         ids=['one_launch', 'one_launch_96k', 'two_launches'])
+def test_separable_cabi(nx, ny, batch):
+    """oopao_dm_opd_sep_f32 on synthetic factors: a grid whose coefficient map
+    fits in shared memory (one launch) and one that does not (two), with
+    empty grid cells, against the float64 product."""
+    from oopao_gb300 import _native as N
+    res, n_act = 64, None
+    rng = np.random.default_rng(nx)
+    gx = rng.standard_normal((nx, res)).astype(np.float32)
+    gy = rng.standard_normal((ny, res)).astype(np.float32)
+    cells = np.full(nx * ny, -1, np.int32)
+    used = rng.choice(nx * ny, size=(nx * ny) * 3 // 4, replace=False)
+    n_act = len(used)
+    cells[used] = rng.permutation(n_act).astype(np.int32)
+    coefs = rng.standard_normal((n_act, batch)).astype(np.float32)
+    C = np.zeros((batch, ny * nx))
+    C[:, used] = coefs[cells[used]].T
+    ref = np.einsum('jy,bji,ix->byx', gy.astype(np.float64), C.reshape(batch, ny, nx), gx.astype(np.float64))
+    dev = lambda a: torch.as_tensor(a, device='cuda')
+    out = torch.empty((batch, res, res), dtype=torch.float32, device='cuda')
+    nb = N.load().oopao_dm_sep_workspace_bytes(ny, res, batch)
+    ws = torch.empty(nb, dtype=torch.uint8, device='cuda')
+    g_x, g_y, c_d, k_d = dev(gx), dev(gy), dev(cells), dev(coefs)
+    N.call('oopao_dm_opd_sep_f32', g_x, g_y, c_d, nx, ny, k_d, n_act, res, batch, 1.0, None, out, ws, nb,
+           N.stream_handle())
+    assert _rel(out.cpu().double().numpy(), ref) < 1e-5
