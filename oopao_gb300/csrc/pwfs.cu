@@ -1507,7 +1507,7 @@ extern "C" int oopao_pwfs_jvp(const oopao_pwfs_plan* p, const float* opd0, int o
         o0, dopd + (size_t)b0 * res * res, (float)phase_scale, p->d_amp, fld, res * res, 0);
     forward_to_z(fld, nb);
     AdJvpArgs ja{p->d_tw, z, g, weights_of(p), part, 0, k, 0, slot_pts, ks, p->bin, cam};
-    ad->jvp<<<dim3(ceil_div(n, ad->l), ks, nb), ad->t * ad->l, ad->smem_jvp, st>>>(ja);
+    ad->jvp<<<dim3(nb, ceil_div(n, ad->l), ks), ad->t * ad->l, ad->smem_jvp, st>>>(ja);
     pwfs_reduce_binned<<<dim3(ceil_div(cam * cam, 256), nb), 256, 0, st>>>(part, dframe + (size_t)b0 * cam * cam,
                                                                            cam * cam, ks);
     launches += 3;

@@ -96,7 +96,9 @@ __global__ void __launch_bounds__(T* L) ad_rows_jvp(AdJvpArgs a) {
     const float2 w = a.tw[(i % R2) * (i / R2)];
     twi[i] = make_float2(w.x, -w.y);
   }
-  const int b = blockIdx.z, slot = a.s0 + blockIdx.y, row = blockIdx.x * L + l;
+  // grid (items, row blocks, slots): the items of one (row block, slot) run
+  // side by side and share the operating-point rows G_k through L2
+  const int b = blockIdx.x, slot = a.s0 + blockIdx.z, row = blockIdx.y * L + l;
   const bool active = row < N;
   const int kbeg = slot * a.slot_pts, kend = kbeg + a.slot_pts;
   float acc[PBB][R1];
@@ -153,7 +155,7 @@ __global__ void __launch_bounds__(T* L) ad_rows_jvp(AdJvpArgs a) {
     }
   }
   __syncthreads();
-  const int bin = a.bin, cam = a.cam, ncr = L / bin, cr0 = (blockIdx.x * L) / bin;
+  const int bin = a.bin, cam = a.cam, ncr = L / bin, cr0 = (blockIdx.y * L) / bin;
   float* out = a.binned + ((size_t)b * a.ksplit + slot) * cam * cam;
   for (int i = tid; i < ncr * cam; i += T * L) {
     const int cr = i / cam, cx = i - (i / cam) * cam;
