@@ -15,7 +15,11 @@ One step follows ``tutorials/AO_closed_loop_Pyramid_WFS.py:601-639`` and
 
 Every operation is a launch of ``liboopao_gb300`` on preallocated buffers; a
 device step counter carries the time index, so the captured graph is
-replayed as is for every later step (``ClosedLoop.run``).
+replayed as is for every later step (``ClosedLoop.run``).  The loop takes the
+sensor's plan (mask, modulation path, weights of a single-wavefront
+measurement), its valid pixels and reference slopes, and the DM's projection
+path when it is built: a change to any of them afterwards (a new mask,
+modulation, pupil shift or calibration) needs a new ClosedLoop.
 
 The turbulence is either the reference's infinite phase screens
 (``oopao_gb300.Atmosphere``, updated on the device inside the captured step)
