@@ -211,11 +211,14 @@ class DeformableMirror:
         if self.flip_:
             gx, gy = gx[:, ::-1], gy[:, ::-1]
         # the dense modes are the reference: the factors must reproduce them
+        # (to round-off of the modes' own precision: float32 with
+        # floating_precision=32)
         scale = np.max(np.abs(self.modes))
+        tol = (2e-7 if self.modes.dtype == np.float32 else 1e-12) * scale
         for k in range(0, len(u0x), 64):
             cols = np.arange(k, min(k + 64, len(u0x)))
             rebuilt = (gy[iy[cols]][:, :, None] * gx[ix[cols]][:, None, :]).reshape(len(cols), res * res)
-            if np.max(np.abs(rebuilt.T - self.modes[:, cols])) > 1e-12 * scale:
+            if np.max(np.abs(rebuilt.T - self.modes[:, cols])) > tol:
                 return None
         return (np.ascontiguousarray(gx, dtype=np.float32), np.ascontiguousarray(gy, dtype=np.float32), cells)
 

@@ -101,6 +101,10 @@ def test_separable_factors_rebuild_the_modes(kw):
                                  flip_=kw.get('flip_', False), floating_precision=64)
     u0x, u0y, _ = O.dm_actuator_pixels(res, 8.0, ns, 0.0, mr.__dict__)
     fake.modes = DM._gaussian_modes(fake, u0x, u0y)
+    fake32 = types.SimpleNamespace(**vars(fake))
+    fake32.floating_precision = 32
+    fake32.modes = DM._gaussian_modes(fake32, u0x, u0y)
+    assert fake32.modes.dtype == np.float32 and DM._separable_factors(fake32, u0x, u0y) is not None
     gx, gy, cells = DM._separable_factors(fake, u0x, u0y)
     ny, nx = gy.shape[0], gx.shape[0]
     assert (cells >= 0).sum() == len(u0x)
