@@ -282,9 +282,12 @@ def large_config(n_tangents=64):
 def dm_projection(peaks):
     """DM influence-function projection OPD = modes @ coefs at the 20x20,
     40x40 and 80x80 sizes: FP32 CUDA-core path vs BF16 tcgen05 path, per
-    batch.  Modes are seeded device-random (timing does not depend on the
-    values).  Dense FLOPs 2*n_pix*n_act*B; IF bytes are the bytes of the IF
-    matrix one call streams (FP32 [n_act][n_pix] or BF16 [n_pix][n_act_pad])."""
+    batch, and the separable projection of Gaussian IFs on the same actuator
+    grid ('separable': factors [n_side+1][res], the DM's default path).
+    Modes and factors are seeded device-random (timing does not depend on
+    the values).  Dense FLOPs 2*n_pix*n_act*B; IF bytes are the bytes of the
+    IF matrix one call streams (FP32 [n_act][n_pix] or BF16
+    [n_pix][n_act_pad])."""
     import torch
     from oopao_gb300 import _native as N
     lib = N.load()
@@ -297,15 +300,24 @@ def dm_projection(peaks):
         mt = torch.randn((n_act, n_pix), device='cuda', generator=g)
         mb = torch.empty((n_pix, n_pad), dtype=torch.bfloat16, device='cuda')
         N.call('oopao_dm_modes_bf16', mt, n_act, n_pix, n_pad, mb, st)
+        n_grid = int(name.split('x')[0]) + 1
+        gxs = torch.randn((n_grid, n_side), device='cuda', generator=g)
+        gys = torch.randn((n_grid, n_side), device='cuda', generator=g)
+        cells = torch.full((n_grid * n_grid,), -1, dtype=torch.int32, device='cuda')
+        cells[:n_act] = torch.arange(n_act, dtype=torch.int32, device='cuda')
         rows = []
         for B in (1, 16, 64, 300):
             c = torch.randn((n_act, B), device='cuda', generator=g)
             o = torch.empty((B, n_pix), device='cuda')
             nb = lib.oopao_dm_bf16_workspace_bytes(n_pad, B)
             ws = torch.zeros(nb, dtype=torch.uint8, device='cuda')
+            nbs = lib.oopao_dm_sep_workspace_bytes(n_grid, n_side, B)
+            wss = torch.zeros(nbs, dtype=torch.uint8, device='cuda')
             runs = {'fp32': lambda: N.call('oopao_dm_opd_acc_f32', mt, c, n_act, n_pix, B, 1.0, None, o, st),
                     'bf16_tc': lambda: N.call('oopao_dm_opd_bf16', mb, n_pad, c, n_act, n_pix, B, 1.0, None, o, ws,
-                                              nb, st)}
+                                              nb, st),
+                    'separable': lambda: N.call('oopao_dm_opd_sep_f32', gxs, gys, cells, n_grid, n_grid, c, n_act,
+                                                n_side, B, 1.0, None, o, wss, nbs, st)}
             row = {'batch': B}
             for key, fn in runs.items():
                 reps = 20
@@ -318,6 +330,10 @@ def dm_projection(peaks):
                 e1.record()
                 torch.cuda.synchronize()
                 ms = e0.elapsed_time(e1) / reps
+                if key == 'separable':
+                    row[key] = {'ms': ms, 'dense_equivalent_tflops': 2.0 * n_pix * n_act * B / ms / 1e9,
+                                'tflops': 2.0 * n_grid * n_side * (n_grid + n_side) * B / ms / 1e9}
+                    continue
                 if_bytes = n_pix * n_act * 4 if key == 'fp32' else n_pix * n_pad * 2
                 row[key] = {'ms': ms, 'tflops': 2.0 * n_pix * n_act * B / ms / 1e9,
                             'if_gbs': if_bytes / ms / 1e6}
@@ -928,6 +944,12 @@ def run_case(args):
         out = {'case': args.case, 'cl_gsc_20x20': cl_gsc()}
     elif args.case == 'cl':
         out = {'case': args.case, 'cl_step': cl_rate()}
+    elif args.case == 'dmproj':
+        try:
+            pk = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
+        except Exception:
+            pk = {'hbm_gbs': 6800.0, 'bf16_tflops': 1900.0}
+        out = {'case': args.case, 'dm_projection': dm_projection(pk)}
     elif args.case == 'next':
         out = {'case': args.case, 'next_rows': next_rows_leg()}
     elif args.case == 'gsc':
@@ -948,7 +970,7 @@ def main():
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline and accuracy legs')
     ap.add_argument('--no-extra', action='store_true',
                     help='skip the interaction-matrix comparisons and the closed-loop rate')
-    ap.add_argument('--case', default=None, help='run a small profiling workload (%s, dm40, gsc, next, clgsc, cl) instead'
+    ap.add_argument('--case', default=None, help='run a small profiling workload (%s, dm40, gsc, next, clgsc, cl, dmproj) instead'
                     % ', '.join(CASES))
     ap.add_argument('--batch', type=int, default=16)
     ap.add_argument('--reps', type=int, default=3)

@@ -250,15 +250,23 @@ class DeformableMirror:
         self._launch_projection(c, B, scale, base, out, N.stream_handle())
         return out
 
-    def projection_path(self):
-        """'separable', 'bf16' (tensor cores) or 'fp32' (dense CUDA cores)."""
-        if self._sep is not None and self.separable_projection:
+    # Batches above this go to the BF16 tensor-core GEMM even when the IFs
+    # factorise (GB300, 40x40: separable 21 us against 46 us at 16 columns,
+    # 74 us against 49 us at 64; the FP32 dense path is slower than the
+    # separable one at every batch).
+    SEPARABLE_MAX_BATCH_VS_TC = 32
+
+    def projection_path(self, B=1):
+        """Path of a projection of B coefficient vectors: 'separable', 'bf16'
+        (tensor cores) or 'fp32' (dense CUDA cores)."""
+        if self._sep is not None and self.separable_projection and (
+                self._modes_bf16 is None or B <= self.SEPARABLE_MAX_BATCH_VS_TC):
             return 'separable'
         return 'bf16' if self._modes_bf16 is not None else 'fp32'
 
     def projection_workspace_bytes(self, B):
         """Device workspace bytes the projection of B coefficient vectors needs."""
-        path = self.projection_path()
+        path = self.projection_path(B)
         if path == 'separable':
             return N.load().oopao_dm_sep_workspace_bytes(self._sep[4], self.resolution, B)
         if path == 'bf16':
@@ -271,7 +279,7 @@ class DeformableMirror:
         nb = self.projection_workspace_bytes(B)
         if nb == 0:
             return None
-        if self.projection_path() == 'separable':
+        if self.projection_path(B) == 'separable':
             if self._sep_ws is None or self._sep_ws.numel() < nb:
                 self._sep_ws = torch.empty(nb, dtype=torch.uint8, device=self._dev)
             return self._sep_ws
@@ -280,19 +288,21 @@ class DeformableMirror:
         return self._tc_ws
 
     def _launch_projection(self, c, B, scale, base, out, stream, ws=None):
-        """out = (modes @ c)^T * scale + base on `stream`: the separable
-        factors when the IFs factorise (exact, 2*ny*res*(nx+res) flops per
-        frame), else the BF16 tensor-core GEMM (if_dtype='bf16') or the FP32
-        GEMV/SGEMM over the dense IF matrix.  ws: a caller-owned workspace of
-        projection_workspace_bytes(B) bytes, or None for the DM's own."""
+        """out = (modes @ c)^T * scale + base on `stream` by
+        projection_path(B): the separable factors when the IFs factorise
+        (exact, 2*ny*res*(nx+res) flops per frame), else the BF16 tensor-core
+        GEMM (if_dtype='bf16') or the FP32 GEMV/SGEMM over the dense IF
+        matrix.  ws: a caller-owned workspace of projection_workspace_bytes(B)
+        bytes, or None for the DM's own."""
         res = self.resolution
         if ws is None:
             ws = self._projection_workspace(B)
-        if self._sep is not None and self.separable_projection:
+        path = self.projection_path(B)
+        if path == 'separable':
             gx, gy, cells, nx, ny = self._sep
             N.call('oopao_dm_opd_sep_f32', gx, gy, cells, nx, ny, c, self.nValidAct, res, B, float(scale), base, out,
                    ws, ws.numel(), stream)
-        elif self._modes_bf16 is not None:
+        elif path == 'bf16':
             N.call('oopao_dm_opd_bf16', self._modes_bf16, self._n_act_pad, c, self.nValidAct, res * res, B,
                    float(scale), base, out, ws, ws.numel(), stream)
         else:

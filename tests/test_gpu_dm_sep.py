@@ -33,16 +33,20 @@ def _rel(a, b):
 def test_separable_projection(kw, batch):
     tel, dm = _dm(**kw)
     assert dm.projection_path() == 'separable'
+    # large batches of a BF16-IF mirror go to the tensor-core GEMM
+    path = dm.projection_path(batch)
+    assert path == ('bf16' if kw.get('if_dtype') == 'bf16' and batch > dm.SEPARABLE_MAX_BATCH_VS_TC else 'separable')
+    tol = 2e-3 if path == 'bf16' else 1e-6
     rng = np.random.default_rng(batch)
     coefs = rng.standard_normal((dm.nValidAct, batch)) * 1e-7
     ref = (dm.modes @ coefs).T.reshape(batch, tel.resolution, tel.resolution)
     c = torch.as_tensor(coefs, dtype=torch.float32, device='cuda')
     out = dm.opd_device(c).cpu().double().numpy()
-    assert _rel(out, ref) < 1e-6
+    assert _rel(out, ref) < tol
     base = torch.as_tensor(rng.standard_normal((batch, tel.resolution, tel.resolution)) * 1e-7,
                            dtype=torch.float32, device='cuda')
     out2 = dm.opd_device(c, base=base).cpu().double().numpy()
-    assert _rel(out2, ref + base.cpu().double().numpy()) < 1e-6
+    assert _rel(out2, ref + base.cpu().double().numpy()) < tol
 
 
 def test_dense_and_separable_agree_through_the_relay():
