@@ -165,10 +165,10 @@ def InteractionMatrix(ngs, tel, dm, wfs, M2C, stroke, atm=None, phaseOffset=0, n
     n_modes = M2C.shape[1]
     t0 = time.time()
     if method == 'batched':
-        if not np.isscalar(phaseOffset) or phaseOffset != 0:
-            off = np.asarray(phaseOffset)
-        else:
-            off = None
+        # phaseOffset: the reference adds it to ngs.phase only after the pull
+        # has been measured (OOPAO/calibration/InteractionMatrix.py:126-133),
+        # so no measured signal sees it and D does not depend on it
+        off = None
         sp = _signals_batched(ngs, tel, dm, wfs, M2C * stroke, off)
         if single_pass:
             intmat = (0.5 * sp / stroke).T

@@ -478,6 +478,33 @@ def case_misreg(OOPAO, name='misreg_tiny', res=24, n_subap=4, modulation=3, ligh
     print(name, {t: rec[t + '_modes'].shape for t in MISREG_CASES})
 
 
+def case_im_offset(OOPAO, name='im_offset_tiny', res=24, n_subap=4, modulation=3, light_ratio=0.5, n_im=4,
+                   seed=13):
+    """InteractionMatrix with a phaseOffset, push-pull and single pass, in
+    chunks of 2 modes (OOPAO/calibration/InteractionMatrix.py:13-169): the
+    reference applies the offset to ngs.phase only after the pull is
+    measured, so it leaves D unchanged.  (A last chunk of one mode makes its
+    push-pull branch fail on the offset's shape, so the mode count is even.)"""
+    import json
+    from OOPAO.calibration.InteractionMatrix import InteractionMatrix
+    tel, ngs, dm, wfs = build(OOPAO, res, n_subap, modulation, light_ratio)
+    m2c = np.random.default_rng(seed).standard_normal((dm.nValidAct, n_im))
+    offset = screen(res, seed + 1, 0.5) * tel.pupil
+    rec = dict(m2c=m2c, offset=offset)
+    with _quiet():
+        for tag, kw in (('pp', dict(single_pass=False)), ('sp', dict(single_pass=True))):
+            c0 = InteractionMatrix(ngs, tel, dm, wfs, M2C=m2c, stroke=1e-8, nMeasurements=2, nTrunc=1, **kw)
+            c1 = InteractionMatrix(ngs, tel, dm, wfs, M2C=m2c, stroke=1e-8, nMeasurements=2, nTrunc=1,
+                                   phaseOffset=offset, **kw)
+            rec[tag + '_D'] = np.array(c0.D)
+            rec[tag + '_D_offset'] = np.array(c1.D)
+            rec[tag + '_Mtrunc'] = np.array(c1.Mtrunc)
+    rec['params'] = json.dumps(dict(res=res, n_subap=n_subap, modulation=modulation, light_ratio=light_ratio,
+                                    n_im=n_im))
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **rec)
+    print(name, 'offset changes D by', float(np.abs(rec['pp_D_offset'] - rec['pp_D']).max()))
+
+
 GSC_CASES = [('gsc_tiny', dict(res=24, n_subap=4, modulation=3, n_modes=12)),
              ('gsc_small', dict(res=40, n_subap=10, modulation=2, n_modes=40))]
 
@@ -564,6 +591,8 @@ def main():
         case_options(OOPAO)
     if not only or 'misreg_tiny' in only:
         case_misreg(OOPAO)
+    if not only or 'im_offset_tiny' in only:
+        case_im_offset(OOPAO)
     if not only or any(n in only for n, _ in KL_CASES):
         from refimport import install_kl_shims
         install_kl_shims()
