@@ -133,9 +133,13 @@ class Detector:
 
     @property
     def frame(self):
+        """The last integrated frame, float64 [cam, cam].  After a batch of
+        wavefronts it is the batch's last frame, as in the reference, whose
+        sensor integrates the frames one after the other
+        (OOPAO/Pyramid.py:825-830); ``device_frame`` holds them all."""
         if self._frame_host is None and self._frame_dev is not None:
-            a = self._frame_dev.detach().to('cpu', torch.float64).numpy()
-            self._frame_host = a[0] if a.ndim == 3 and a.shape[0] == 1 else a
+            t = self._frame_dev.detach()
+            self._frame_host = (t[-1] if t.ndim == 3 else t).to('cpu', torch.float64).numpy()
         return self._frame_host
 
     @frame.setter

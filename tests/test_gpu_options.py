@@ -85,6 +85,10 @@ def test_option_case(golden, case):
     dm.coefs = d['coefs2']
     ngs ** tel * dm * wfs
     assert O.rel_l2(wfs.signal, d[name + '_batch_signal']) < TOL
+    # the camera keeps the batch's last frame, as the reference's per-mode integration does
+    frames = wfs.cam.device_frame
+    assert frames.shape[0] == 2 and np.asarray(wfs.cam.frame).shape == frames.shape[1:]
+    assert O.rel_l2(wfs.cam.frame, frames[-1].double().cpu().numpy()) == 0
 
 
 def test_weights_switch_between_single_and_batch(golden):
