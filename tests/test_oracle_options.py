@@ -191,3 +191,26 @@ def test_old_mask_against_quadrant_definition():
         q = m[rows, cols]
         assert np.ptp(np.diff(q, axis=1)) < 1e-12
         assert np.ptp(np.diff(q, axis=0)) < 1e-12
+
+
+@pytest.mark.parametrize('old', [False, True], ids=['faces', 'old_quadrants'])
+@pytest.mark.parametrize('centred', [True, False], ids=['4px', '1px'])
+def test_drop_in_mask_functions_match_the_oracle(old, centred):
+    """The drop-in Pyramid's host mask builders (get_phase_mask,
+    get_phase_mask_old) against the pinned oracle, with face shifts, rooftop
+    and rotation (no GPU needed)."""
+    import types
+    from oopao_gb300.pyramid import Pyramid
+    res, ns, sep, edge = 24, 4, 2, 1
+    sx, sy = [1.0, -0.5, 0.25, 0.0], [0.0, 0.5, -1.0, 0.75]
+    fake = types.SimpleNamespace(telescope=types.SimpleNamespace(resolution=res), nSubap=ns, psfCentering=centred,
+                                 rooftop=0.0 if old else 0.4, theta_rotation=0.0 if old else 0.05,
+                                 n_pix_separation=sep)
+    n = int((ns * 2 + sep + edge * 2) * res / ns)
+    if old:
+        got = Pyramid.get_phase_mask_old(fake, n, ns, sep, edge, psf_centering=centred, sx=sx, sy=sy)
+        want = O.phase_mask_old(res, ns, sep, edge, centred, sx, sy)
+    else:
+        got = Pyramid.get_phase_mask(fake, n, ns, sep, edge, psf_centering=centred, sx=sx, sy=sy)
+        want = O.phase_mask(res, ns, sep, edge, centred, fake.rooftop, fake.theta_rotation, sx, sy)
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-12)
