@@ -48,6 +48,9 @@ def bioedge_masks(res, n_subap, n_pix_separation=2., n_pix_edge=None, grey_width
         A[N // 2 + rl:, N // 2:] = 0.
     B = np.sqrt(1 - A ** 2)
     C, D = A.T.copy(), B.T.copy()
+    # one shift for all four masks (OOPAO/BioEdge.py:361-364)
+    sx = [sx] * 4 if np.isscalar(sx) else sx
+    sy = [sy] * 4 if np.isscalar(sy) else sy
     tts = [-sx[3] * tip * norma + sy[3] * tilt * norma, -sx[2] * tip * norma + sy[2] * tilt * norma,
            -sx[1] * tip * norma + sy[1] * tilt * norma, -sx[0] * tip * norma + sy[0] * tilt * norma]
     base = [A, B, C, D]

@@ -54,3 +54,20 @@ def test_dm_and_screen_measurements(case):
     f, s2d, s = b.measure(d['screen_phase'])
     assert O.rel_l2(f, d['screen_frame']) < TOL
     assert O.rel_l2(s, d['screen_signal']) < TOL
+
+
+@pytest.mark.parametrize('kw', [dict(), dict(grey_width=1.0, quadrants_numbering=(2, 3, 0, 1)),
+                                dict(grey_width=0.5, grey_length=2, sx=[1, 0, -1, 0.5], sy=[0, 1, 0.5, -1]),
+                                dict(sx=0.5, sy=-0.25)],
+                         ids=['plain', 'grey_numbering', 'grey_length_shifts', 'scalar_shift'])
+def test_drop_in_bioedge_masks_match_the_oracle(kw):
+    """The drop-in BioEdge's host mask builder against the pinned oracle (no
+    GPU needed)."""
+    from oopao_gb300.bioedge import bioedge_masks
+    res, ns, sep = 32, 4, 2
+    edge = sep // 2
+    n = int((ns * 2 + sep + edge * 2) * res / ns)
+    zp = n / res
+    got = np.asarray(bioedge_masks(n, res, ns, zp, **kw))
+    want = np.asarray(B.bioedge_masks(res, ns, sep, edge, **kw))
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-12)
