@@ -214,3 +214,35 @@ def test_drop_in_mask_functions_match_the_oracle(old, centred):
         got = Pyramid.get_phase_mask(fake, n, ns, sep, edge, psf_centering=centred, sx=sx, sy=sy)
         want = O.phase_mask(res, ns, sep, edge, centred, fake.rooftop, fake.theta_rotation, sx, sy)
     np.testing.assert_allclose(got, want, rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize('kw', [dict(modulation=3), dict(modulation=2, nTheta_user_defined=12),
+                                dict(modulation=3, delta_theta=0.3, extraModulationFactor=1),
+                                dict(modulation=3, delta_Tip=0.5, delta_Tilt=-0.25),
+                                dict(modulation=0, user_modulation_path=[[1, 0], [0, 1], [-1, 0.5]]),
+                                dict(modulation=0)],
+                         ids=['default', 'user_ntheta', 'delta_extra', 'tip_tilt', 'user_path', 'no_modulation'])
+def test_drop_in_modulation_path_matches_the_oracle(kw):
+    """The drop-in Pyramid's modulation setter (host logic, no GPU) against
+    the pinned oracle's modulation_path."""
+    import types
+    from oopao_gb300.pyramid import Pyramid
+    p = object.__new__(Pyramid)
+    p.telescope = types.SimpleNamespace(resolution=24)
+    p.user_modulation_path = kw.get('user_modulation_path')
+    p.modulation_length = 2 * np.pi
+    p.nTheta_user_defined = kw.get('nTheta_user_defined')
+    p.extraModulationFactor = kw.get('extraModulationFactor', 0)
+    p.delta_theta = kw.get('delta_theta', 0.0)
+    p._delta_Tip = kw.get('delta_Tip', 0.0)
+    p._delta_Tilt = kw.get('delta_Tilt', 0.0)
+    p.isCalibrated = False
+    p._plan = None
+    p.modulation = kw['modulation']
+    want, n_theta = O.modulation_path(kw['modulation'], kw.get('nTheta_user_defined'), p.extraModulationFactor,
+                                      p.delta_theta, p._delta_Tip, p._delta_Tilt, user_path=p.user_modulation_path)
+    assert p.nTheta == n_theta
+    if want is None:
+        assert p.modulation_path is None
+    else:
+        np.testing.assert_allclose(np.asarray(p.modulation_path, dtype=np.float64), want, rtol=0, atol=1e-14)
