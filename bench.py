@@ -66,6 +66,47 @@ def kl_like_basis(modes, pupil, n_modes, diameter=8.0, r0=0.15, L0=25.0):
     return np.ascontiguousarray(_KL_CACHE[key][:, :n_modes])
 
 
+KL_FIXTURE = os.path.join(ROOT, 'tests', 'golden', 'kl_c1.npz')
+ERR_COLS = 32
+
+
+def reference_kl_c1(n_modes):
+    """The first `n_modes` columns of the reference's own KL basis of the
+    21x21 Gaussian DM on the 120 px, 8 m pupil (compute_KL_basis with lim
+    1e-3, piston removed; stored by tests/golden/make_golden.py): 357 x
+    n_modes float64, orthonormal over the pupil (1 m RMS per unit
+    coefficient).  Both arms of the headline use it."""
+    with np.load(KL_FIXTURE) as z:
+        return np.ascontiguousarray(z['m2c'][:, :n_modes])
+
+
+def err_columns(n_modes, n=ERR_COLS, seed=1234):
+    """Seeded, sorted subset of `n` interaction-matrix columns on which the
+    float64 oracle is run (all columns when there are at most `n`)."""
+    if n_modes <= n:
+        return list(range(n_modes))
+    return sorted(int(c) for c in np.random.default_rng(seed).choice(n_modes, n, replace=False))
+
+
+def oracle_im(res, nsub, mod, ntheta, m2c, stroke, cols, threads=None):
+    """Float64 oracle push-pull columns `cols` of M2C at `stroke` (the
+    reference's InteractionMatrix column rule) and its run time."""
+    from oracle import pwfs_oracle as O
+    threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    pup = O.telescope_pupil(res)
+    inten = O.source_intensity(pup, O.n_photon('V0', 8), 1e-3, 8.0)
+    ow = O.build_pyramid(res, nsub, mod, 0.5, inten, n_theta_user=ntheta, workers=threads)
+    D = O.interaction_matrix(ow, O.dm_modes(res, 8.0, nsub), m2c[:, cols], stroke, O.PHOTOMETRY['V0'][0], pup,
+                             single_pass=False, workers=threads)
+    return D, time.perf_counter() - t0
+
+
+def rel_fro(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
 def build_system(dev_index, res=RES, nsub=NSUB, mod=MOD, ntheta=NTHETA, max_batch=100, if_dtype='fp32'):
     import oopao_gb300 as og
     with _quiet():
@@ -89,9 +130,13 @@ def _timed(fn):
 
 def im_comparison(tel, ngs, dm, wfs, m2c, n_per_mode, with_error=True):
     """Interaction-matrix build times of one system: the plain per-mode
-    push-pull GPU path (operator path ngs**tel*dm*wfs per mode, timed on
-    `n_per_mode` modes and scaled to all), the batched push-pull path and
-    the batched tangent (JVP) path; JVP error against a float64 derivative."""
+    push-pull GPU path (operator path ngs**tel*dm*wfs per mode; its time is
+    measured on the first `n_per_mode` modes and scaled linearly to all
+    modes), the batched push-pull path and the batched tangent (JVP) path.
+    Errors are relative Frobenius norms over ERR_COLS seeded columns (named
+    in the output): the batched push-pull matrix against the float64 oracle
+    at the same stroke, the tangent matrix against a float64 derivative (the
+    oracle's push-pull at 1e-12 m)."""
     from oopao_gb300.calibration import InteractionMatrix
     from oopao_gb300.autodiff import jvp_interaction_matrix
     n_modes = m2c.shape[1]
@@ -99,34 +144,39 @@ def im_comparison(tel, ngs, dm, wfs, m2c, n_per_mode, with_error=True):
     _, t_pm = _timed(lambda: InteractionMatrix(ngs, tel, dm, wfs, m2c[:, :n_per_mode], STROKE, single_pass=False,
                                                method='per_mode', invert=False))
     InteractionMatrix(ngs, tel, dm, wfs, m2c[:, :8], STROKE, single_pass=False, method='batched', invert=False)
-    _, t_b = _timed(lambda: InteractionMatrix(ngs, tel, dm, wfs, m2c, STROKE, single_pass=False,
-                                              method='batched', invert=False))
+    Db, t_b = _timed(lambda: InteractionMatrix(ngs, tel, dm, wfs, m2c, STROKE, single_pass=False,
+                                               method='batched', invert=False))
     jvp_interaction_matrix(ngs, tel, dm, wfs, m2c[:, :8])
     D, t_j = _timed(lambda: jvp_interaction_matrix(ngs, tel, dm, wfs, m2c))
     out = {'modes': n_modes, 'per_mode_push_pull_ms': t_pm / n_per_mode * n_modes * 1000.0,
+           'per_mode_push_pull_note': 'measured on %d modes, scaled linearly to %d' % (n_per_mode, n_modes),
            'per_mode_timed_modes': n_per_mode, 'batched_push_pull_ms': t_b * 1000.0, 'jvp_ms': t_j * 1000.0}
     out['jvp_speedup_vs_per_mode_push_pull'] = out['per_mode_push_pull_ms'] / out['jvp_ms']
     out['batched_speedup_vs_per_mode_push_pull'] = out['per_mode_push_pull_ms'] / out['batched_push_pull_ms']
     if with_error:
-        from oracle import pwfs_oracle as O
-        res, nsub = tel.resolution, dm.nActAlongDiameter
-        inten = O.source_intensity(O.telescope_pupil(res), O.n_photon('V0', 8), 1e-3, 8.0)
-        ow = O.build_pyramid(res, nsub, wfs.modulation, 0.5, inten, n_theta_user=wfs.nTheta,
-                             workers=os.cpu_count())
-        Dref = O.interaction_matrix(ow, O.dm_modes(res, 8.0, nsub), m2c[:, :2], 1e-12, ngs.wavelength,
-                                    O.telescope_pupil(res), single_pass=False, workers=os.cpu_count())
-        out['jvp_rel_fro_err_vs_fp64_2cols'] = O.rel_l2(D[:, :2].double().cpu().numpy(), Dref)
+        res, nsub, k = tel.resolution, int(round(dm.nActAlongDiameter)), wfs.nTheta
+        cols = err_columns(n_modes)
+        Dd, t1 = oracle_im(res, nsub, wfs.modulation, k, m2c, 1e-12, cols)
+        Dp, t2 = oracle_im(res, nsub, wfs.modulation, k, m2c, STROKE, cols)
+        out['error_columns'] = cols
+        out['jvp_rel_fro_err_vs_fp64_derivative'] = rel_fro(D[:, cols].double().cpu().numpy(), Dd)
+        out['batched_rel_fro_err_vs_fp64_push_pull'] = rel_fro(np.asarray(Db.D)[:, cols], Dp)
+        out['oracle_seconds'] = t1 + t2
     return out
 
 
-def cl_rate(n_steps=2000):
+def cl_rate(n_steps=2000, n_oracle=20):
     """Graph-replayed closed-loop steps/s on the 40x40 configuration: 240 px,
     N=504, modulation 5 l/D x 96 points, 41x41 DM, 3-layer infinite phase
     screens (r0 0.12 m, L0 30 m, 0/5/10 km, 10/15/20 m/s, updated on the GPU
     inside the captured step), 1000-mode KL integrator (gain 0.4,
     delay 1, reconstructor M2C @ M from the JVP interaction matrix and its
     full FP64 pseudo-inverse); BF16 tensor-core IF projection with FP32
-    accumulation.  Reports the replay rate and the residual of the loop."""
+    accumulation.  Reports the replay rate and the residual of the loop, and
+    the error against the float64 oracle loop (same reconstructor, the
+    float64 restatement of the same seeded infinite screens) over the first
+    `n_oracle` frames: slopes of every frame, residual WFE trajectory,
+    long-exposure PSF and Strehl ratio, final commands."""
     import torch
     from oopao_gb300.autodiff import jvp_interaction_matrix
     from oopao_gb300.calibration import CalibrationVault
@@ -168,15 +218,62 @@ def cl_rate(n_steps=2000):
     dm.separable_projection = False
     ms_dense, wfe_dense = timed_loop('cl_steps_dense_dm')
     dm.separable_projection = path == 'separable'
+    oracle = cl_oracle_error(tel, ngs, dm, wfs, R, atm, n_oracle,
+                             (0.12, 30.0, [1 / 3, 1 / 3, 1 / 3], [10., 15., 20.], [0., 72., 144.],
+                              [0., 5000., 10000.]))
     return {'config': '40x40 PWFS, 240 px, N=504, 96 points, 41x41 DM (%d act), 3 infinite-screen layers, '
                       '1000 KL modes'
-                      % dm.nValidAct,
+                      % dm.nValidAct, 'fp64_oracle': oracle,
             'steps': n_steps, 'us_per_step': ms * 1000.0, 'khz': 1.0 / ms,
             'graph': True, 'variant': int(N_variant(wfs)), 'dm': path,
             'us_per_step_dense_bf16_dm': ms_dense * 1000.0,
             'wfe_rel_diff_dense_vs_default': float(np.linalg.norm(wfe_dense - wfe) / np.linalg.norm(wfe)),
             'tc_status': dm.tensor_core_status(), 'wfe_first_nm': float(wfe[0] * 1e9),
             'wfe_mean_last_500_nm': float(wfe[-500:].mean() * 1e9)}
+
+
+def cl_oracle_error(tel, ngs, dm, wfs, R, atm, n_oracle, atm_params, gain=0.4):
+    """Run `n_oracle` eager steps of the GPU loop (science PSF on) and the
+    float64 oracle loop on the same reconstructor and the float64
+    restatement of the same seeded atmosphere; relative L2 errors of the
+    per-frame slopes, the residual WFE trajectory, the long-exposure PSF, the
+    final commands and the Strehl ratio."""
+    import torch
+    from oopao_gb300.closed_loop import ClosedLoop
+    from oracle import atm_oracle as A
+    from oracle import pwfs_oracle as O
+    res, nsub = tel.resolution, int(round(dm.nActAlongDiameter))
+    cl = ClosedLoop(tel, ngs, dm, wfs, R, gain=gain, layers=atm, max_steps=n_oracle + 10, science=True)
+    sig = []
+    for _ in range(n_oracle):
+        cl.step()
+        sig.append(cl.s[0].double().cpu().numpy())
+    torch.cuda.synchronize()
+    wfe, psf, sr = cl.residual_wfe, cl.long_exposure_psf(), cl.long_exposure_strehl()
+    coefs = cl.coefs.double().cpu().numpy()
+    del cl
+    t0 = time.perf_counter()
+    pup = O.telescope_pupil(res)
+    inten = O.source_intensity(pup, O.n_photon('V0', 8), 1e-3, 8.0)
+    ow = O.build_pyramid(res, nsub, wfs.modulation, 0.5, inten, n_theta_user=wfs.nTheta, workers=os.cpu_count())
+    r0, L0, fr, ws, wd, alt = atm_params
+    ora = A.OracleAtmosphere(res, tel.D, 1e-3, r0, L0, fr, ws, wd, alt)
+
+    def turbulence(t):
+        ora.update()            # step t sees the atmosphere after t + 1 updates
+        return ora.opd
+
+    ref = O.closed_loop(ow, O.dm_modes(res, tel.D, nsub), np.asarray(R, np.float64), turbulence, pup,
+                        ngs.wavelength, gain, n_oracle, workers=os.cpu_count(), record_signals=True)
+    sig = np.stack(sig)
+    per_frame = [O.rel_l2(sig[t], ref['signals'][t]) for t in range(n_oracle)]
+    return {'frames': n_oracle, 'oracle_seconds': time.perf_counter() - t0,
+            'signal_rel_l2': O.rel_l2(sig, ref['signals']), 'signal_rel_l2_max_frame': max(per_frame),
+            'wfe_rel_l2': O.rel_l2(wfe, ref['wfe']), 'psf_le_rel_l2': O.rel_l2(psf, ref['psf_le']),
+            'commands_rel_l2': O.rel_l2(coefs, ref['coefs']),
+            'strehl_le_pct': sr, 'oracle_strehl_le_pct': ref['strehl_le'],
+            'strehl_rel_err': abs(sr - ref['strehl_le']) / ref['strehl_le'],
+            'wfe_nm_first_last': [float(wfe[0] * 1e9), float(wfe[-1] * 1e9)]}
 
 
 def cl_strehl(n_steps=500, n_oracle=100):
@@ -663,50 +760,76 @@ def kernel_bytes(kernel, res, n, cam, units, items, launches):
 KERNELS = ['pwfs_rows_fwd', 'pwfs_cols', 'pwfs_rows_inv', 'pwfs_bin']
 
 
-def cpu_oracle_rate(budget_s=12.0, min_frames=4, threads=None):
+def headline_config():
+    """`config` of the headline JSON line, the same for both arms."""
+    return {'workload': WORKLOAD, 'modes': NMODES, 'frames_per_im': 2 * NMODES, 'modulation_points': NTHETA,
+            'fft_grid': 264, 'camera': 44, 'stroke_m': STROKE,
+            'basis': "the reference's KL basis of the 21x21 DM (tests/golden/kl_c1.npz), first %d modes" % NMODES,
+            'l2': 'intermediates (>=2.4 GB per launch) exceed L2; no flush needed'}
+
+
+def cpu_oracle_rate(m2c, budget_s=12.0, min_frames=4, threads=None, modes_per_step=None, seed=7):
     """Oracle (float64 numpy/scipy port of the reference) push-pull frames/s on
-    the host cores for a bounded sample of the workload."""
+    the host cores for a bounded sample of the workload: seeded columns of
+    the same M2C, two frames each.  Either runs for `budget_s` seconds or, with
+    `modes_per_step`, exactly that many modes.  Returns
+    (frames/s, frames, seconds, threads)."""
     from oracle import pwfs_oracle as O
     threads = threads or os.cpu_count() or 1
     inten = O.source_intensity(O.telescope_pupil(RES), O.n_photon('V0', 8), 1e-3, 8.0)
     wfs = O.build_pyramid(RES, NSUB, MOD, 0.5, inten, n_theta_user=NTHETA, workers=threads)
     modes = O.dm_modes(RES, 8.0, NSUB)
     pupil = O.telescope_pupil(RES)
-    m2c = kl_like_basis(modes, pupil, 8)
     lam = O.PHOTOMETRY['V0'][0]
-    frames, t0 = 0, time.perf_counter()
-    m = 0
+    order = np.random.default_rng(seed).permutation(m2c.shape[1])
+    frames, t0, m = 0, time.perf_counter(), 0
     while True:
-        O.interaction_matrix(wfs, modes, m2c[:, m % 8:m % 8 + 1], STROKE, lam, pupil, single_pass=False,
+        c = int(order[m % len(order)])
+        O.interaction_matrix(wfs, modes, m2c[:, c:c + 1], STROKE, lam, pupil, single_pass=False,
                              workers=threads)
         frames += 2
         m += 1
         el = time.perf_counter() - t0
-        if frames >= min_frames and el >= budget_s:
+        if modes_per_step is not None:
+            if m >= modes_per_step:
+                break
+        elif frames >= min_frames and el >= budget_s:
             break
     return frames / el, frames, el, threads
 
 
+REF_MODES_PER_STEP = 8
+
+
 def run_reference(args):
+    """Reference arm: the float64 oracle port of the reference's push-pull
+    interaction-matrix loop on the host cores.  One step = REF_MODES_PER_STEP
+    seeded modes of the same 300-mode KL basis (2 frames each), timed whole;
+    `value` = frames over the K timed steps / their wall time."""
     rank = int(os.environ.get('RANK', '0'))
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    rates = []
+    m2c = reference_kl_c1(NMODES)
+    times, frames = [], 0
     for i in range(args.warmup + args.steps):
-        r, frames, el, thr = cpu_oracle_rate(budget_s=1.0, min_frames=2, threads=threads)
+        r, fr, el, thr = cpu_oracle_rate(m2c, threads=threads, modes_per_step=REF_MODES_PER_STEP, seed=100 + i)
         if i >= args.warmup:
-            rates.append(r)
-    v = statistics.median(rates)
+            times.append(el)
+            frames += fr
+    total = sum(times)
+    v = frames / total
     line = {
         'metric': 'PWFS frames/s (batched IM build)', 'value': v, 'unit': 'frames/s',
         'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
-        'ms_per_step': 1000.0 * 2 * NMODES / v, 'higher_is_better': True, 'scaling': 'weak',
+        'ms_per_step': 1000.0 * total / args.steps, 'frames_per_step': 2 * REF_MODES_PER_STEP,
+        'higher_is_better': True, 'scaling': 'weak',
         'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'impl': 'reference',
-        'config': {'workload': WORKLOAD, 'sample': 'per step: 1 s of push-pull modes (2 frames each)'},
+        'config': headline_config(),
         'cpu_baseline': {'value': v, 'unit': 'frames/s', 'cores': threads, 'kind': 'port',
-                         'sample': 'push-pull IM columns, >=1 s per step, float64 oracle, scipy.fft workers=%d'
-                                   % threads},
+                         'sample': 'per step: %d seeded push-pull modes (%d frames) of the %d-mode basis, '
+                                   'float64 oracle, scipy.fft workers=%d'
+                                   % (REF_MODES_PER_STEP, 2 * REF_MODES_PER_STEP, NMODES, threads)},
         'e2e': {'value': v, 'unit': 'frames/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
     }
     print(json.dumps(line))
@@ -724,7 +847,7 @@ def run_ours(args):
     from oopao_gb300 import _native as N
     from oopao_gb300.calibration import InteractionMatrix, _signals_batched
     tel, ngs, dm, wfs = build_system(local)
-    m2c = kl_like_basis(dm.modes, tel.pupil, NMODES)
+    m2c = reference_kl_c1(NMODES)
     dev = wfs._dev
     m2c_dev = torch.as_tensor(m2c.astype(np.float32), device=dev)
     n, cam, k = wfs.resolution, wfs._cam_eff, wfs.nTheta
@@ -823,28 +946,25 @@ def run_ours(args):
     # ---- reported CPU baseline (rank 0, N=1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        r, frames, el, thr = cpu_oracle_rate()
+        r, frames, el, thr = cpu_oracle_rate(m2c)
         cpu = {'value': r, 'unit': 'frames/s', 'cores': thr, 'kind': 'port',
-               'sample': '%d push-pull frames (%d KL modes) in %.1f s, float64 oracle, '
+               'sample': '%d push-pull frames (%d seeded modes of the same basis) in %.1f s, float64 oracle, '
                          'scipy.fft workers=%d' % (frames, frames // 2, el, thr)}
 
-    # accuracy of this step's IM against the float64 oracle on 2 columns
+    # accuracy of this step's IM against the float64 oracle on seeded columns
     err = None
     if rank == 0 and not args.no_cpu:
-        from oracle import pwfs_oracle as O
-        inten = O.source_intensity(O.telescope_pupil(RES), O.n_photon('V0', 8), 1e-3, 8.0)
-        ow = O.build_pyramid(RES, NSUB, MOD, 0.5, inten, n_theta_user=NTHETA, workers=os.cpu_count())
-        Dref = O.interaction_matrix(ow, O.dm_modes(RES, 8.0, NSUB), m2c[:, :2], STROKE,
-                                    ngs.wavelength, O.telescope_pupil(RES), single_pass=False,
-                                    workers=os.cpu_count())
-        err = O.rel_l2(D[:, :2].double().cpu().numpy(), Dref)
+        cols = err_columns(NMODES)
+        Dref, t_or = oracle_im(RES, NSUB, MOD, NTHETA, m2c, STROKE, cols)
+        err = {'rel_fro': rel_fro(D[:, cols].double().cpu().numpy(), Dref), 'columns': cols,
+               'oracle_seconds': t_or}
 
     extra = {}
     if rank == 0 and world == 1 and not args.no_extra:
         extra['im_c1_300'] = im_comparison(tel, ngs, dm, wfs, m2c, n_per_mode=30)
         tel3, ngs3, dm3, wfs3 = build_system(0, 240, 40, 5, 96, max_batch=16)
         autotune.tune_pyramid(wfs3, batch=16)
-        m2c3 = kl_like_basis(dm3.modes, tel3.pupil, 1000)
+        m2c3 = kl_like_basis(dm3.modes, tel3.pupil, 1000, r0=0.12, L0=30.0)
         extra['im_c3_1000'] = im_comparison(tel3, ngs3, dm3, wfs3, m2c3, n_per_mode=10)
         del tel3, ngs3, dm3, wfs3
         extra['cl_step'] = cl_rate()
@@ -865,10 +985,9 @@ def run_ours(args):
             'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms_step,
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
             'data': 'synthetic (seeded KL basis, Gaussian IFs)',
-            'config': {'workload': WORKLOAD, 'frames_per_step': frames_step, 'modulation_points': k,
-                       'fft_grid': n, 'camera': cam, 'batch_per_launch': wfs.max_batch,
-                       'l2': 'intermediates (>=2.4 GB per launch) exceed L2; no flush needed',
-                       'im_rel_fro_err_vs_fp64_oracle_2cols': err},
+            'frames_per_step': frames_step, 'batch_per_launch': wfs.max_batch,
+            'config': headline_config(),
+            'im_rel_fro_err_vs_fp64_oracle': err,
             'roofline': {'bound': 'hbm', 'kernel': top, 'variant': variant, 'achieved': achieved, 'peak': peak,
                          'unit': 'GB/s', 'frac': achieved / peak, 'peak_kind': peak_kind,
                          'traffic': traffic, 'kernel_share': share,

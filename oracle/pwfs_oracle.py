@@ -652,31 +652,37 @@ def strehl_meter(psf: np.ndarray, psf_ref: np.ndarray) -> float:
 
 def closed_loop(wfs: OraclePyramid, modes: np.ndarray, reconstructor: np.ndarray, turbulence_opd,
                 pupil: np.ndarray, wavelength: float, gain: float, n_steps: int, frame_delay: int = 1,
-                science: bool = True, workers: int = 1) -> dict:
+                science: bool = True, workers: int = 1, record_signals: bool = False) -> dict:
     """The loop of ``tutorials/AO_closed_loop_Pyramid_WFS.py:601-639`` in
     float64: at step t the residual OPD = turbulence_opd(t) + modes @ coefs;
     its standard deviation over the pupil is logged; the sensor measures it;
     coefs -= gain * R @ s_t (frame delay 1) or R @ s_{t-1} (delay 2).  With
     ``science``, the science PSF of every residual is summed and the
-    long-exposure Strehl ratio is returned with the flat-wavefront PSF."""
+    long-exposure Strehl ratio is returned with the flat-wavefront PSF.  With
+    ``record_signals``, the slopes of every step are returned too."""
     res = pupil.shape[0]
     coefs = np.zeros(modes.shape[1])
     s_prev = np.zeros(reconstructor.shape[1])
     ip = pupil > 0
     wfe = np.zeros(n_steps)
     psf_le = 0.0
+    signals = []
     for t in range(n_steps):
         opd = turbulence_opd(t) + (modes @ coefs).reshape(res, res)
         wfe[t] = np.std(opd[ip])
         if science:
             psf_le = psf_le + science_psf(opd, wfs.intensity, pupil, wavelength)
         _, _, _, s = wfs.measure(opd * 2 * np.pi / wavelength, workers=workers)
+        if record_signals:
+            signals.append(s)
         if frame_delay == 1:
             coefs = coefs - gain * reconstructor @ s
         else:
             coefs = coefs - gain * reconstructor @ s_prev
             s_prev = s
     out = {'wfe': wfe, 'coefs': coefs}
+    if record_signals:
+        out['signals'] = np.stack(signals)
     if science:
         ref = science_psf(np.zeros((res, res)), wfs.intensity, pupil, wavelength)
         out.update(psf_le=psf_le, psf_ref=ref, strehl_le=strehl_meter(psf_le, ref))

@@ -2,7 +2,9 @@
 
 Run in a container that holds the reference source tree:
 
-    python tests/golden/make_golden.py [/path/to/OOPAO/project]
+    python tests/golden/make_golden.py /path/to/OOPAO/project [case ...]
+
+(or with the project root in the environment variable OOPAO_REFERENCE).
 
 It imports the reference through ``refimport.import_reference`` (display and
 I/O dependencies stubbed), builds Telescope / Source / DeformableMirror /
@@ -293,6 +295,56 @@ def case_kl(OOPAO, name, res, n_subap, r0=0.15, L0=25.0):
     print(name, 'M2C', rec['m2c'].shape)
 
 
+def case_c3(OOPAO, name='c3', n_kl=24, r0=0.12, L0=30.0):
+    """The 40x40 closed-loop optics: 8 m, 240 px, 40x40 pyramid, modulation
+    5 l/D with 96 points, N = 504, 84x84 camera, 41x41 Gaussian DM (coupling
+    0.35).  Geometry, valid pixels, reference slopes, one DM shape and one
+    seeded screen measured through the reference's own Pyramid, and push-pull
+    interaction-matrix columns (stroke 1e-8, nMeasurements 1) of the first
+    `n_kl` modes of the reference's compute_KL_basis (r0 0.12 m, L0 30 m,
+    lim 1e-3, piston removed).  The 504 x 504 focal image is not stored."""
+    import json
+    from refimport import install_kl_shims
+    install_kl_shims()
+    from OOPAO.Atmosphere import Atmosphere
+    from OOPAO.calibration.InteractionMatrix import InteractionMatrix
+    from OOPAO.calibration.compute_KL_modal_basis import compute_KL_basis
+    res, n_subap, modulation, light_ratio = 240, 40, 5, 0.5
+    tel, ngs, dm, wfs = build(OOPAO, res, n_subap, modulation, light_ratio, nTheta_user_defined=96)
+    rec = geometry_record(tel, ngs, dm, wfs)
+    rec['params'] = json.dumps(dict(res=res, n_subap=n_subap, modulation=modulation, light_ratio=light_ratio,
+                                    nTheta_user_defined=96, n_kl=n_kl, r0=r0, L0=L0))
+    coefs = np.random.default_rng(31).standard_normal(dm.nValidAct) * 60e-9
+    out = measure_dm(tel, ngs, dm, wfs, coefs)
+    rec['dm_coefs'] = coefs
+    for k, v in out.items():
+        if k not in ('raw', 'focal'):
+            rec['dm_' + k] = v
+    ph = screen(res, 32, 2.0) * tel.pupil
+    out = measure_phase(tel, ngs, dm, wfs, ph)
+    rec['screen_phase'] = ph
+    for k, v in out.items():
+        if k != 'raw':
+            rec['screen_' + k] = v
+    with _quiet():
+        atm = Atmosphere(telescope=tel, r0=r0, L0=L0, fractionalR0=[1.0], windSpeed=[10.], windDirection=[0.],
+                         altitude=[0.])
+        m2c = np.asarray(compute_KL_basis(tel, atm, dm, lim=1e-3, remove_piston=True))[:, :n_kl]
+        dm.coefs = 0
+        ngs ** tel
+        calib_pp = InteractionMatrix(ngs, tel, dm, wfs, M2C=m2c, stroke=1e-8, nMeasurements=1,
+                                     single_pass=False)
+    rec['im_m2c'] = m2c
+    rec['im_pp_D'] = np.array(calib_pp.D)
+    rec['modes_colsum'] = dm.modes.sum(axis=0)
+    rec['modes_sq'] = float((dm.modes ** 2).sum())
+    rec['mask_row0'] = np.array(wfs.mask[0])
+    rec['mask_col_mid'] = np.array(wfs.mask[:, wfs.resolution // 2 - 3])
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **rec)
+    print(name, 'N', rec['N'], 'cam', rec['cam'], 'K', rec['n_theta'], 'nSignal', rec['n_signal'],
+          'nAct', rec['n_act'], 'IM', rec['im_pp_D'].shape)
+
+
 POSTPROCESSING_MODES = ['slopesMaps', 'slopesMaps_incidence_flux', 'slopesMaps_camera_flux', 'fullFrame_camera_flux',
                         'fullFrame_incidence_flux', 'fullFrame_sum_flux', 'fullFrame']
 
@@ -567,10 +619,15 @@ CASES = [
 
 
 def main():
-    """argv: [reference project root] [case names...] (default: every case)."""
+    """argv: reference project root (or $OOPAO_REFERENCE), then case names (default: every case)."""
     from refimport import import_reference
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
-    only = set(sys.argv[2:])
+    args = sys.argv[1:]
+    if args and os.path.isdir(os.path.join(args[0], 'OOPAO')):
+        ref_root, only = args[0], set(args[1:])
+    else:
+        ref_root, only = os.environ.get('OOPAO_REFERENCE'), set(args)
+    if not ref_root:
+        raise SystemExit('usage: make_golden.py REFERENCE_ROOT [case ...] (or set OOPAO_REFERENCE)')
     OOPAO = import_reference(ref_root)
     for name, args, kw in CASES:
         if not only or name in only:
@@ -579,6 +636,8 @@ def main():
         case_atmosphere(OOPAO)
     if not only or 'c5_screen' in only:
         case_large(OOPAO)
+    if not only or 'c3' in only:
+        case_c3(OOPAO)
     for name, args, kw in BIOEDGE_CASES:
         if not only or name in only:
             case_bioedge(OOPAO, name, *args, **kw)

@@ -98,18 +98,27 @@ def install_kl_shims():
     sys.modules['numexpr'] = numexpr
 
 
-def import_reference(ref_root='/root/reference', work='/tmp/OOPAO_refcopy'):
-    """Return the imported ``OOPAO`` package from a stubbed copy of ``ref_root``."""
+def import_reference(ref_root, work=None):
+    """Return the imported ``OOPAO`` package from a stubbed copy of ``ref_root``
+    (the reference project root, which holds ``OOPAO/``).  The copy goes to a
+    fresh temporary directory (or to `work`, which must not exist yet), so a
+    copy of older reference sources is never reused."""
     if 'OOPAO' in sys.modules:
         return sys.modules['OOPAO']
+    if not ref_root or not os.path.isdir(os.path.join(ref_root, 'OOPAO')):
+        raise SystemExit('reference project root without an OOPAO/ package: %r' % (ref_root,))
+    if work is None:
+        import tempfile
+        work = tempfile.mkdtemp(prefix='OOPAO_refcopy_')
     dst = os.path.join(work, 'OOPAO')
-    if not os.path.isdir(dst):
-        os.makedirs(work, exist_ok=True)
-        shutil.copytree(os.path.join(ref_root, 'OOPAO'), dst)
-        for root, dirs, files in os.walk(dst):
-            os.chmod(root, 0o755)
-            for f in files:
-                os.chmod(os.path.join(root, f), 0o644)
+    if os.path.exists(dst):
+        raise SystemExit('%s exists: give a fresh directory' % dst)
+    os.makedirs(work, exist_ok=True)
+    shutil.copytree(os.path.join(ref_root, 'OOPAO'), dst)
+    for root, dirs, files in os.walk(dst):
+        os.chmod(root, 0o755)
+        for f in files:
+            os.chmod(os.path.join(root, f), 0o644)
     for name in _STUBS:
         if name not in sys.modules:
             sys.modules[name] = _StubModule(name)
