@@ -334,8 +334,13 @@ def case_c3(OOPAO, name='c3', n_kl=24, r0=0.12, L0=30.0):
         ngs ** tel
         calib_pp = InteractionMatrix(ngs, tel, dm, wfs, M2C=m2c, stroke=1e-8, nMeasurements=1,
                                      single_pass=False)
+        # the float64 derivative: the same push-pull with a stroke 1000x
+        # smaller, whose O(stroke^2) truncation is ~1e-6 of the 1e-8 m one
+        calib_fine = InteractionMatrix(ngs, tel, dm, wfs, M2C=m2c, stroke=1e-11, nMeasurements=1,
+                                       single_pass=False)
     rec['im_m2c'] = m2c
     rec['im_pp_D'] = np.array(calib_pp.D)
+    rec['im_fine_D'] = np.array(calib_fine.D)
     rec['modes_colsum'] = dm.modes.sum(axis=0)
     rec['modes_sq'] = float((dm.modes ** 2).sum())
     rec['mask_row0'] = np.array(wfs.mask[0])

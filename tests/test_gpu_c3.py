@@ -6,7 +6,8 @@ Gaussian DM), through the drop-in classes ``ngs**tel*dm*wfs``,
 
 Tolerances (FP32 path): relative L2 <= 1e-5 for frames, signal_2D and
 signal; identical valid-pixel maps; push-pull IM columns (stroke 1e-8 m, a
-difference of O(1) slopes) <= 1e-4 relative Frobenius over all 24 columns.
+difference of O(1) slopes) <= 1e-4 relative Frobenius over all 24 columns;
+the tangent IM <= 1e-4 against the reference's float64 derivative.
 """
 import contextlib
 import io
@@ -83,9 +84,13 @@ def test_push_pull_interaction_matrix(c3, method):
 
 def test_tangent_interaction_matrix(c3):
     """The interaction matrix from batched tangents (JVPs) against the
-    reference's push-pull columns: a derivative against a +-1e-8 m finite
-    difference, so the bound is the stroke's truncation, not round-off."""
+    reference's float64 derivative (its own push-pull with a 1e-11 m stroke,
+    whose O(stroke^2) truncation is ~1e-9 relative): <= 1e-4 relative
+    Frobenius over all 24 columns.  Against the reference's 1e-8 m push-pull
+    the distance is that stroke's own truncation, 3.1e-3 between the
+    reference's two strokes, so the bound there is 4e-3."""
     d, (tel, ngs, dm, wfs) = c3
     from oopao_gb300.autodiff import jvp_interaction_matrix
     D = jvp_interaction_matrix(ngs, tel, dm, wfs, d['im_m2c']).double().cpu().numpy()
-    assert O.rel_l2(D, d['im_pp_D']) < 2e-3
+    assert O.rel_l2(D, d['im_fine_D']) < 1e-4
+    assert O.rel_l2(D, d['im_pp_D']) < 4e-3
