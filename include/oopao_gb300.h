@@ -105,6 +105,20 @@ int oopao_pwfs_get_variant(const oopao_pwfs_plan* plan);
 int oopao_pwfs_num_variants(const oopao_pwfs_plan* plan);
 int oopao_pwfs_variant_info(const oopao_pwfs_plan* plan, int variant, int* info);
 
+/* Two-pass propagation for masks that factorise per axis.  The reference's
+ * single path (pyramid_transform, OOPAO/Pyramid.py:612-646) applies the
+ * N x N mask between full 2-D transforms; when the plan's mask equals
+ * mcol[r] * mrow[c] within float32 rounding (the four-face mask with one
+ * shift for all faces, no rooftop, no rotation: OOPAO/Pyramid.py:453-480)
+ * the filter splits into a row filter shared by the points with equal x_k
+ * and a column filter per point, and oopao_pwfs_measure / oopao_pwfs_jvp run
+ * two passes instead of three.  Same results within float32 round-off.
+ * set_separable(plan, 0) forces the three-pass path (1, the default, uses
+ * the two passes whenever they apply); separable() returns 1 when a measure
+ * call without a focal-plane frame takes the two-pass path, else 0. */
+int oopao_pwfs_set_separable(oopao_pwfs_plan* plan, int enable);
+int oopao_pwfs_separable(const oopao_pwfs_plan* plan);
+
 /* Bytes of device workspace oopao_pwfs_measure needs for `batch` items
  * processed in one chunk (a smaller workspace makes it loop over chunks;
  * it must hold at least one item). */

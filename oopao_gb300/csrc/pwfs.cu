@@ -104,6 +104,13 @@ struct oopao_pwfs_plan {
   int n_masks;                    // Fourier masks measured together (1, or Bi-O Edge's 4)
   float2* d_masks;                // [n_masks][n][n] when n_masks > 1
   int* d_err;                     // device error word (bounded waits of the persistent column pass)
+  // two-pass path for a mask that factorises per axis (pwfs_sep.cuh)
+  const struct SepPasses* sep;    // compile-time two-pass plan for n, or null
+  bool mask_sep;                  // mask == mcol (x) mrow within float32 rounding
+  bool sep_on;                    // oopao_pwfs_set_separable (default on)
+  float2* d_mrow;                 // [n] factor along a row (column frequency)
+  float2* d_mcol;                 // [n] factor along a column (row frequency)
+  int sep_cols_ctas;              // resident column-pass CTAs on this device
   // signal processing
   int sp_mode, nq, n2d, n_signal, cam2;
   int q_r0[4], q_c0[4];
@@ -274,6 +281,7 @@ __global__ void __launch_bounds__(kThreads) pwfs_rows_inv(RowsInvArgs a) {
 }
 
 #include "pwfs_fast.cuh"
+#include "pwfs_sep.cuh"
 namespace {
 // Compile-time plans (N = R1*R2, T threads per line, lines per CTA of the
 // three passes).  Sizes without an entry use the generic kernels.
@@ -612,7 +620,78 @@ void free_plan(oopao_pwfs_plan* p) {
   cudaFree(p->d_sig_index);
   cudaFree(p->d_err);
   cudaFree(p->d_masks);
+  cudaFree(p->d_mrow);
+  cudaFree(p->d_mcol);
   free(p);
+}
+
+// Rank-one factorisation M[r][c] = mcol[r] * mrow[c] of an n x n complex
+// mask: pivot on the entry of largest modulus, mrow = the pivot's row,
+// mcol = the pivot's column / pivot.  Accepted when the float32 factors
+// reproduce every entry within 1e-6 of max|M| (the mask itself is stored in
+// complex64, ~6e-8 rounding).  The reference's four-face mask factorises
+// whenever the faces share one shift and there is no rooftop or rotation.
+bool factor_mask(const float2* m, int n, std::vector<float2>* mrow, std::vector<float2>* mcol) {
+  const size_t nn = (size_t)n * n;
+  size_t piv = 0;
+  double best = -1.0;
+  for (size_t i = 0; i < nn; i++) {
+    const double a = (double)m[i].x * m[i].x + (double)m[i].y * m[i].y;
+    if (a > best) { best = a; piv = i; }
+  }
+  if (!(best > 0.0)) return false;
+  const int r0 = (int)(piv / n), c0 = (int)(piv % n);
+  const double pr = m[piv].x, pi = m[piv].y, pa = pr * pr + pi * pi;
+  mrow->resize(n);
+  mcol->resize(n);
+  for (int c = 0; c < n; c++) (*mrow)[c] = m[(size_t)r0 * n + c];
+  for (int r = 0; r < n; r++) {
+    const double ar = m[(size_t)r * n + c0].x, ai = m[(size_t)r * n + c0].y;
+    (*mcol)[r] = make_float2((float)((ar * pr + ai * pi) / pa), (float)((ai * pr - ar * pi) / pa));
+  }
+  const double tol = 1e-6 * sqrt(best);
+  for (int r = 0; r < n; r++) {
+    const double ur = (*mcol)[r].x, ui = (*mcol)[r].y;
+    for (int c = 0; c < n; c++) {
+      const double vr = (*mrow)[c].x, vi = (*mrow)[c].y;
+      const float2 e = m[(size_t)r * n + c];
+      const double dr = ur * vr - ui * vi - e.x, di = ur * vi + ui * vr - e.y;
+      if (dr * dr + di * di > tol * tol) return false;
+    }
+  }
+  return true;
+}
+
+// Two-pass set-up for mask 0 of the plan: factorise it, upload the factors
+// and opt the kernels into their shared memory.  A mask that does not
+// factorise (or an n without a two-pass plan) leaves mask_sep false.
+cudaError_t sep_setup(oopao_pwfs_plan* p, const float* mask_host) {
+  p->mask_sep = false;
+  // 16-byte tile copies need an even pupil; the column pass must fit in shared memory
+  if (!p->sep || p->res % 2 || p->sep->smem_cols(p->res) > kSmemLimit) return cudaSuccess;
+  std::vector<float2> mrow, mcol;
+  if (!factor_mask(reinterpret_cast<const float2*>(mask_host), p->n, &mrow, &mcol)) return cudaSuccess;
+  cudaError_t e = cudaSuccess;
+  if (!p->d_mrow) e = cudaMalloc((void**)&p->d_mrow, sizeof(float2) * p->n);
+  if (e == cudaSuccess && !p->d_mcol) e = cudaMalloc((void**)&p->d_mcol, sizeof(float2) * p->n);
+  if (e == cudaSuccess) e = cudaMemcpy(p->d_mrow, mrow.data(), sizeof(float2) * p->n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(p->d_mcol, mcol.data(), sizeof(float2) * p->n, cudaMemcpyHostToDevice);
+  const SepPasses* s = p->sep;
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(s->rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_rows);
+  for (int m = 0; m < 3 && e == cudaSuccess; m++)
+    e = cudaFuncSetAttribute(s->cols[m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_cols(p->res));
+  int dev = 0, sms = 0, occ = 0;
+  if (e == cudaSuccess) e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, s->cols[kSepIntensity], s->t * s->l_cols,
+                                                      s->smem_cols(p->res));
+  if (e == cudaSuccess) {
+    p->sep_cols_ctas = sms * std::max(occ, 1);
+    p->mask_sep = true;
+  }
+  return e;
 }
 
 // numpy.linspace(-pi, pi, res)[j]
@@ -741,6 +820,12 @@ extern "C" int oopao_pwfs_plan_create(oopao_pwfs_plan** out, int res, int n, int
   if (e == cudaSuccess) e = cudaMalloc((void**)&p->d_err, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(p->d_err, 0, sizeof(int));
   if (p->fast && e == cudaSuccess) e = fast_attrs(p->fast, res, &p->inv_target_ctas, &p->cols3_ctas);
+  {
+    const SepPasses* sc = nullptr;
+    p->sep = sep_candidates(n, &sc) > 0 ? sc : nullptr;
+    p->sep_on = true;
+  }
+  if (e == cudaSuccess) e = sep_setup(p, mask_host);
   if (e != cudaSuccess) {
     oopao_set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
     free_plan(p);
@@ -794,6 +879,8 @@ extern "C" int oopao_pwfs_set_masks(oopao_pwfs_plan* p, int n_masks, const float
   }
   cudaFree(p->d_masks);
   p->d_masks = nullptr;
+  p->mask_sep = false;
+  if (n_masks == 1) OOPAO_CUDA_TRY(sep_setup(p, masks_host));
   if (n_masks > 1) {
     OOPAO_CUDA_TRY(cudaMalloc((void**)&p->d_masks, sizeof(float2) * nn * n_masks));
     OOPAO_CUDA_TRY(cudaMemcpy(p->d_masks, masks_host, sizeof(float2) * nn * n_masks, cudaMemcpyHostToDevice));
@@ -950,6 +1037,100 @@ extern "C" int oopao_pwfs_measure_focal(const oopao_pwfs_plan* p, const float* o
 }
 
 namespace {
+// The two-pass path serves a call when the plan's single mask factorises,
+// a compile-time two-pass plan exists, no focal-plane frame is wanted (it
+// needs the 2-D spectrum, which the two passes never form) and the camera
+// binning divides the column block (or raw data is wanted).
+bool sep_applies(const oopao_pwfs_plan* p, bool focal, bool raw) {
+  return p->sep && p->mask_sep && p->sep_on && p->variant >= 1 && p->n_masks == 1 && !focal &&
+         (raw || p->sep->l_cols % p->bin == 0);
+}
+
+// Slots over modulation points for the two-pass column pass: a divisor d of
+// K (at most `cap`) minimising waves(d) * (K/d + 1/2), the time model of
+// CTAs that each sum K/d points after a fixed set-up of about half a point.
+int sep_ksplit(const oopao_pwfs_plan* p, int bc, int cap) {
+  if (p->ksplit > 0 && p->ksplit <= cap) return p->ksplit;
+  const int blocks = p->n / p->sep->l_cols, resident = std::max(1, p->sep_cols_ctas);
+  int best = 1;
+  double best_t = 1e300;
+  for (int d = 1; d <= p->k && d <= cap; d++) {
+    if (p->k % d) continue;
+    const double ctas = (double)blocks * d * bc;
+    const double t = ceil(ctas / resident) * ((double)p->k / d + 0.5);
+    if (t < best_t - 1e-9) {
+      best_t = t;
+      best = d;
+    }
+  }
+  return best;
+}
+
+// Workspace of one two-pass chunk of bc items with ks slots.
+size_t sep_chunk_bytes(const oopao_pwfs_plan* p, int bc, int ks, bool fused) {
+  const size_t y = (size_t)p->ngroups * p->res * p->n * sizeof(float2);
+  const size_t f = (size_t)p->res * p->res * sizeof(float2);
+  const size_t part = (size_t)ks * (fused ? (size_t)p->cam * p->cam : (size_t)p->n * p->n) * sizeof(float);
+  return (size_t)bc * (y + f + part) + 1024;
+}
+
+// Two-pass measurement (pwfs_sep.cuh): field, filtered rows of every
+// row-transform group, filtered columns summed over slots of points and
+// binned, then the fixed-order sum of the slots.  Returns
+// OOPAO_ERR_WORKSPACE (without launching) when one item does not fit.
+int measure_sep(const oopao_pwfs_plan* p, const float* opd, double phase_scale, int batch, float* frame,
+                float* raw, char* base, size_t usable, cudaStream_t st) {
+  const SepPasses* s = p->sep;
+  const int n = p->n, res = p->res, k = p->k, cam = p->cam, ng = p->ngroups;
+  const bool fused = raw == nullptr;
+  const int cap = fused ? kMaxSlotsBinned : kMaxSlotsRaw;
+  const size_t item = sep_chunk_bytes(p, 1, 1, fused);
+  int bc = (int)std::min<size_t>((size_t)batch, std::max<size_t>(1, p->l2_budget / item));
+  int ks = sep_ksplit(p, bc, cap);
+  while (bc > 1 && sep_chunk_bytes(p, bc, ks, fused) > usable) {
+    bc = (bc + 1) / 2;
+    ks = sep_ksplit(p, bc, cap);
+  }
+  if (sep_chunk_bytes(p, bc, ks, fused) > usable) return OOPAO_ERR_WORKSPACE;
+  float2* y = (float2*)base;
+  float2* field = y + (size_t)bc * ng * res * n;
+  float* part = (float*)(field + (size_t)bc * res * res);
+  PwfsProfile* prof = p->prof->enabled ? p->prof : nullptr;
+  auto mark = [&](int stage) {
+    if (prof) prof->mark(stage, st);
+  };
+  int launches = 0;
+  for (int b0 = 0; b0 < batch; b0 += bc) {
+    const int nb = std::min(bc, batch - b0);
+    mark(0);
+    pwfs_field<<<dim3(ceil_div(res * res, 256), nb), 256, 0, st>>>(opd + (size_t)b0 * res * res, (float)phase_scale,
+                                                                   p->d_amp, field, res * res);
+    mark(0);
+    SepRowsArgs ra{p->d_tw, field, p->d_growfac, p->d_mrow, y, res, ng, p->off};
+    mark(0);
+    s->rows<<<dim3(ceil_div(res, s->l_rows), ng, nb), s->t * s->l_rows, s->smem_rows, st>>>(ra);
+    mark(0);
+    SepColsArgs ca{p->d_tw, p->d_mcol, y, p->d_group, p->d_colfac, weights_of(p), nullptr, nullptr,
+                   fused ? nullptr : part, fused ? part : nullptr, res, p->off, ng, k / ks, ks, p->bin, cam};
+    mark(1);
+    s->cols[kSepIntensity]<<<dim3(n / s->l_cols, ks, nb), s->t * s->l_cols, s->smem_cols(res), st>>>(ca);
+    mark(1);
+    mark(3);
+    if (fused) {
+      pwfs_reduce_binned<<<dim3(ceil_div(cam * cam, 256), nb), 256, 0, st>>>(part, frame + (size_t)b0 * cam * cam,
+                                                                             cam * cam, ks);
+    } else {
+      pwfs_bin<<<dim3(cam, nb), 128, 0, st>>>(part, frame + (size_t)b0 * cam * cam,
+                                              raw + (size_t)b0 * n * n, n, cam, p->bin, ks);
+    }
+    mark(3);
+    launches += 4;
+  }
+  oopao_count_launches(launches);
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}
+
 int measure_impl(const oopao_pwfs_plan* p, const float* opd, double phase_scale, int batch, float* frame,
                  float* raw, float* focal, void* ws, size_t ws_bytes, void* stream) {
   OOPAO_CHECK_ARG(p && opd && frame && ws, "NULL argument");
@@ -957,6 +1138,10 @@ int measure_impl(const oopao_pwfs_plan* p, const float* opd, double phase_scale,
   cudaStream_t st = (cudaStream_t)stream;
   uintptr_t base = ((uintptr_t)ws + 255) & ~(uintptr_t)255;
   const size_t usable = ws_bytes > (base - (uintptr_t)ws) ? ws_bytes - (base - (uintptr_t)ws) : 0;
+  if (sep_applies(p, focal != nullptr, raw != nullptr)) {
+    const int r = measure_sep(p, opd, phase_scale, batch, frame, raw, (char*)base, usable, st);
+    if (r != OOPAO_ERR_WORKSPACE) return r;  // else the three-pass path below, in smaller passes
+  }
   size_t units = default_units(p, batch);
   PassPlan pp = plan_passes(p, batch, raw != nullptr, units);
   while (pp.bytes > usable && units > 1) {
@@ -1447,20 +1632,85 @@ extern "C" size_t oopao_pwfs_ad_workspace_bytes(const oopao_pwfs_plan* p, int ba
   return g + per * std::min<size_t>((size_t)batch, cap_items) + 4096;
 }
 
+namespace {
+// Tangent through the two passes: the operating point's filtered rows, then
+// its fields G_k stored once ([K][N][N], the storing column pass), then per
+// chunk of tangents the filtered rows of i dphi W and the tangent column
+// pass, which sums 2 w_k Re(conj(G_k) dG_k) against the stored G_k.  The
+// items of one (column block, slot) run side by side, so they share the G_k
+// columns through L2.  OOPAO_ERR_WORKSPACE (nothing launched) when one item
+// does not fit.
+int jvp_sep(const oopao_pwfs_plan* p, const float* opd0, int opd0_batch, const float* dopd, double phase_scale,
+            int batch, float* dframe, char* base, size_t usable, cudaStream_t st) {
+  const SepPasses* s = p->sep;
+  const int n = p->n, res = p->res, k = p->k, cam = p->cam, ng = p->ngroups;
+  float2* g = (float2*)base;  // [k][n][n] operating-point fields
+  float2* w0 = g + (size_t)k * n * n;
+  char* chunk = (char*)(w0 + (size_t)res * res);
+  const size_t fixed = (size_t)(chunk - base);
+  if (usable <= fixed) return OOPAO_ERR_WORKSPACE;
+  const size_t avail = usable - fixed;
+  int bc = opd0_batch == 1 ? batch : 1;
+  bc = (int)std::min<size_t>((size_t)bc, std::max<size_t>(1, p->l2_budget / sep_chunk_bytes(p, 1, 1, true)));
+  int ks = sep_ksplit(p, bc, kMaxSlotsBinned);
+  while (bc > 1 && sep_chunk_bytes(p, bc, ks, true) > avail) {
+    bc = (bc + 1) / 2;
+    ks = sep_ksplit(p, bc, kMaxSlotsBinned);
+  }
+  if (sep_chunk_bytes(p, bc, ks, true) > avail) return OOPAO_ERR_WORKSPACE;
+  float2* y = (float2*)chunk;
+  float2* fld = y + (size_t)bc * ng * res * n;
+  float* part = (float*)(fld + (size_t)bc * res * res);
+  const int ks0 = sep_ksplit(p, 1, kMaxSlotsBinned);
+  int launches = 0;
+  for (int b0 = 0; b0 < batch; b0 += bc) {
+    const int nb = std::min(bc, batch - b0);
+    const float* o0 = opd0 + (opd0_batch == 1 ? 0 : (size_t)b0 * res * res);
+    if (b0 == 0 || opd0_batch != 1) {
+      pwfs_field<<<dim3(ceil_div(res * res, 256), 1), 256, 0, st>>>(o0, (float)phase_scale, p->d_amp, w0, res * res);
+      SepRowsArgs ra{p->d_tw, w0, p->d_growfac, p->d_mrow, y, res, ng, p->off};
+      s->rows<<<dim3(ceil_div(res, s->l_rows), ng, 1), s->t * s->l_rows, s->smem_rows, st>>>(ra);
+      SepColsArgs ca{p->d_tw, p->d_mcol, y, p->d_group, p->d_colfac, nullptr, nullptr, g, nullptr, nullptr,
+                     res, p->off, ng, k / ks0, ks0, p->bin, cam};
+      s->cols[kSepStore]<<<dim3(n / s->l_cols, ks0, 1), s->t * s->l_cols, s->smem_cols(res), st>>>(ca);
+      launches += 3;
+    }
+    pwfs_field_tangent<<<dim3(ceil_div(res * res, 256), nb), 256, 0, st>>>(
+        o0, dopd + (size_t)b0 * res * res, (float)phase_scale, p->d_amp, fld, res * res, 0);
+    SepRowsArgs ra{p->d_tw, fld, p->d_growfac, p->d_mrow, y, res, ng, p->off};
+    s->rows<<<dim3(ceil_div(res, s->l_rows), ng, nb), s->t * s->l_rows, s->smem_rows, st>>>(ra);
+    SepColsArgs ca{p->d_tw, p->d_mcol, y, p->d_group, p->d_colfac, weights_of(p), g, nullptr, nullptr, part,
+                   res, p->off, ng, k / ks, ks, p->bin, cam};
+    s->cols[kSepTangent]<<<dim3(n / s->l_cols, ks, nb), s->t * s->l_cols, s->smem_cols(res), st>>>(ca);
+    pwfs_reduce_binned<<<dim3(ceil_div(cam * cam, 256), nb), 256, 0, st>>>(part, dframe + (size_t)b0 * cam * cam,
+                                                                           cam * cam, ks);
+    launches += 4;
+  }
+  oopao_count_launches(launches);
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}
+}  // namespace
+
 extern "C" int oopao_pwfs_jvp(const oopao_pwfs_plan* p, const float* opd0, int opd0_batch, const float* dopd,
                               double phase_scale, int batch, float* dframe, void* ws, size_t ws_bytes,
                               void* stream) {
   OOPAO_CHECK_ARG(p && opd0 && dopd && dframe && ws, "NULL argument");
   OOPAO_CHECK_ARG(batch >= 1 && (opd0_batch == 1 || opd0_batch == batch), "opd0_batch must be 1 or batch");
+  cudaStream_t st = (cudaStream_t)stream;
+  uintptr_t base = ((uintptr_t)ws + 255) & ~(uintptr_t)255;
+  OOPAO_CHECK_ARG(ws_bytes > base - (uintptr_t)ws, "workspace too small");
+  const size_t usable = ws_bytes - (base - (uintptr_t)ws);
+  if (sep_applies(p, false, false)) {
+    const int r = jvp_sep(p, opd0, opd0_batch, dopd, phase_scale, batch, dframe, (char*)base, usable, st);
+    if (r != OOPAO_ERR_WORKSPACE) return r;  // else the three-pass tangent below
+  }
   const AdPasses* ad = nullptr;
   int st0 = ad_setup(p, &ad);
   if (st0) return st0;
   OOPAO_CHECK_ARG(ad->l % p->bin == 0, "tangent pass needs the camera binning to divide its row block");
-  cudaStream_t st = (cudaStream_t)stream;
   const FastPasses* f = p->fast;
   const int n = p->n, res = p->res, k = p->k, cam = p->cam;
-  uintptr_t base = ((uintptr_t)ws + 255) & ~(uintptr_t)255;
-  const size_t usable = ws_bytes - (base - (uintptr_t)ws);
   float2* g = (float2*)base;  // [k][n][n] operating-point fields
   float2* w0 = g + (size_t)k * n * n;
   char* chunk = (char*)(w0 + (size_t)res * res);
@@ -1621,6 +1871,17 @@ extern "C" int oopao_pwfs_variant_info(const oopao_pwfs_plan* p, int variant, in
 }
 
 extern "C" int oopao_pwfs_get_variant(const oopao_pwfs_plan* p) { return p ? p->variant : -1; }
+
+extern "C" int oopao_pwfs_set_separable(oopao_pwfs_plan* p, int enable) {
+  OOPAO_CHECK_ARG(p, "NULL plan");
+  p->sep_on = enable != 0;
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_pwfs_separable(const oopao_pwfs_plan* p) {
+  if (!p) return -1;
+  return sep_applies(p, false, false) ? 1 : 0;
+}
 
 // ---------------------------------------------------------------------------
 // Allocation-free measurement.
