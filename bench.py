@@ -758,6 +758,42 @@ def kernel_bytes(kernel, res, n, cam, units, items, launches):
 
 
 KERNELS = ['pwfs_rows_fwd', 'pwfs_cols', 'pwfs_rows_inv', 'pwfs_bin']
+# stages of the two-pass path (masks that factorise per axis): 0 field + filtered
+# rows, 1 filtered columns with the |G|^2 sum and binning, 3 fixed-order slot sum
+KERNELS_SEP = ['pwfs_srows', 'pwfs_scols', 'unused', 'pwfs_reduce_binned']
+
+
+def kernel_bytes_sep(kernel, res, n, cam, ng, units, items, ksplit):
+    """Algorithmic DRAM bytes of the two-pass kernels over the timed region:
+    `units` (item, point) pairs, `items` frames, `ng` row-transform groups.
+    Row stage: OPD in (4 res^2), field out and back in (16 res^2), filtered
+    rows out (8 res N per group).  Column stage: the filtered rows of a point
+    read once per point (8 res N) and binned slot partials out (4 cam^2 per
+    slot).  Reduce: the slot partials in, the frame out."""
+    if kernel == 'pwfs_srows':
+        return items * (4 * res * res + 16 * res * res + ng * 8 * res * n)
+    if kernel == 'pwfs_scols':
+        return units * 8 * res * n + items * ksplit * 4 * cam * cam
+    return items * (ksplit + 1) * 4 * cam * cam
+
+
+def fft_flops(kernel, res, n, ng, units, items):
+    """Nominal FFT flops (5 N log2 N per length-N complex transform) of the
+    two-pass kernels: per group and pupil row a forward and an inverse row
+    transform; per (item, point) N forward and N inverse column transforms."""
+    per = 5.0 * n * np.log2(n)
+    if kernel == 'pwfs_srows':
+        return items * ng * res * 2 * per
+    if kernel == 'pwfs_scols':
+        return units * n * 2 * per
+    return 0.0
+
+
+def fp32_peak_tflops(sm_mhz):
+    """FP32 CUDA-core peak at the sampled SM clock: SMs x 128 lanes x 2 flops."""
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    return sms * 128 * 2 * sm_mhz * 1e6 / 1e12
 
 
 def headline_config():
@@ -905,13 +941,33 @@ def run_ours(args):
     value = frames_step * world / (ms_step / 1000.0)
 
     # ---- roofline of the dominant kernel
-    totals = {KERNELS[i]: ms[i] for i in range(4)}
+    two_pass = N.call('oopao_pwfs_separable', plan.h) == 1
+    names = KERNELS_SEP if two_pass else KERNELS
+    totals = {names[i]: ms[i] for i in range(4) if cnt[i]}
     top = max(totals, key=totals.get)
-    ti = KERNELS.index(top)
+    ti = names.index(top)
     items = frames_step * args.steps
     units = items * k
     nl = cnt[ti]
-    byts = kernel_bytes(top, RES, n, cam, units, items, nl)
+    fp32 = None
+    if two_pass:
+        info = np.zeros(4, np.int32)
+        N.call('oopao_pwfs_pass_info', plan.h, wfs.max_batch, info)
+        ng, ks = int(info[1]), int(info[2])
+        byts = kernel_bytes_sep(top, RES, n, cam, ng, units, items, ks)
+        flops = fft_flops(top, RES, n, ng, units, items)
+        sm_mhz = (clocks or {}).get('sm_mhz') or 2070.0
+        fpk = fp32_peak_tflops(sm_mhz)
+        ach_tf = flops / (totals[top] / 1000.0) / 1e12
+        fp32 = {'achieved_tflops': ach_tf, 'peak_tflops': fpk, 'frac': ach_tf / fpk,
+                'peak_kind': 'nominal (SMs x 128 FP32 lanes x 2 x sampled SM clock)',
+                'flops': 'nominal FFT flops, 5 N log2 N per length-N transform'}
+        # the per-point bytes of the three-pass formulation, 8 (2 res N + 2 N^2):
+        # the bandwidth a bandwidth-bound three-pass pipeline would need for
+        # this frame rate
+        three_pass_gbs = units * 8 * (2 * RES * n + 2 * n * n) / (sum(totals.values()) / 1000.0) / 1e9
+    else:
+        byts = kernel_bytes(top, RES, n, cam, units, items, nl)
     achieved = byts / (totals[top] / 1000.0) / 1e9
     peak, peak_kind = load_peaks()
     variant = int(N_variant(wfs))
@@ -988,11 +1044,16 @@ def run_ours(args):
             'frames_per_step': frames_step, 'batch_per_launch': wfs.max_batch,
             'config': headline_config(),
             'im_rel_fro_err_vs_fp64_oracle': err,
-            'roofline': {'bound': 'hbm', 'kernel': top, 'variant': variant, 'achieved': achieved, 'peak': peak,
-                         'unit': 'GB/s', 'frac': achieved / peak, 'peak_kind': peak_kind,
-                         'traffic': traffic, 'kernel_share': share,
-                         'kernel_ms': {kk: totals[kk] for kk in KERNELS},
-                         'launches': {KERNELS[i]: cnt[i] for i in range(4)}},
+            'roofline': {'bound': 'hbm', 'kernel': top, 'variant': variant, 'two_pass': two_pass,
+                         'achieved': achieved, 'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
+                         'peak_kind': peak_kind, 'traffic': traffic, 'kernel_share': share,
+                         'kernel_ms': totals,
+                         'launches': {names[i]: cnt[i] for i in range(4) if cnt[i]},
+                         'fp32': fp32,
+                         'limiter': ('FP32 issue: the column pass moves %.0f%% of the HBM peak and runs its FFTs '
+                                     'from registers and shared memory' % (100 * achieved / peak))
+                         if two_pass else None,
+                         'three_pass_equivalent_gbs': three_pass_gbs if two_pass else None},
             'e2e': e2e,
             'gpu_launches': int(launches),
             'clocks': clocks,

@@ -113,11 +113,19 @@ int oopao_pwfs_variant_info(const oopao_pwfs_plan* plan, int variant, int* info)
  * the filter splits into a row filter shared by the points with equal x_k
  * and a column filter per point, and oopao_pwfs_measure / oopao_pwfs_jvp run
  * two passes instead of three.  Same results within float32 round-off.
- * set_separable(plan, 0) forces the three-pass path (1, the default, uses
- * the two passes whenever they apply); separable() returns 1 when a measure
- * call without a focal-plane frame takes the two-pass path, else 0. */
+ * set_separable(plan, 0) forces the three-pass path; set_separable(plan, i)
+ * with 1 <= i <= num_separable selects compile-time two-pass plan i (radix
+ * order, columns per CTA) and uses the two passes whenever they apply (a new
+ * plan starts on plan 1).  separable() returns 1 when a measure call without
+ * a focal-plane frame takes the two-pass path, else 0. */
 int oopao_pwfs_set_separable(oopao_pwfs_plan* plan, int enable);
 int oopao_pwfs_separable(const oopao_pwfs_plan* plan);
+int oopao_pwfs_num_separable(const oopao_pwfs_plan* plan);
+/* How a measure call of `batch` items without raw data or focal frame is
+ * launched (instrumentation, no reference counterpart): info[4] = (1 if the
+ * two-pass path runs, row-transform groups, partial slots over modulation
+ * points, items per chunk). */
+int oopao_pwfs_pass_info(const oopao_pwfs_plan* plan, int batch, int* info);
 
 /* Bytes of device workspace oopao_pwfs_measure needs for `batch` items
  * processed in one chunk (a smaller workspace makes it loop over chunks;

@@ -37,6 +37,8 @@ SIGNATURES = {
     'oopao_pwfs_variant_info': (c_int, [c_void_p, c_int, c_void_p]),
     'oopao_pwfs_set_separable': (c_int, [c_void_p, c_int]),
     'oopao_pwfs_separable': (c_int, [c_void_p]),
+    'oopao_pwfs_num_separable': (c_int, [c_void_p]),
+    'oopao_pwfs_pass_info': (c_int, [c_void_p, c_int, c_void_p]),
     'oopao_pwfs_workspace_bytes': (c_size_t, [c_void_p, c_int]),
     'oopao_pwfs_measure': (c_int, [c_void_p, c_void_p, c_double, c_int, c_void_p, c_void_p, c_void_p,
                                    c_size_t, c_void_p]),
@@ -134,7 +136,7 @@ def call(name, *args):
     st = getattr(lib, name)(*[_arg(a) for a in args])
     if SIGNATURES[name][0] is c_int and name not in ('oopao_abi_version', 'oopao_pwfs_n_signal', 'oopao_pwfs_n_masks',
                                                      'oopao_pwfs_get_variant', 'oopao_pwfs_num_variants',
-                                                     'oopao_pwfs_separable'):
+                                                     'oopao_pwfs_separable', 'oopao_pwfs_num_separable'):
         check(st, name)
     return st
 

@@ -662,23 +662,11 @@ bool factor_mask(const float2* m, int n, std::vector<float2>* mrow, std::vector<
   return true;
 }
 
-// Two-pass set-up for mask 0 of the plan: factorise it, upload the factors
-// and opt the kernels into their shared memory.  A mask that does not
-// factorise (or an n without a two-pass plan) leaves mask_sep false.
-cudaError_t sep_setup(oopao_pwfs_plan* p, const float* mask_host) {
-  p->mask_sep = false;
-  // 16-byte tile copies need an even pupil; the column pass must fit in shared memory
-  if (!p->sep || p->res % 2 || p->sep->smem_cols(p->res) > kSmemLimit) return cudaSuccess;
-  std::vector<float2> mrow, mcol;
-  if (!factor_mask(reinterpret_cast<const float2*>(mask_host), p->n, &mrow, &mcol)) return cudaSuccess;
-  cudaError_t e = cudaSuccess;
-  if (!p->d_mrow) e = cudaMalloc((void**)&p->d_mrow, sizeof(float2) * p->n);
-  if (e == cudaSuccess && !p->d_mcol) e = cudaMalloc((void**)&p->d_mcol, sizeof(float2) * p->n);
-  if (e == cudaSuccess) e = cudaMemcpy(p->d_mrow, mrow.data(), sizeof(float2) * p->n, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(p->d_mcol, mcol.data(), sizeof(float2) * p->n, cudaMemcpyHostToDevice);
+// Opt the plan's two-pass kernels into their shared memory and record the
+// resident column-pass CTAs on this device.
+cudaError_t sep_attrs(oopao_pwfs_plan* p) {
   const SepPasses* s = p->sep;
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(s->rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_rows);
+  cudaError_t e = cudaFuncSetAttribute(s->rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_rows);
   for (int m = 0; m < 3 && e == cudaSuccess; m++)
     e = cudaFuncSetAttribute(s->cols[m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_cols(p->res));
   int dev = 0, sms = 0, occ = 0;
@@ -687,10 +675,27 @@ cudaError_t sep_setup(oopao_pwfs_plan* p, const float* mask_host) {
   if (e == cudaSuccess)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, s->cols[kSepIntensity], s->t * s->l_cols,
                                                       s->smem_cols(p->res));
-  if (e == cudaSuccess) {
-    p->sep_cols_ctas = sms * std::max(occ, 1);
-    p->mask_sep = true;
-  }
+  if (e == cudaSuccess) p->sep_cols_ctas = sms * std::max(occ, 1);
+  return e;
+}
+
+// Two-pass set-up for mask 0 of the plan: factorise it, upload the factors
+// and prepare the kernels.  A mask that does not factorise (or an n without
+// a two-pass plan) leaves mask_sep false.
+cudaError_t sep_setup(oopao_pwfs_plan* p, const float* mask_host) {
+  p->mask_sep = false;
+  // 16-byte tile copies need an even pupil; the column pass must fit in shared memory
+  if (!p->sep || p->res % 2 || p->sep->smem_cols(p->res) > kSmemLimit)
+    return cudaSuccess;
+  std::vector<float2> mrow, mcol;
+  if (!factor_mask(reinterpret_cast<const float2*>(mask_host), p->n, &mrow, &mcol)) return cudaSuccess;
+  cudaError_t e = cudaSuccess;
+  if (!p->d_mrow) e = cudaMalloc((void**)&p->d_mrow, sizeof(float2) * p->n);
+  if (e == cudaSuccess && !p->d_mcol) e = cudaMalloc((void**)&p->d_mcol, sizeof(float2) * p->n);
+  if (e == cudaSuccess) e = cudaMemcpy(p->d_mrow, mrow.data(), sizeof(float2) * p->n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(p->d_mcol, mcol.data(), sizeof(float2) * p->n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = sep_attrs(p);
+  if (e == cudaSuccess) p->mask_sep = true;
   return e;
 }
 
@@ -1874,8 +1879,58 @@ extern "C" int oopao_pwfs_get_variant(const oopao_pwfs_plan* p) { return p ? p->
 
 extern "C" int oopao_pwfs_set_separable(oopao_pwfs_plan* p, int enable) {
   OOPAO_CHECK_ARG(p, "NULL plan");
-  p->sep_on = enable != 0;
+  OOPAO_CHECK_ARG(enable >= 0, "enable must be 0 (three passes) or a two-pass plan index >= 1");
+  if (enable == 0) {
+    p->sep_on = false;
+    return OOPAO_OK;
+  }
+  const SepPasses* c = nullptr;
+  const int cnt = sep_candidates(p->n, &c);
+  if (enable > cnt) {
+    oopao_set_last_error("no such two-pass plan for this FFT size", __FILE__, __LINE__);
+    return OOPAO_ERR_UNSUPPORTED;
+  }
+  if (p->sep != c + (enable - 1)) {
+    const SepPasses* prev = p->sep;
+    p->sep = c + (enable - 1);
+    if (p->res % 2 || p->sep->smem_cols(p->res) > kSmemLimit) {
+      p->sep = prev;
+      oopao_set_last_error("that two-pass plan does not fit this pupil", __FILE__, __LINE__);
+      return OOPAO_ERR_UNSUPPORTED;
+    }
+    OOPAO_CUDA_TRY(sep_attrs(p));
+  }
+  p->sep_on = true;
   return OOPAO_OK;
+}
+
+extern "C" int oopao_pwfs_pass_info(const oopao_pwfs_plan* p, int batch, int* info) {
+  OOPAO_CHECK_ARG(p && info && batch >= 1, "bad argument");
+  const size_t ws = oopao_pwfs_workspace_bytes(p, batch);
+  info[1] = p->ngroups;
+  if (sep_applies(p, false, false)) {
+    int bc = (int)std::min<size_t>((size_t)batch, std::max<size_t>(1, p->l2_budget / sep_chunk_bytes(p, 1, 1, true)));
+    int ks = sep_ksplit(p, bc, kMaxSlotsBinned);
+    while (bc > 1 && sep_chunk_bytes(p, bc, ks, true) > ws - 256) {
+      bc = (bc + 1) / 2;
+      ks = sep_ksplit(p, bc, kMaxSlotsBinned);
+    }
+    info[0] = 1;
+    info[2] = ks;
+    info[3] = bc;
+  } else {
+    const PassPlan pp = plan_passes(p, batch, false, default_units(p, batch));
+    info[0] = 0;
+    info[2] = pp.ksplit;
+    info[3] = pp.bc;
+  }
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_pwfs_num_separable(const oopao_pwfs_plan* p) {
+  if (!p) return -1;
+  const SepPasses* c = nullptr;
+  return sep_candidates(p->n, &c);
 }
 
 extern "C" int oopao_pwfs_separable(const oopao_pwfs_plan* p) {

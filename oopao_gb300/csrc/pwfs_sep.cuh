@@ -191,8 +191,8 @@ struct SepColsSmem {
   static size_t bytes(int res) { return sizeof(float2) * (kTiles + tile(res)); }
 };
 
-template <int N, int R1, int R2, int T, int L, int MODE>
-__global__ void __launch_bounds__(T* L) pwfs_scols(SepColsArgs a) {
+template <int N, int R1, int R2, int T, int L, int MODE, int MAXREG>
+__global__ void __launch_bounds__(T* L) __maxnreg__(MAXREG) pwfs_scols(SepColsArgs a) {
   using S = SepColsSmem<N, R1, R2, T, L>;
   constexpr int R1P = S::LAY1 >> 16, LS1 = S::LS1;
   constexpr int R2P = S::LAY2 >> 16, LS2 = S::LS2;
@@ -317,24 +317,25 @@ struct SepPasses {
   size_t (*smem_cols)(int res);
 };
 
-template <int N, int R1, int R2, int T, int LR, int LC>
+// MAXREG caps the column pass's registers per thread (its occupancy).
+template <int N, int R1, int R2, int T, int LR, int LC, int MAXREG>
 SepPasses make_sep() {
   static_assert(N % LC == 0, "column blocks must tile N");
   constexpr int R1P = pad_odd(R1), R2P = pad_odd(R2);
   constexpr bool ALIAS = (R1 + T - 1) / T == 1;
   constexpr int LSR1 = xchg_stride(R2 * R1P, T, LR, R1P, R2, R1);
   constexpr int LSR2 = xchg_stride(R1 * R2P, T, LR, R2P, R1, R2);
-  constexpr int LSC1 = cols_layout(R1, R2, T, LC) & 0xFFFF, LSC2 = cols_layout(R2, R1, T, LC) & 0xFFFF;
   constexpr int LSR = ALIAS ? imax(LSR1, LSR2) : LSR1 + LSR2;
+  constexpr int LSC1 = cols_layout(R1, R2, T, LC) & 0xFFFF, LSC2 = cols_layout(R2, R1, T, LC) & 0xFFFF;
   constexpr int LSC = ALIAS ? imax(LSC1, LSC2) : LSC1 + LSC2;
   // the binning epilogue reuses the exchange as [LC][N] floats
   static_assert((size_t)LC * LSC * 2 >= (size_t)LC * N, "exchange too small for the binning rows");
   SepPasses s;
   s.n = N; s.r1 = R1; s.r2 = R2; s.t = T; s.l_rows = LR; s.l_cols = LC;
   s.rows = pwfs_srows<N, R1, R2, T, LR>;
-  s.cols[kSepIntensity] = pwfs_scols<N, R1, R2, T, LC, kSepIntensity>;
-  s.cols[kSepTangent] = pwfs_scols<N, R1, R2, T, LC, kSepTangent>;
-  s.cols[kSepStore] = pwfs_scols<N, R1, R2, T, LC, kSepStore>;
+  s.cols[kSepIntensity] = pwfs_scols<N, R1, R2, T, LC, kSepIntensity, MAXREG>;
+  s.cols[kSepTangent] = pwfs_scols<N, R1, R2, T, LC, kSepTangent, MAXREG>;
+  s.cols[kSepStore] = pwfs_scols<N, R1, R2, T, LC, kSepStore, MAXREG>;
   s.smem_rows = sizeof(float2) * (3 * (size_t)N + (size_t)LR * LSR);
   s.smem_cols = &SepColsSmem<N, R1, R2, T, LC>::bytes;
   return s;
