@@ -138,11 +138,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
+  int issued = 0;  // loads issued by the producer (warp 0, lane 0)
   if (warp == 0 && lane == 0) {
     // TMA producer
     for (int kb = 0; kb < p.nk; kb++) {
       const int s = kb % kStages;
       if (!mbar_wait(&empty[s], ((kb / kStages) & 1) ^ 1, p.err, 1)) break;
+      issued = kb + 1;
       mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
       tma_load_2d(sa + s * A_BYTES, &tma_a, &full[s], kb * kBK, m0);
       tma_load_2d(sb + s * B_BYTES, &tma_b, &full[s], kb * kBK, n0);
@@ -188,6 +190,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
     }
+  }
+  if (!ok && warp == 0 && lane == 0) {
+    // a wait timed out: give each stage's last issued load a bounded
+    // chance to land before the CTA's shared memory is released
+    for (int kb = issued - 1; kb >= 0 && kb >= issued - kStages; kb--)
+      mbar_wait(&full[kb % kStages], (kb / kStages) & 1, nullptr, 0);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
