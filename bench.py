@@ -376,6 +376,83 @@ def large_config(n_tangents=64):
     return out
 
 
+def config4_leg(n_modes=500, n_screens=64, n_steps=200, sigma=50e-9, n_fd=4, seed=0):
+    """Differentiable PWFS on the 40x40 optics (240 px, N=504, 96 points,
+    41x41 DM): the loss ||signal(M2C x) - target||^2 over the first 500 KL
+    modes, 64 seeded modal screens with coefficients ~N(0, 50 nm) (the modes
+    are 1 m RMS per unit coefficient), the targets measured through the same
+    sensor.  Reports the hand-written adjoint gradient against central finite
+    differences (step 1e-3 rad RMS of phase along seeded unit directions, every
+    screen) and against the gradient of the push-pull interaction matrix
+    (2 D^T (s - t), stroke 1e-8 m) at the flat operating point, then the time
+    per step of 200 batched gradient-descent (Adam) steps and the loss and
+    modal error before and after."""
+    import torch
+    import oopao_gb300 as og
+    from oopao_gb300 import autodiff as AD
+    from oopao_gb300 import autotune
+    tel, ngs, dm, wfs = build_system(0, 240, 40, 5, 96, max_batch=n_screens)
+    m2c = kl_like_basis(dm.modes, tel.pupil, n_modes, r0=0.12, L0=30.0)
+    autotune.tune_pyramid(wfs, batch=n_screens)
+    ngs ** tel
+    truth = np.stack([np.random.default_rng(seed + s).standard_normal(n_modes) for s in range(n_screens)], axis=1)
+    truth *= sigma
+    dev = wfs._dev
+    m = torch.as_tensor(m2c, dtype=torch.float32, device=dev)
+    with torch.no_grad():
+        targets = AD.dm_signal(wfs, dm, m @ torch.as_tensor(truth, dtype=torch.float32, device=dev))
+    x0 = np.zeros_like(truth)
+    loss0, g = AD.modal_loss_grad(wfs, dm, m2c, x0, targets)
+    g = g.double().cpu().numpy()
+    # adjoint against central differences of the loss
+    rng = np.random.default_rng(seed + 1000)
+    h = 1e-3 * ngs.wavelength / (2 * np.pi)
+    fd_err = []
+    for _ in range(n_fd):
+        u = rng.standard_normal(truth.shape)
+        u /= np.linalg.norm(u, axis=0)
+        lp = AD.modal_loss(wfs, dm, m2c, x0 + h * u, targets).cpu().numpy()
+        lm = AD.modal_loss(wfs, dm, m2c, x0 - h * u, targets).cpu().numpy()
+        fd = (lp - lm) / (2 * h)
+        ad = (g * u).sum(axis=0)
+        fd_err.append(float(np.max(np.abs(fd - ad)) / np.max(np.abs(ad))))
+    # adjoint against the push-pull interaction matrix at the flat point
+    with _quiet():
+        calib = og.InteractionMatrix(ngs, tel, dm, wfs, M2C=m2c, stroke=1e-8, nMeasurements=1, single_pass=False,
+                                     invert=False)
+    with torch.no_grad():
+        s0 = AD.dm_signal(wfs, dm, torch.zeros((dm.nValidAct, 1), device=dev))
+    r = s0.double().cpu().numpy()[0][:, None] - targets.double().cpu().numpy().T
+    g_pp = 2 * np.asarray(calib.D).T @ r
+    pp_err = float(np.linalg.norm(g - g_pp) / np.linalg.norm(g_pp))
+    # batched gradient descent
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    x, hist = AD.modal_gradient_descent(wfs, dm, m2c, targets, n_iter=n_steps, lr=0.2 * sigma)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    xe = x.double().cpu().numpy()
+    # the same estimation in the sensor's linear range: the screens scaled to
+    # 50 nm RMS in total (coefficients ~N(0, 50 nm / sqrt(500)))
+    lin = truth / np.sqrt(n_modes)
+    with torch.no_grad():
+        t_lin = AD.dm_signal(wfs, dm, m @ torch.as_tensor(lin, dtype=torch.float32, device=dev))
+    x_lin, h_lin = AD.modal_gradient_descent(wfs, dm, m2c, t_lin, n_iter=n_steps // 2,
+                                             lr=0.2 * sigma / np.sqrt(n_modes))
+    lin_err = float(np.linalg.norm(x_lin.double().cpu().numpy() - lin) / np.linalg.norm(lin))
+    return {'config': '40x40 PWFS, 240 px, N=504, 96 points, 41x41 DM, %d KL modes, %d seeded modal screens, '
+                      'coefficients ~N(0, %g nm)' % (n_modes, n_screens, sigma * 1e9),
+            'linear_range': {'coefficients': 'N(0, %.2f nm): 50 nm RMS wavefronts' % (sigma * 1e9 / np.sqrt(n_modes)),
+                             'gd_steps': n_steps // 2, 'loss_first': h_lin[0], 'loss_last': h_lin[-1],
+                             'modal_rel_err_last': lin_err},
+            'adjoint_vs_fd_1e-3rad_max_rel_err': max(fd_err), 'fd_directions': n_fd,
+            'adjoint_vs_push_pull_im_rel_err': pp_err,
+            'gd_steps': n_steps, 'gd_ms_per_step': el * 1000.0 / n_steps, 'optimizer': 'Adam, lr 0.2 sigma',
+            'loss_first': hist[0], 'loss_last': hist[-1], 'loss_at_step_50': hist[min(49, len(hist) - 1)],
+            'modal_rel_err_first': 1.0, 'modal_rel_err_last': float(np.linalg.norm(xe - truth) / np.linalg.norm(truth)),
+            'wavefront_rms_nm_truth': float(np.sqrt((truth ** 2).sum(axis=0)).mean() * 1e9)}
+
+
 def dm_projection(peaks):
     """DM influence-function projection OPD = modes @ coefs at the 20x20,
     40x40 and 80x80 sizes: FP32 CUDA-core path vs BF16 tcgen05 path, per
@@ -1025,6 +1102,7 @@ def run_ours(args):
         del tel3, ngs3, dm3, wfs3
         extra['cl_step'] = cl_rate()
         extra['cl_strehl_20x20'] = cl_strehl()
+        extra['config4_differentiable'] = config4_leg()
         extra['large_80x80'] = large_config()
         try:
             pk = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
@@ -1124,6 +1202,8 @@ def run_case(args):
         out = {'case': args.case, 'cl_gsc_20x20': cl_gsc()}
     elif args.case == 'cl':
         out = {'case': args.case, 'cl_step': cl_rate()}
+    elif args.case == 'c4':
+        out = {'case': args.case, 'config4_differentiable': config4_leg()}
     elif args.case == 'dmproj':
         try:
             pk = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
@@ -1150,7 +1230,7 @@ def main():
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline and accuracy legs')
     ap.add_argument('--no-extra', action='store_true',
                     help='skip the interaction-matrix comparisons and the closed-loop rate')
-    ap.add_argument('--case', default=None, help='run a small profiling workload (%s, dm40, gsc, next, clgsc, cl, dmproj) instead'
+    ap.add_argument('--case', default=None, help='run a small profiling workload (%s, dm40, gsc, next, clgsc, cl, c4, dmproj) instead'
                     % ', '.join(CASES))
     ap.add_argument('--batch', type=int, default=16)
     ap.add_argument('--reps', type=int, default=3)

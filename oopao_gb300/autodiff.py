@@ -232,6 +232,31 @@ def lift_estimate(wfs, dm, M2C, target, n_iter=5, x0=None, damping=0.0):
     return x
 
 
+def modal_loss(wfs, dm, M2C, x, targets):
+    """Per-item loss ||s(M2C x_b) - t_b||^2 [B] (float64 sums of the float32
+    signals) for modal coefficients x [nModes, B] (metres)."""
+    dev = wfs._dev
+    m2c = torch.as_tensor(np.ascontiguousarray(M2C, dtype=np.float32), device=dev)
+    t = _as_device(targets, dev)
+    with torch.no_grad():
+        s = dm_signal(wfs, dm, m2c @ _as_device(x, dev))
+        return ((s.double() - t.double()) ** 2).sum(dim=1)
+
+
+def modal_loss_grad(wfs, dm, M2C, x, targets):
+    """Per-item loss [B] and its gradient d loss_b / d x_b [nModes, B] by the
+    hand-written adjoint (signal VJP, propagation VJP with each modulation
+    point's field recomputed, DM adjoint, M2C^T)."""
+    dev = wfs._dev
+    m2c = torch.as_tensor(np.ascontiguousarray(M2C, dtype=np.float32), device=dev)
+    t = _as_device(targets, dev)
+    xv = _as_device(x, dev).clone().requires_grad_(True)
+    s = dm_signal(wfs, dm, m2c @ xv)
+    loss = ((s - t) ** 2).sum(dim=1)
+    loss.sum().backward()
+    return ((s.detach().double() - t.double()) ** 2).sum(dim=1), xv.grad.detach()
+
+
 def modal_gradient_descent(wfs, dm, M2C, targets, n_iter=200, lr=1e-2, x0=None):
     """Batched modal estimation by gradient descent on ||s(M2C x_b) - t_b||^2
     with the hand-written adjoint.  targets [B, nSignal]; returns x [nModes, B]
@@ -256,4 +281,5 @@ def modal_gradient_descent(wfs, dm, M2C, targets, n_iter=200, lr=1e-2, x0=None):
 
 
 __all__ = ['pyramid_signal', 'dm_signal', 'jvp_interaction_matrix', 'lift_estimate', 'modal_gradient_descent',
+           'modal_loss', 'modal_loss_grad',
            'frames', 'frame_jvp', 'frame_vjp', 'signal_jvp', 'signal_vjp']
