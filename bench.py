@@ -339,25 +339,38 @@ def cl_strehl(n_steps=500, n_oracle=100):
     return out
 
 
-def large_config(n_tangents=64):
+def large_config(n_modes=4000, chunk=16, oracle_cols=4, n_loop=200):
     """39 m, 480 px, 80x80 pyramid (N=1920, 320x320 camera, modulation 4 l/D
-    x 128 points): frames/s of the autotuned compiled plan at batch 1 and 4,
-    and tangents/s of the JVP (the columns of an interaction matrix built from
-    tangents) for `n_tangents` smooth pupil-plane directions, batch 8."""
+    x 128 points), 81x81 Gaussian DM: frames/s of the autotuned plan at batch
+    1 and 4; a 4000-mode interaction matrix built by batched tangents (JVPs)
+    around the flat wavefront, whose operating-point fields G_k of the 128
+    points are computed once and kept (3.8 GB, the checkpoint every tangent
+    reads); and the graph-replayed closed-loop step with 35 infinite-screen
+    layers (r0 0.157 m, L0 25 m).  The modes are seeded random commands of
+    the 81x81 DM (smooth DM shapes, 10 nm RMS): a KL basis at this size needs
+    the dense 9.6 GB IF matrix.  Error: `oracle_cols` columns against a
+    float64 central difference (+-1e-3 rad RMS) of the float64 oracle.  The
+    loop's reconstructor is a zero matrix of the right size (5209 x 10048):
+    the MVM runs in full, the timing does not depend on its values."""
     import torch
     import oopao_gb300 as og
     from oopao_gb300 import autodiff as AD
     from oopao_gb300 import autotune
+    from oopao_gb300.closed_loop import ClosedLoop
     with _quiet():
         tel = og.Telescope(resolution=480, diameter=39.0, samplingTime=1e-3)
         ngs = og.Source(optBand='V0', magnitude=8)
         ngs * tel
         wfs = og.Pyramid(nSubap=80, telescope=tel, modulation=4, lightRatio=0.5, n_pix_separation=80, n_pix_edge=40,
-                         nTheta_user_defined=128, max_batch=8)
+                         nTheta_user_defined=128, max_batch=chunk)
+        t0 = time.perf_counter()
+        dm = og.DeformableMirror(tel, nSubap=80, mechCoupling=0.35)
+        dm_build_s = time.perf_counter() - t0
     ngs ** tel
     wfs.plan.set_amplitude(ngs.intensity, wfs._amplitude_key())
-    out = {'config': '39 m, 480 px, 80x80 PWFS, N=1920, cam 320, modulation 4 l/D x 128 points',
-           'n_signal': wfs.nSignal}
+    out = {'config': '39 m, 480 px, 80x80 PWFS, N=1920, cam 320, modulation 4 l/D x 128 points, 81x81 DM',
+           'n_signal': wfs.nSignal, 'n_act': dm.nValidAct, 'dm_build_s': dm_build_s,
+           'dm_projection': dm.projection_path()}
     g = torch.Generator(device='cuda').manual_seed(0)
     for B in (1, 4):
         tune = autotune.tune_pyramid(wfs, batch=B)
@@ -366,13 +379,77 @@ def large_config(n_tangents=64):
         _, t = _timed(lambda: [wfs._measure_frames(opd, 2 * np.pi / ngs.wavelength) for _ in range(3)])
         out['frames_per_s_batch%d' % B] = 3 * B / t
         out['variant_batch%d' % B] = tune['variant']
-    pup = torch.as_tensor(tel.pupil, dtype=torch.float32, device='cuda')
+    # ---- 4000-mode IM from batched tangents
+    autotune.tune_pyramid(wfs, batch=chunk)
+    cmd = torch.randn((dm.nValidAct, n_modes), device='cuda', generator=g)
+    pup = torch.as_tensor(tel.pupil, dtype=torch.float32, device='cuda') > 0
+    rms = torch.stack([dm.opd_device(cmd[:, i:i + 64].contiguous())[:, pup].std(dim=1)
+                       for i in range(0, 256, 64)]).mean()
+    cmd *= 10e-9 / rms
     opd0 = torch.zeros((1, 480, 480), device='cuda')
-    dirs = torch.randn((n_tangents, 480, 480), device='cuda', generator=g) * pup * 10e-9
-    AD.frame_jvp(wfs, opd0, dirs[:8])
-    _, t = _timed(lambda: [AD.frame_jvp(wfs, opd0, dirs[i:i + 8]) for i in range(0, n_tangents, 8)])
-    out['jvp_tangents_per_s'] = n_tangents / t
-    out['im_4000_modes_estimate_s'] = 4000 / out['jvp_tangents_per_s']
+    frame0 = AD.frames(wfs, opd0)
+
+    def build_im():
+        cols = []
+        for b0 in range(0, n_modes, chunk):
+            dopd = dm.opd_device(cmd[:, b0:b0 + chunk].contiguous())
+            _, ds = AD.signal_jvp(wfs, frame0, AD.frame_jvp(wfs, opd0, dopd))
+            cols.append(ds)
+        return torch.cat(cols).T
+
+    build_im()  # warm-up (plans, workspaces)
+    D, t_im = _timed(build_im)
+    out['im_modes'] = n_modes
+    out['im_build_s'] = t_im
+    out['im_tangents_per_s'] = n_modes / t_im
+    out['im_chunk'] = chunk
+    out['checkpoint_bytes'] = 128 * 1920 * 1920 * 8
+    # float64 oracle derivative of the camera frame along a few modes
+    if oracle_cols:
+        from oracle import pwfs_oracle as O
+        workers = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        geom = O.pyramid_geometry(480, 80, 80, n_pix_edge=40)
+        path, K = O.modulation_path(4, 128)
+        tt = O.tt_buffers(path, geom)
+        inten = O.source_intensity(O.telescope_pupil(480), O.n_photon('V0', 8), 1e-3, 39.0)
+        scale = 2 * np.pi / ngs.wavelength
+        errs = []
+        cols = [int(c) for c in np.random.default_rng(7).choice(n_modes, oracle_cols, replace=False)]
+        for c in cols:
+            dopd = dm.opd_device(cmd[:, c:c + 1].contiguous())
+            got = AD.frame_jvp(wfs, opd0, dopd)[0].double().cpu().numpy()
+            dphi = dopd[0].double().cpu().numpy() * scale * tel.pupil
+            h = 1e-3 / np.sqrt((dphi[tel.pupil > 0] ** 2).mean())
+            fp = O.camera_frame(O.wfs_raw(h * dphi, inten, tt, geom, workers=workers), geom)
+            fm = O.camera_frame(O.wfs_raw(-h * dphi, inten, tt, geom, workers=workers), geom)
+            ref = (fp - fm) / (2 * h)
+            errs.append(float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
+        out['im_frame_derivative_rel_err_vs_fp64_oracle'] = {
+            'columns': cols, 'rel_l2': errs, 'oracle_seconds': time.perf_counter() - t0,
+            'reference': 'float64 oracle camera frames, central difference +-1e-3 rad RMS'}
+    del D, cmd
+    # ---- 35-layer closed-loop step
+    with _quiet():
+        atm = og.Atmosphere(telescope=tel, r0=0.157, L0=25, fractionalR0=[1 / 35] * 35,
+                            windSpeed=list(np.linspace(5., 30., 35)), windDirection=list(np.linspace(0., 340., 35)),
+                            altitude=list(np.linspace(0., 20000., 35)))
+        atm.initializeAtmosphere(tel)
+    autotune.tune_pyramid(wfs, batch=1)
+    R = np.zeros((dm.nValidAct, wfs.nSignal), dtype=np.float32)
+    cl = ClosedLoop(tel, ngs, dm, wfs, R, gain=0.4, layers=atm, max_steps=n_loop + 30)
+    cl.capture()
+    cl.run(10)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    cl.run(n_loop)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / n_loop
+    out['cl_35_layers'] = {'steps': n_loop, 'us_per_step': ms * 1e3, 'hz': 1e3 / ms, 'graph': True,
+                           'layers': 35, 'atm_status': atm.status(),
+                           'reconstructor': 'zero matrix %dx%d (timing only)' % R.shape}
     return out
 
 
@@ -1202,6 +1279,8 @@ def run_case(args):
         out = {'case': args.case, 'cl_gsc_20x20': cl_gsc()}
     elif args.case == 'cl':
         out = {'case': args.case, 'cl_step': cl_rate()}
+    elif args.case == 'c5':
+        out = {'case': args.case, 'large_80x80': large_config()}
     elif args.case == 'c4':
         out = {'case': args.case, 'config4_differentiable': config4_leg()}
     elif args.case == 'dmproj':
@@ -1230,7 +1309,7 @@ def main():
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline and accuracy legs')
     ap.add_argument('--no-extra', action='store_true',
                     help='skip the interaction-matrix comparisons and the closed-loop rate')
-    ap.add_argument('--case', default=None, help='run a small profiling workload (%s, dm40, gsc, next, clgsc, cl, c4, dmproj) instead'
+    ap.add_argument('--case', default=None, help='run a small profiling workload (%s, dm40, gsc, next, clgsc, cl, c4, c5, dmproj) instead'
                     % ', '.join(CASES))
     ap.add_argument('--batch', type=int, default=16)
     ap.add_argument('--reps', type=int, default=3)

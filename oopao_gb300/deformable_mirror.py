@@ -97,29 +97,36 @@ class DeformableMirror:
         self.coordinates = np.stack([xIF, yIF], axis=1)
         self.xIF, self.yIF = xIF, yIF
         self._sep_host = None
+        self._modes = None
+        self._modes_t_dev = None
         if modes is None:
             u0x = self.resolution / 2 + xIF * self.resolution / self.D
             u0y = self.resolution / 2 + yIF * self.resolution / self.D
-            self.modes = self._gaussian_modes(u0x, u0y)
+            self._u0 = (u0x, u0y)
+            sep = self._separable_factors(u0x, u0y)
             if np.isscalar(self.actuator_selection):
-                pup = telescope.pupil.flatten() == 1
-                std = np.std(self.modes[pup, :], axis=0)
+                std = self._if_std(telescope.pupil, sep)
                 keep = np.where(std > self.actuator_selection * np.max(std))[0]
-                self.modes = self.modes[:, keep]
+                if self._modes is not None:
+                    self._modes = self._modes[:, keep]
                 self.validAct = keep
                 self.nValidAct = len(keep)
                 self.nIF = self.nValidAct
                 self.xIF, self.yIF = self.xIF[keep], self.yIF[keep]
                 self.coordinates = self.coordinates[keep]
                 u0x, u0y = u0x[keep], u0y[keep]
-            self._sep_host = self._separable_factors(u0x, u0y)
+                self._u0 = (u0x, u0y)
+                if sep is not None:
+                    sep = self._separable_factors(u0x, u0y)
+            self._sep_host = sep
+            if sep is None and self._modes is None:
+                self._modes = self._gaussian_modes(u0x, u0y)
         else:
-            self.modes = np.asarray(modes) * self.sign
-            self.nValidAct = self.modes.shape[1]
-        if self.modes.shape[0] != self.resolution ** 2:
-            raise OopaoError('modes must be [resolution**2, n_modes]')
+            self._modes = np.asarray(modes) * self.sign
+            self.nValidAct = self._modes.shape[1]
+            if self._modes.shape[0] != self.resolution ** 2:
+                raise OopaoError('modes must be [resolution**2, n_modes]')
         self._dev = device()
-        self._modes_t = None
         self._upload_modes()
         # the separable projection serves every batch when the IFs factorise
         self.separable_projection = self._sep_host is not None
@@ -127,7 +134,8 @@ class DeformableMirror:
         self._sep_ws = None
         if self._sep_host is not None:
             gx, gy, cells = self._sep_host
-            self._sep = (torch.as_tensor(gx, device=self._dev), torch.as_tensor(gy, device=self._dev),
+            self._sep = (torch.as_tensor(gx, dtype=torch.float32, device=self._dev),
+                         torch.as_tensor(gy, dtype=torch.float32, device=self._dev),
                          torch.as_tensor(cells, device=self._dev), gx.shape[0], gy.shape[0])
         self._opd_dev = None
         self._opd_host = None
@@ -137,6 +145,50 @@ class DeformableMirror:
         print_(self, print_dm_properties)
 
     # ------------------------------------------------------------ IF build
+    @property
+    def modes(self):
+        """Influence functions [res**2, nValidAct] (OOPAO/DeformableMirror.py:
+        572-600).  When the Gaussian IFs factorise per axis the projections
+        run on the factors, and this dense matrix (9.6 GB in float64 for an
+        80x80 DM at 480 px) is built on first access only."""
+        if self._modes is None:
+            self._modes = self._gaussian_modes(*self._u0)
+        return self._modes
+
+    @modes.setter
+    def modes(self, value):
+        self._modes = value
+        self._modes_t_dev = None
+
+    @property
+    def _modes_t(self):
+        """The IFs transposed, [nValidAct, res**2] float32 on the device (the
+        dense FP32 projection and the DM adjoint), uploaded on first use."""
+        if self._modes_t_dev is None:
+            mt = np.ascontiguousarray(np.asarray(self.modes, dtype=np.float32).T)
+            self._modes_t_dev = torch.as_tensor(mt, device=self._dev)
+        return self._modes_t_dev
+
+    def _if_std(self, pupil, sep):
+        """Standard deviation of each IF over the pupil pixels (the reference's
+        actuator selection, np.std(modes[pupil, :], axis=0)), from the factors
+        when they exist: with P the pupil, the IF of the actuator in grid cell
+        (iy, ix) has mean (gy P gx^T)[iy, ix] / n and second moment
+        (gy^2 P (gx^2)^T)[iy, ix] / n."""
+        if sep is None:
+            pup = pupil.flatten() == 1
+            return np.std(self.modes[pup, :], axis=0)
+        gx, gy, cells = sep
+        P = (np.asarray(pupil) == 1).astype(np.float64)
+        n = P.sum()
+        m1 = gy @ P @ gx.T / n
+        m2 = (gy ** 2) @ P @ (gx ** 2).T / n
+        std_cell = np.sqrt(np.maximum(m2 - m1 ** 2, 0.0)).reshape(-1)
+        out = np.empty(len(self._u0[0]))
+        live = cells >= 0
+        out[cells[live]] = std_cell[live]
+        return out
+
     @staticmethod
     def rotate_coordinates(x, y, angle):
         """Rotation of the actuator grid by `angle` radians (:559-562)."""
@@ -210,21 +262,19 @@ class DeformableMirror:
             gx = gx[:, ::-1]
         if self.flip_:
             gx, gy = gx[:, ::-1], gy[:, ::-1]
-        # the dense modes are the reference: the factors must reproduce them
-        # (to round-off of the modes' own precision: float32 with
-        # floating_precision=32)
-        scale = np.max(np.abs(self.modes))
-        tol = (2e-7 if self.modes.dtype == np.float32 else 1e-12) * scale
-        for k in range(0, len(u0x), 64):
-            cols = np.arange(k, min(k + 64, len(u0x)))
-            rebuilt = (gy[iy[cols]][:, :, None] * gx[ix[cols]][:, None, :]).reshape(len(cols), res * res)
-            if np.max(np.abs(rebuilt.T - self.modes[:, cols])) > tol:
-                return None
-        return (np.ascontiguousarray(gx, dtype=np.float32), np.ascontiguousarray(gy, dtype=np.float32), cells)
+        # the dense IFs are the reference: the factors must reproduce them (to
+        # round-off of the modes' own precision, float32 with
+        # floating_precision=32) on a spread sample of actuators; the product
+        # of the two 1-D Gaussians is the 2-D one by construction
+        cols = np.unique(np.linspace(0, len(u0x) - 1, min(len(u0x), 128)).astype(int))
+        dense = self._gaussian_modes(u0x[cols], u0y[cols])
+        tol = (2e-7 if dense.dtype == np.float32 else 1e-12) * np.max(np.abs(dense))
+        rebuilt = (gy[iy[cols]][:, :, None] * gx[ix[cols]][:, None, :]).reshape(len(cols), res * res)
+        if np.max(np.abs(rebuilt.T - dense)) > tol:
+            return None
+        return (np.ascontiguousarray(gx), np.ascontiguousarray(gy), cells)
 
     def _upload_modes(self):
-        mt = np.ascontiguousarray(np.asarray(self.modes, dtype=np.float32).T)
-        self._modes_t = torch.as_tensor(mt, device=self._dev)
         self._modes_bf16 = None
         if self.if_dtype == 'bf16':
             self._n_act_pad = (self.nValidAct + 63) // 64 * 64
