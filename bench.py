@@ -1213,7 +1213,8 @@ def run_ours(args):
             'gpu_launches': int(launches),
             'clocks': clocks,
             'cpu_baseline': cpu,
-            'autotune': {'variant': tune['variant'], 'ms_per_variant': tune['ms']},
+            'autotune': {'variant': tune['variant'], 'ms_per_variant': tune['ms'],
+                         'two_pass': tune.get('two_pass')},
         }
         line.update(extra)
         print(json.dumps(line))
@@ -1245,6 +1246,8 @@ def run_case(args):
             tune = {'variant': args.variant}
         else:
             tune = autotune.tune_pyramid(wfs, batch=args.batch)
+        if args.three_pass:
+            N.call('oopao_pwfs_set_separable', wfs.plan.h, 0)
         ngs ** tel
         wfs.plan.set_amplitude(ngs.intensity, wfs._amplitude_key())
         opd = torch.randn((args.batch, res, res), device='cuda', generator=g) * 50e-9
@@ -1255,6 +1258,7 @@ def run_case(args):
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_pop()
         out = {'case': args.case, 'batch': args.batch, 'reps': args.reps, 'variant': tune['variant'],
+               'two_pass': N.call('oopao_pwfs_separable', wfs.plan.h) == 1,
                'frame_sum': float(frame.double().sum().item())}
     elif args.case == 'dm40':
         tel, ngs, dm, wfs = None, None, None, None
@@ -1314,6 +1318,8 @@ def main():
     ap.add_argument('--batch', type=int, default=16)
     ap.add_argument('--reps', type=int, default=3)
     ap.add_argument('--variant', type=int, default=-1, help='kernel variant for --case (-1: autotune)')
+    ap.add_argument('--three-pass', action='store_true',
+                    help='pwfs20/pwfs40 cases: force the three-pass propagation (masks that do not factorise)')
     args = ap.parse_args()
     if args.case:
         import __graft_entry__

@@ -236,6 +236,13 @@ size_t oopao_dm_bf16_workspace_bytes(int n_act_pad, int batch);
 int oopao_dm_opd_bf16(const void* modes, int n_act_pad, const float* coefs, int n_act, int n_pix, int batch,
                       float scale, const float* base, float* opd, void* workspace, size_t workspace_bytes,
                       void* stream);
+/* The same with the GEMM's batch tile chosen by the caller (autotuner hook,
+ * no reference counterpart): tile_n = 64 or 128 columns per CTA tile, or 0
+ * for the automatic rule (GEMV up to 4 columns, 64 up to 64, else 128); a
+ * non-zero tile_n uses the tensor cores at every batch. */
+int oopao_dm_opd_bf16_tiled(const void* modes, int n_act_pad, const float* coefs, int n_act, int n_pix, int batch,
+                            float scale, const float* base, float* opd, void* workspace, size_t workspace_bytes,
+                            int tile_n, void* stream);
 
 /* Separable influence functions (DeformableMirror.modesComputation,
  * OOPAO/DeformableMirror.py:572-600, with anamorphosisAngle = 0 on a

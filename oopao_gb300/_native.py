@@ -62,6 +62,8 @@ SIGNATURES = {
     'oopao_dm_bf16_workspace_bytes': (c_size_t, [c_int, c_int]),
     'oopao_dm_opd_bf16': (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_float, c_void_p, c_void_p,
                                   c_void_p, c_size_t, c_void_p]),
+    'oopao_dm_opd_bf16_tiled': (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_float, c_void_p, c_void_p,
+                                        c_void_p, c_size_t, c_int, c_void_p]),
     'oopao_cl_screen': (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                 c_int, c_void_p, c_void_p, c_void_p]),
     'oopao_cl_integrate': (c_int, [c_void_p, c_void_p, c_int, c_int, c_float, c_void_p, c_void_p, c_void_p]),

@@ -366,14 +366,22 @@ extern "C" int oopao_dm_modes_bf16(const float* modes_t, int n_act, int n_pix, i
 
 extern "C" size_t oopao_dm_bf16_workspace_bytes(int n_act_pad, int batch) {
   if (n_act_pad <= 0 || batch <= 0) return 0;
-  const int bn = batch <= 64 ? 64 : 128;
-  const size_t batch_pad = (size_t)ceil_div(batch, bn) * bn;
+  // padded to the larger tile, so that either tile width fits
+  const size_t batch_pad = (size_t)ceil_div(batch, 128) * 128;
   return 256 + 2 * batch_pad * n_act_pad * 2;
 }
 
 extern "C" int oopao_dm_opd_bf16(const void* modes, int n_act_pad, const float* coefs, int n_act, int n_pix,
                                  int batch, float scale, const float* base, float* opd, void* workspace,
                                  size_t workspace_bytes, void* stream) {
+  return oopao_dm_opd_bf16_tiled(modes, n_act_pad, coefs, n_act, n_pix, batch, scale, base, opd, workspace,
+                                 workspace_bytes, 0, stream);
+}
+
+extern "C" int oopao_dm_opd_bf16_tiled(const void* modes, int n_act_pad, const float* coefs, int n_act, int n_pix,
+                                       int batch, float scale, const float* base, float* opd, void* workspace,
+                                       size_t workspace_bytes, int tile_n, void* stream) {
+  OOPAO_CHECK_ARG(tile_n == 0 || tile_n == 64 || tile_n == 128, "tile_n must be 0 (automatic), 64 or 128");
   OOPAO_CHECK_ARG(modes && coefs && opd && workspace, "NULL argument");
   OOPAO_CHECK_ARG(n_act > 0 && n_pix > 0 && batch > 0, "sizes must be positive");
   OOPAO_CHECK_ARG(n_act_pad >= n_act && n_act_pad % kBK == 0, "n_act_pad must be a multiple of 64 and >= n_act");
@@ -382,7 +390,7 @@ extern "C" int oopao_dm_opd_bf16(const void* modes, int n_act_pad, const float* 
   OOPAO_CHECK_ARG(workspace_bytes >= oopao_dm_bf16_workspace_bytes(n_act_pad, batch), "workspace too small");
   OOPAO_CHECK_ARG(ceil_div(n_pix, kBM) <= 65535, "n_pix above 65535 * 128");
   cudaStream_t st = (cudaStream_t)stream;
-  if (batch <= kGemvMaxBatch) {
+  if (batch <= kGemvMaxBatch && tile_n == 0) {
     OOPAO_CHECK_ARG((size_t)batch * n_act_pad * sizeof(float) <= 200 * 1024, "n_act_pad too large for the GEMV form");
     OOPAO_CUDA_TRY(cudaMemsetAsync(workspace, 0, sizeof(int), st));
     cudaError_t e = cudaSuccess;
@@ -399,7 +407,7 @@ extern "C" int oopao_dm_opd_bf16(const void* modes, int n_act_pad, const float* 
     oopao_count_launches(1);
     return OOPAO_OK;
   }
-  const int bn = batch <= 64 ? 64 : 128;
+  const int bn = tile_n ? tile_n : (batch <= 64 ? 64 : 128);
   const int batch_pad = ceil_div(batch, bn) * bn;
   int* err = reinterpret_cast<int*>(workspace);
   __nv_bfloat16* ct = reinterpret_cast<__nv_bfloat16*>((char*)workspace + 256);

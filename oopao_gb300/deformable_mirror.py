@@ -130,6 +130,11 @@ class DeformableMirror:
         self._upload_modes()
         # the separable projection serves every batch when the IFs factorise
         self.separable_projection = self._sep_host is not None
+        # batches above this go to the BF16 tensor-core GEMM (if_dtype='bf16'),
+        # and the GEMM's batch tile per batch size: [(max batch, 64 or 128)],
+        # empty for the library's rule; both set by autotune.tune_dm
+        self.separable_max_batch = self.SEPARABLE_MAX_BATCH_VS_TC
+        self.tc_tile_rule = []
         self._sep = None
         self._sep_ws = None
         if self._sep_host is not None:
@@ -310,7 +315,7 @@ class DeformableMirror:
         """Path of a projection of B coefficient vectors: 'separable', 'bf16'
         (tensor cores) or 'fp32' (dense CUDA cores)."""
         if self._sep is not None and self.separable_projection and (
-                self._modes_bf16 is None or B <= self.SEPARABLE_MAX_BATCH_VS_TC):
+                self._modes_bf16 is None or B <= self.separable_max_batch):
             return 'separable'
         return 'bf16' if self._modes_bf16 is not None else 'fp32'
 
@@ -353,8 +358,9 @@ class DeformableMirror:
             N.call('oopao_dm_opd_sep_f32', gx, gy, cells, nx, ny, c, self.nValidAct, res, B, float(scale), base, out,
                    ws, ws.numel(), stream)
         elif path == 'bf16':
-            N.call('oopao_dm_opd_bf16', self._modes_bf16, self._n_act_pad, c, self.nValidAct, res * res, B,
-                   float(scale), base, out, ws, ws.numel(), stream)
+            tile = next((t for bound, t in self.tc_tile_rule if B <= bound), 0)
+            N.call('oopao_dm_opd_bf16_tiled', self._modes_bf16, self._n_act_pad, c, self.nValidAct, res * res, B,
+                   float(scale), base, out, ws, ws.numel(), tile, stream)
         else:
             N.call('oopao_dm_opd_acc_f32', self._modes_t, c, self.nValidAct, res * res, B, float(scale), base, out,
                    stream)
