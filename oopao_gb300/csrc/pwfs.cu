@@ -669,6 +669,10 @@ cudaError_t sep_attrs(oopao_pwfs_plan* p) {
   cudaError_t e = cudaFuncSetAttribute(s->rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_rows);
   for (int m = 0; m < 3 && e == cudaSuccess; m++)
     e = cudaFuncSetAttribute(s->cols[m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_cols(p->res));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(s->cols_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_cols(p->res));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(s->rows_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_rows);
   int dev = 0, sms = 0, occ = 0;
   if (e == cudaSuccess) e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1775,14 +1779,84 @@ extern "C" int oopao_pwfs_jvp(const oopao_pwfs_plan* p, const float* opd0, int o
   return OOPAO_OK;
 }
 
+namespace {
+// Adjoint through the two passes (pwfs_sep.cuh): per chunk of items, the
+// field and the filtered rows of each item's operating point, the adjoint
+// column pass (G_k, Gbar_k, conjugate column filter -> V_k on the pupil
+// rows), the adjoint row pass (conjugate row filter, Im(. conj(E~_k))
+// summed over slots of points) and the fixed-order sum of the slots, scaled
+// to OPD units.  OOPAO_ERR_WORKSPACE (nothing launched) when one item does
+// not fit.
+int vjp_sep(const oopao_pwfs_plan* p, const float* opd, const float* fbar, double phase_scale, int batch,
+            float* opd_bar, char* base, size_t usable, cudaStream_t st) {
+  const SepPasses* s = p->sep;
+  const int n = p->n, res = p->res, k = p->k, cam = p->cam, ng = p->ngroups;
+  const int rblocks = ceil_div(res, s->l_rows);
+  auto row_slots = [&](int bc) {
+    const int want = ceil_div(8 * std::max(1, p->sep_cols_ctas), rblocks * bc);
+    int best = 1;
+    for (int d = 1; d <= k && d <= kMaxSlotsBinned; d++) {
+      if (k % d) continue;
+      best = d;
+      if (d >= want) break;
+    }
+    return best;
+  };
+  auto chunk_bytes = [&](int bc, int ksr) {
+    return (size_t)bc * ((size_t)ng * res * n * 8 + (size_t)res * res * 8 + (size_t)k * res * n * 8 +
+                         (size_t)ksr * res * res * 4) + 1024;
+  };
+  int bc = (int)std::min<size_t>((size_t)batch, std::max<size_t>(1, p->l2_budget / chunk_bytes(1, 1)));
+  int ksr = row_slots(bc);
+  while (bc > 1 && chunk_bytes(bc, ksr) > usable) {
+    bc = (bc + 1) / 2;
+    ksr = row_slots(bc);
+  }
+  if (chunk_bytes(bc, ksr) > usable) return OOPAO_ERR_WORKSPACE;
+  float2* y = (float2*)base;
+  float2* fld = y + (size_t)bc * ng * res * n;
+  float2* v = fld + (size_t)bc * res * res;
+  float* part = (float*)(v + (size_t)bc * k * res * n);
+  int launches = 0;
+  for (int b0 = 0; b0 < batch; b0 += bc) {
+    const int nb = std::min(bc, batch - b0);
+    const int ksc = sep_ksplit(p, nb, kMaxSlotsBinned);
+    pwfs_field<<<dim3(ceil_div(res * res, 256), nb), 256, 0, st>>>(opd + (size_t)b0 * res * res, (float)phase_scale,
+                                                                   p->d_amp, fld, res * res);
+    SepRowsArgs ra{p->d_tw, fld, p->d_growfac, p->d_mrow, y, res, ng, p->off};
+    s->rows<<<dim3(rblocks, ng, nb), s->t * s->l_rows, s->smem_rows, st>>>(ra);
+    SepAdjArgs ca{p->d_tw, p->d_mcol, p->d_mrow, y, p->d_group, p->d_colfac, p->d_growfac, weights_of(p),
+                  fbar + (size_t)b0 * cam * cam, fld, v, part, res, p->off, ng, k / ksc, ksc, p->bin, cam};
+    s->cols_adj<<<dim3(n / s->l_cols, ksc, nb), s->t * s->l_cols, s->smem_cols(res), st>>>(ca);
+    SepAdjArgs rb = ca;
+    rb.slot_pts = k / ksr;
+    rb.ksplit = ksr;
+    s->rows_adj<<<dim3(rblocks, ksr, nb), s->t * s->l_rows, s->smem_rows, st>>>(rb);
+    pwfs_reduce_scaled<<<dim3(ceil_div(res * res, 256), nb), 256, 0, st>>>(
+        part, opd_bar + (size_t)b0 * res * res, res * res, ksr, (float)phase_scale);
+    launches += 5;
+  }
+  oopao_count_launches(launches);
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}
+}  // namespace
+
 extern "C" int oopao_pwfs_vjp(const oopao_pwfs_plan* p, const float* opd, const float* fbar, double phase_scale,
                               int batch, float* opd_bar, void* ws, size_t ws_bytes, void* stream) {
   OOPAO_CHECK_ARG(p && opd && fbar && opd_bar && ws, "NULL argument");
   OOPAO_CHECK_ARG(batch >= 1, "batch must be >= 1");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (sep_applies(p, false, false) && p->n % p->bin == 0) {
+    uintptr_t b2 = ((uintptr_t)ws + 255) & ~(uintptr_t)255;
+    if (ws_bytes > b2 - (uintptr_t)ws) {
+      const int r = vjp_sep(p, opd, fbar, phase_scale, batch, opd_bar, (char*)b2, ws_bytes - (b2 - (uintptr_t)ws), st);
+      if (r != OOPAO_ERR_WORKSPACE) return r;  // else the three-pass adjoint below
+    }
+  }
   const AdPasses* ad = nullptr;
   int st0 = ad_setup(p, &ad);
   if (st0) return st0;
-  cudaStream_t st = (cudaStream_t)stream;
   const FastPasses* f = p->fast;
   const int n = p->n, res = p->res, k = p->k, cam = p->cam;
   uintptr_t base = ((uintptr_t)ws + 255) & ~(uintptr_t)255;

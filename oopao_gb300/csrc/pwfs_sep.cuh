@@ -27,8 +27,10 @@
 #include "xchg.cuh"
 
 // One line through forward FFT -> diagonal filter -> inverse FFT, by the T
-// threads of the line (butterflies j = t, t+T, ...).  load(e) gives input
-// element e of the line, filt(u) the filter at frequency u, store(p, j, v)
+// threads of the line (butterflies j = t, t+T, ...).  load(p, m, j) gives
+// input element j + m*R2 of the line (butterfly j = t + p*T; the same
+// positions store() receives for the outputs, so one chain's outputs can
+// feed the next from registers), filt(u) the filter at frequency u, store(p, j, v)
 // receives the outputs v[q] = line[j + q*R2] (q < R1) of butterfly j = t+p*T.
 // x1/x2: this line's forward/inverse exchange rows (stage outputs at j*RP+q).
 // after_a() runs right after the barrier that ends the input loads.
@@ -45,7 +47,7 @@ __device__ __forceinline__ void sep_chain(int t, float2* x1, float2* x2, const f
     if (j < R2) {
       float2 v[R1];
 #pragma unroll
-      for (int m = 0; m < R1; m++) v[m] = load(j + m * R2);
+      for (int m = 0; m < R1; m++) v[m] = load(p, m, j);
       dft<R1, false>(v);
 #pragma unroll
       for (int q = 0; q < R1; q++) x1[j * RP1 + q] = v[q];
@@ -130,8 +132,8 @@ __global__ void __launch_bounds__(T* L) pwfs_srows(SepRowsArgs a) {
   float2* y = a.y + (((size_t)b * a.ng + g) * res + row) * N;
   sep_chain<N, R1, R2, T, R1P, R2P>(
       t, b1 + l * LS1, b2 + l * LS2, tw, twi,
-      [&](int e) {
-        const int jc = e - off;
+      [&](int, int m, int j) {
+        const int jc = j + m * R2 - off;
         return (active && jc >= 0 && jc < res) ? cmul(fld[jc], rf[jc]) : make_float2(0.f, 0.f);
       },
       [&](int u) { return mf[u]; },
@@ -247,8 +249,8 @@ __global__ void __launch_bounds__(T* L) __maxnreg__(MAXREG) pwfs_scols(SepColsAr
     float2* go = (MODE == kSepStore) ? a.gout + (size_t)kk * N * N + c : nullptr;
     sep_chain<N, R1, R2, T, R1P, R2P>(
         t, b1 + l * LS1, b2 + l * LS2, tw, twi,
-        [&](int e) {
-          const int i = e - off;
+        [&](int, int m, int j) {
+          const int i = j + m * R2 - off;
           return (i >= 0 && i < res) ? cmul(yt[i * L], cf[i]) : make_float2(0.f, 0.f);
         },
         [&](int u) { return mf[u]; },
@@ -309,10 +311,197 @@ __global__ void __launch_bounds__(T* L) __maxnreg__(MAXREG) pwfs_scols(SepColsAr
   }
 }
 
+// ---- adjoint (VJP) through the two passes ----
+// Per item and point k, with G_k the forward field and the camera cotangent
+// fbar: Gbar_k = 2 w_k fbar(binned pixel) G_k; the adjoint of the two 1-D
+// filters is the same chain with the conjugate factors (forward FFT,
+// * conj(m), inverse FFT: the transposes of the unnormalised transforms),
+// so E~bar_k = (Fr^-1 conj(mrow) Fr)(Fc^-1 conj(mcol) Fc) Gbar_k on the
+// pupil, and phibar = sum_k Im(E~bar_k conj(E~_k)) with E~_k = W rowfac_k
+// colfac_k.  Column pass: G_k from the filtered rows (as in pwfs_scols),
+// Gbar_k formed in registers and, as the next chain's stage-A inputs (the
+// same thread positions), sent through the conjugate column filter; the
+// pupil rows of the result, times conj(colfac_k), go to V_k [res][N].  Row
+// pass: per pupil row, each point's V_k row through the conjugate row filter,
+// Im(. conj(W rowfac_k)) summed over a slot of points.
+struct SepAdjArgs {
+  const float2* tw;
+  const float2* mcol;    // [N]
+  const float2* mrow;    // [N]
+  const float2* y;       // [B][ng][res][N] filtered rows of the operating point
+  const int* group;      // [K]
+  const float2* colfac;  // [K][res]
+  const float2* rowfac;  // [groups][res]
+  const float* weights;  // [K] or null
+  const float* fbar;     // [B][cam][cam] camera-frame cotangent
+  const float2* field;   // [B][res][res] W
+  float2* v;             // [B][K][res][N]
+  float* phibar;         // [B][ksplit][res][res] slot partials (row pass)
+  int res, off, ng, slot_pts, ksplit, bin, cam;
+};
+
+// Two chains per point with Gbar held between them: 128 registers keep it
+// (with 96 it spilled ~300 bytes per thread).
+template <int N, int R1, int R2, int T, int L>
+__global__ void __maxnreg__(128) pwfs_scols_adj(SepAdjArgs a) {
+  using S = SepColsSmem<N, R1, R2, T, L>;
+  constexpr int R1P = S::LAY1 >> 16, LS1 = S::LS1;
+  constexpr int R2P = S::LAY2 >> 16, LS2 = S::LS2;
+  constexpr int PBA = (R2 + T - 1) / T;
+  constexpr bool ALIAS = S::ALIAS;
+  extern __shared__ __align__(16) float2 sm[];
+  float2* tw = sm;
+  float2* twi = sm + N;
+  float2* mf = sm + 2 * N;
+  float2* b1 = sm + S::kXch;
+  float2* b2 = ALIAS ? b1 : b1 + L * LS1;
+  const int res = a.res, off = a.off;
+  float2* tile = sm + S::kTiles;
+  const int tid = threadIdx.x;
+  const int l = tid % L, t = tid / L;
+  for (int i = tid; i < N; i += T * L) {
+    tw[i] = a.tw[(i % R1) * (i / R1)];
+    const float2 w = a.tw[(i % R2) * (i / R2)];
+    twi[i] = make_float2(w.x, -w.y);
+    mf[i] = a.mcol[i];
+  }
+  const int b = blockIdx.z, slot = blockIdx.y, c0 = blockIdx.x * L, c = c0 + l;
+  const int kbeg = slot * a.slot_pts, kend = kbeg + a.slot_pts;
+  const float* fb = a.fbar + (size_t)b * a.cam * a.cam + c / a.bin;
+  auto issue = [&](int kk) {
+    const float2* src = a.y + ((size_t)b * a.ng + a.group[kk]) * res * N + c0;
+    for (int i = tid; i < res * (L / 2); i += T * L) {
+      const int row = i / (L / 2), ch = i - (i / (L / 2)) * (L / 2);
+      cp_async16(tile + row * L + 2 * ch, src + (size_t)row * N + 2 * ch);
+    }
+    const float2* cfs = a.colfac + (size_t)kk * res;
+    for (int i = tid; i < res / 2; i += T * L) cp_async16(tile + res * L + 2 * i, cfs + 2 * i);
+    cp_async_commit();
+  };
+  issue(kbeg);
+  for (int kk = kbeg; kk < kend; kk++) {
+    cp_async_wait<0>();
+    __syncthreads();
+    const float2* yt = tile + l;
+    const float2* cf = tile + res * L;
+    const float w2 = 2.f * (a.weights ? a.weights[kk] : 1.f);
+    float2 gb[PBA][R1];  // Gbar of this column, rows j + q*R2
+    sep_chain<N, R1, R2, T, R1P, R2P>(
+        t, b1 + l * LS1, b2 + l * LS2, tw, twi,
+        [&](int, int m, int j) {
+          const int i = j + m * R2 - off;
+          return (i >= 0 && i < res) ? cmul(yt[i * L], cf[i]) : make_float2(0.f, 0.f);
+        },
+        [&](int u) { return mf[u]; },
+        [&](int p, int j, const float2* v) {
+#pragma unroll
+          for (int q = 0; q < R1; q++) {
+            const float s = w2 * __ldg(fb + ((j + q * R2) / a.bin) * a.cam);
+            gb[p][q] = make_float2(s * v[q].x, s * v[q].y);
+          }
+        },
+        [&] {
+          if (kk + 1 < kend) issue(kk + 1);
+        });
+    if (ALIAS) __syncthreads();  // the first chain's last exchange reads are done
+    float2* vo = a.v + ((size_t)b * gridDim.y * a.slot_pts + kk) * res * N + c;
+    const float2* cfg = a.colfac + (size_t)kk * res;
+    sep_chain<N, R1, R2, T, R1P, R2P>(
+        t, b1 + l * LS1, b2 + l * LS2, tw, twi,
+        [&](int p, int m, int) { return gb[p][m]; },
+        [&](int u) { return cconj(mf[u]); },
+        [&](int, int j, const float2* v) {
+#pragma unroll
+          for (int q = 0; q < R1; q++) {
+            const int i = j + q * R2 - off;
+            if (i >= 0 && i < res) vo[(size_t)i * N] = cmul(v[q], cconj(__ldg(cfg + i)));
+          }
+        },
+        [] {});
+  }
+}
+
+template <int N, int R1, int R2, int T, int L>
+__global__ void __maxnreg__(128) pwfs_srows_adj(SepAdjArgs a) {
+  constexpr int R1P = pad_odd(R1), R2P = pad_odd(R2);
+  constexpr int LS1 = xchg_stride(R2 * R1P, T, L, R1P, R2, R1);
+  constexpr int LS2 = xchg_stride(R1 * R2P, T, L, R2P, R1, R2);
+  constexpr bool ALIAS = (R1 + T - 1) / T == 1;
+  constexpr int PBA = (R2 + T - 1) / T;
+  extern __shared__ float2 sm[];
+  float2* tw = sm;
+  float2* twi = sm + N;
+  float2* mf = sm + 2 * N;
+  float2* b1 = sm + 3 * N;
+  float2* b2 = ALIAS ? b1 : b1 + L * LS1;
+  const int tid = threadIdx.x;
+  const int l = tid / T, t = tid - (tid / T) * T;
+  for (int i = tid; i < N; i += T * L) {
+    tw[i] = a.tw[(i % R1) * (i / R1)];
+    const float2 w = a.tw[(i % R2) * (i / R2)];
+    twi[i] = make_float2(w.x, -w.y);
+    mf[i] = cconj(a.mrow[i]);
+  }
+  __syncthreads();
+  const int res = a.res, off = a.off;
+  const int b = blockIdx.z, slot = blockIdx.y, row = blockIdx.x * L + l;
+  const bool active = row < res;
+  const int K = gridDim.y * a.slot_pts;
+  const int kbeg = slot * a.slot_pts, kend = kbeg + a.slot_pts;
+  const float2* fld = a.field + ((size_t)b * res + (active ? row : 0)) * res;
+  float acc[PBA][R1];
+#pragma unroll
+  for (int p = 0; p < PBA; p++)
+#pragma unroll
+    for (int q = 0; q < R1; q++) acc[p][q] = 0.f;
+  for (int kk = kbeg; kk < kend; kk++) {
+    if (ALIAS && kk > kbeg) __syncthreads();  // the previous point's exchange reads are done
+    const float2* vr = a.v + (((size_t)b * K + kk) * res + (active ? row : 0)) * N;
+    const float2* rf = a.rowfac + (size_t)a.group[kk] * res;
+    // an offset the compiler cannot see is zero keeps the field loads inside
+    // the loop instead of hoisted into registers across points
+    int zero;
+    asm volatile("mov.b32 %0, 0;" : "=r"(zero));
+    const float2* fr = fld + zero;
+    sep_chain<N, R1, R2, T, R1P, R2P>(
+        t, b1 + l * LS1, b2 + l * LS2, tw, twi,
+        [&](int, int m, int j) { return active ? vr[j + m * R2] : make_float2(0.f, 0.f); },
+        [&](int u) { return mf[u]; },
+        [&](int p, int j, const float2* v) {
+          if (active) {
+#pragma unroll
+            for (int q = 0; q < R1; q++) {
+              const int jc = j + q * R2 - off;
+              if (jc >= 0 && jc < res) {
+                const float2 e = cmul(fr[jc], __ldg(rf + jc));
+                acc[p][q] += v[q].y * e.x - v[q].x * e.y;
+              }
+            }
+          }
+        },
+        [] {});
+  }
+  if (!active) return;
+  float* out = a.phibar + (((size_t)b * a.ksplit + slot) * res + row) * res;
+#pragma unroll
+  for (int p = 0; p < PBA; p++) {
+    const int j = t + p * T;
+    if (j < R2) {
+#pragma unroll
+      for (int q = 0; q < R1; q++) {
+        const int jc = j + q * R2 - off;
+        if (jc >= 0 && jc < res) out[jc] = acc[p][q];
+      }
+    }
+  }
+}
+
 struct SepPasses {
   int n, r1, r2, t, l_rows, l_cols;
   void (*rows)(SepRowsArgs);
   void (*cols[3])(SepColsArgs);  // indexed by kSepIntensity / kSepTangent / kSepStore
+  void (*cols_adj)(SepAdjArgs);
+  void (*rows_adj)(SepAdjArgs);
   size_t smem_rows;
   size_t (*smem_cols)(int res);
 };
@@ -336,6 +525,8 @@ SepPasses make_sep() {
   s.cols[kSepIntensity] = pwfs_scols<N, R1, R2, T, LC, kSepIntensity, MAXREG>;
   s.cols[kSepTangent] = pwfs_scols<N, R1, R2, T, LC, kSepTangent, MAXREG>;
   s.cols[kSepStore] = pwfs_scols<N, R1, R2, T, LC, kSepStore, MAXREG>;
+  s.cols_adj = pwfs_scols_adj<N, R1, R2, T, LC>;
+  s.rows_adj = pwfs_srows_adj<N, R1, R2, T, LR>;
   s.smem_rows = sizeof(float2) * (3 * (size_t)N + (size_t)LR * LSR);
   s.smem_cols = &SepColsSmem<N, R1, R2, T, LC>::bytes;
   return s;
