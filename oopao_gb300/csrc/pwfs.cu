@@ -1061,8 +1061,8 @@ bool sep_applies(const oopao_pwfs_plan* p, bool focal, bool raw) {
 // points, with one CTA's time of tail.  Against a sweep of every divisor on
 // GB300 (20x20 at batch 1/16/100, 40x40 at batch 1/4/16) it picks the
 // fastest or one within 3%.
-int sep_ksplit(const oopao_pwfs_plan* p, int bc, int cap) {
-  if (p->ksplit > 0 && p->ksplit <= cap) return p->ksplit;
+int sep_ksplit(const oopao_pwfs_plan* p, int bc, int cap, bool use_set = true) {
+  if (use_set && p->ksplit > 0 && p->ksplit <= cap) return p->ksplit;
   const int blocks = p->n / p->sep->l_cols, resident = std::max(1, p->sep_cols_ctas);
   int best = 1;
   double best_t = 1e300;
@@ -1664,16 +1664,18 @@ int jvp_sep(const oopao_pwfs_plan* p, const float* opd0, int opd0_batch, const f
   const size_t avail = usable - fixed;
   int bc = opd0_batch == 1 ? batch : 1;
   bc = (int)std::min<size_t>((size_t)bc, std::max<size_t>(1, p->l2_budget / sep_chunk_bytes(p, 1, 1, true)));
-  int ks = sep_ksplit(p, bc, kMaxSlotsBinned);
+  // slot counts from the model: a count set for measure calls (autotuner) was
+  // timed on another batch and another kernel form
+  int ks = sep_ksplit(p, bc, kMaxSlotsBinned, false);
   while (bc > 1 && sep_chunk_bytes(p, bc, ks, true) > avail) {
     bc = (bc + 1) / 2;
-    ks = sep_ksplit(p, bc, kMaxSlotsBinned);
+    ks = sep_ksplit(p, bc, kMaxSlotsBinned, false);
   }
   if (sep_chunk_bytes(p, bc, ks, true) > avail) return OOPAO_ERR_WORKSPACE;
   float2* y = (float2*)chunk;
   float2* fld = y + (size_t)bc * ng * res * n;
   float* part = (float*)(fld + (size_t)bc * res * res);
-  const int ks0 = sep_ksplit(p, 1, kMaxSlotsBinned);
+  const int ks0 = sep_ksplit(p, 1, kMaxSlotsBinned, false);
   int launches = 0;
   for (int b0 = 0; b0 < batch; b0 += bc) {
     const int nb = std::min(bc, batch - b0);
@@ -1820,7 +1822,7 @@ int vjp_sep(const oopao_pwfs_plan* p, const float* opd, const float* fbar, doubl
   int launches = 0;
   for (int b0 = 0; b0 < batch; b0 += bc) {
     const int nb = std::min(bc, batch - b0);
-    const int ksc = sep_ksplit(p, nb, kMaxSlotsBinned);
+    const int ksc = sep_ksplit(p, nb, kMaxSlotsBinned, false);
     pwfs_field<<<dim3(ceil_div(res * res, 256), nb), 256, 0, st>>>(opd + (size_t)b0 * res * res, (float)phase_scale,
                                                                    p->d_amp, fld, res * res);
     SepRowsArgs ra{p->d_tw, fld, p->d_growfac, p->d_mrow, y, res, ng, p->off};
