@@ -5,7 +5,10 @@
 // pass; N must be a multiple of LC), and the column pass's register cap.
 // Measured on GB300 (20x20 at batch 1-100, 40x40 at batch 1-16): the first
 // entry of each size is the fastest or within 1%; register caps of 72-80
-// (more resident CTAs, with spills) and the other radix orders were slower.
+// (more resident CTAs, with spills), the other radix orders, and separate
+// forward/inverse exchange buffers where one could be shared (two barriers
+// fewer per point, but a third fewer resident warps: 3-17% slower) were
+// slower.
 #include "common.cuh"
 #include "pwfs_sep.cuh"
 

@@ -35,12 +35,18 @@
 // x1/x2: this line's forward/inverse exchange rows (stage outputs at j*RP+q).
 // after_a() runs right after the barrier that ends the input loads.
 // Every thread of the CTA calls it (it holds CTA-wide barriers).
-template <int N, int R1, int R2, int T, int RP1, int RP2, class Load, class Filt, class Store, class AfterA>
-__device__ __forceinline__ void sep_chain(int t, float2* x1, float2* x2, const float2* tw, const float2* twi,
-                                          Load load, Filt filt, Store store, AfterA after_a) {
+// SHARE: x2 is x1 (one exchange buffer, one more barrier; needs one stage-B
+// butterfly per thread).  before_last() runs just before the barrier that
+// ends the forward half.
+template <int N, int R1, int R2, int T, int RP1, int RP2, bool SHARE, class Load, class Filt, class Store,
+          class AfterA, class BeforeLast>
+__device__ __forceinline__ void sep_chain_x(int t, float2* x1, float2* x2, const float2* tw, const float2* twi,
+                                            Load load, Filt filt, Store store, AfterA after_a,
+                                            BeforeLast before_last) {
   constexpr int PBA = (R2 + T - 1) / T;  // forward stage A / inverse stage B' butterflies
   constexpr int PBB = (R1 + T - 1) / T;  // forward stage B / inverse stage A' butterflies
-  constexpr bool ALIAS = PBB == 1;       // x2 reuses x1 after a barrier
+  static_assert(!SHARE || PBB == 1, "a shared exchange needs one stage-B butterfly per thread");
+  constexpr bool ALIAS = SHARE;
 #pragma unroll
   for (int p = 0; p < PBA; p++) {
     const int j = t + p * T;
@@ -76,6 +82,7 @@ __device__ __forceinline__ void sep_chain(int t, float2* x1, float2* x2, const f
       for (int q = 0; q < R2; q++) x2[j * RP2 + q] = v[q];
     }
   }
+  before_last();
   __syncthreads();
 #pragma unroll
   for (int p = 0; p < PBA; p++) {
@@ -91,6 +98,15 @@ __device__ __forceinline__ void sep_chain(int t, float2* x1, float2* x2, const f
       store(p, j, v);
     }
   }
+}
+
+// The chain with the default exchange: shared whenever each thread holds one
+// stage-B butterfly.
+template <int N, int R1, int R2, int T, int RP1, int RP2, class Load, class Filt, class Store, class AfterA>
+__device__ __forceinline__ void sep_chain(int t, float2* x1, float2* x2, const float2* tw, const float2* twi,
+                                          Load load, Filt filt, Store store, AfterA after_a) {
+  sep_chain_x<N, R1, R2, T, RP1, RP2, (R1 + T - 1) / T == 1>(t, x1, x2, tw, twi, load, filt, store, after_a,
+                                                               [] {});
 }
 
 struct SepRowsArgs {
@@ -182,20 +198,20 @@ __device__ __forceinline__ void cp_async_wait() {
 
 // Shared memory of the column pass: twiddles, filter, exchange, then the
 // prefetch buffer of a point's Y' tile [res][L] and colfac row [res].
-template <int N, int R1, int R2, int T, int L>
+template <int N, int R1, int R2, int T, int L, bool SHARE = (R1 + T - 1) / T == 1>
 struct SepColsSmem {
   static constexpr int LAY1 = cols_layout(R1, R2, T, L), LAY2 = cols_layout(R2, R1, T, L);
   static constexpr int LS1 = LAY1 & 0xFFFF, LS2 = LAY2 & 0xFFFF;
-  static constexpr bool ALIAS = (R1 + T - 1) / T == 1;
+  static constexpr bool ALIAS = SHARE;
   static constexpr size_t kXch = 3 * (size_t)N;                                   // float2 offset
   static constexpr size_t kTiles = kXch + (size_t)L * (ALIAS ? imax(LS1, LS2) : LS1 + LS2);
   static __host__ __device__ size_t tile(int res) { return (size_t)res * (L + 1); }  // float2 per buffer
   static size_t bytes(int res) { return sizeof(float2) * (kTiles + tile(res)); }
 };
 
-template <int N, int R1, int R2, int T, int L, int MODE, int MAXREG>
+template <int N, int R1, int R2, int T, int L, int MODE, int MAXREG, bool SHARE>
 __global__ void __launch_bounds__(T* L) __maxnreg__(MAXREG) pwfs_scols(SepColsArgs a) {
-  using S = SepColsSmem<N, R1, R2, T, L>;
+  using S = SepColsSmem<N, R1, R2, T, L, SHARE>;
   constexpr int R1P = S::LAY1 >> 16, LS1 = S::LS1;
   constexpr int R2P = S::LAY2 >> 16, LS2 = S::LS2;
   constexpr int PBA = (R2 + T - 1) / T;
@@ -237,17 +253,23 @@ __global__ void __launch_bounds__(T* L) __maxnreg__(MAXREG) pwfs_scols(SepColsAr
   for (int p = 0; p < PBA; p++)
 #pragma unroll
     for (int q = 0; q < R1; q++) acc[p][q] = 0.f;
-  for (int kk = kbeg; kk < kend; kk++) {
+  if constexpr (!SHARE) {
     cp_async_wait<0>();
-    // the tile is visible to every thread, and the previous point's
-    // exchange reads are done (the exchange buffers are reused)
     __syncthreads();
+  }
+  for (int kk = kbeg; kk < kend; kk++) {
+    if constexpr (SHARE) {
+      cp_async_wait<0>();
+      // the tile is visible to every thread, and the previous point's
+      // exchange reads are done (the exchange buffer is reused)
+      __syncthreads();
+    }
     const float2* yt = tile + l;
     const float2* cf = tile + res * L;
     const float w = a.weights ? a.weights[kk] : 1.f;
     const float2* gi = (MODE == kSepTangent) ? a.g0 + (size_t)kk * N * N + c : nullptr;
     float2* go = (MODE == kSepStore) ? a.gout + (size_t)kk * N * N + c : nullptr;
-    sep_chain<N, R1, R2, T, R1P, R2P>(
+    sep_chain_x<N, R1, R2, T, R1P, R2P, SHARE>(
         t, b1 + l * LS1, b2 + l * LS2, tw, twi,
         [&](int, int m, int j) {
           const int i = j + m * R2 - off;
@@ -269,6 +291,12 @@ __global__ void __launch_bounds__(T* L) __maxnreg__(MAXREG) pwfs_scols(SepColsAr
         },
         [&] {
           if (kk + 1 < kend) issue(kk + 1);
+        },
+        [&] {
+          // separate exchanges: the next point's tile lands before the
+          // barrier that ends this point's forward half (its stage A follows
+          // this point's stage B' with no barrier in between)
+          if constexpr (!SHARE) cp_async_wait<0>();
         });
   }
   if constexpr (MODE == kSepStore) return;
@@ -507,7 +535,7 @@ struct SepPasses {
 };
 
 // MAXREG caps the column pass's registers per thread (its occupancy).
-template <int N, int R1, int R2, int T, int LR, int LC, int MAXREG>
+template <int N, int R1, int R2, int T, int LR, int LC, int MAXREG, bool SHARE = (R1 + T - 1) / T == 1>
 SepPasses make_sep() {
   static_assert(N % LC == 0, "column blocks must tile N");
   constexpr int R1P = pad_odd(R1), R2P = pad_odd(R2);
@@ -516,19 +544,19 @@ SepPasses make_sep() {
   constexpr int LSR2 = xchg_stride(R1 * R2P, T, LR, R2P, R1, R2);
   constexpr int LSR = ALIAS ? imax(LSR1, LSR2) : LSR1 + LSR2;
   constexpr int LSC1 = cols_layout(R1, R2, T, LC) & 0xFFFF, LSC2 = cols_layout(R2, R1, T, LC) & 0xFFFF;
-  constexpr int LSC = ALIAS ? imax(LSC1, LSC2) : LSC1 + LSC2;
+  constexpr int LSC = SHARE ? imax(LSC1, LSC2) : LSC1 + LSC2;
   // the binning epilogue reuses the exchange as [LC][N] floats
   static_assert((size_t)LC * LSC * 2 >= (size_t)LC * N, "exchange too small for the binning rows");
   SepPasses s;
   s.n = N; s.r1 = R1; s.r2 = R2; s.t = T; s.l_rows = LR; s.l_cols = LC;
   s.rows = pwfs_srows<N, R1, R2, T, LR>;
-  s.cols[kSepIntensity] = pwfs_scols<N, R1, R2, T, LC, kSepIntensity, MAXREG>;
-  s.cols[kSepTangent] = pwfs_scols<N, R1, R2, T, LC, kSepTangent, MAXREG>;
-  s.cols[kSepStore] = pwfs_scols<N, R1, R2, T, LC, kSepStore, MAXREG>;
+  s.cols[kSepIntensity] = pwfs_scols<N, R1, R2, T, LC, kSepIntensity, MAXREG, SHARE>;
+  s.cols[kSepTangent] = pwfs_scols<N, R1, R2, T, LC, kSepTangent, MAXREG, SHARE>;
+  s.cols[kSepStore] = pwfs_scols<N, R1, R2, T, LC, kSepStore, MAXREG, SHARE>;
   s.cols_adj = pwfs_scols_adj<N, R1, R2, T, LC>;
   s.rows_adj = pwfs_srows_adj<N, R1, R2, T, LR>;
   s.smem_rows = sizeof(float2) * (3 * (size_t)N + (size_t)LR * LSR);
-  s.smem_cols = &SepColsSmem<N, R1, R2, T, LC>::bytes;
+  s.smem_cols = &SepColsSmem<N, R1, R2, T, LC, SHARE>::bytes;
   return s;
 }
 

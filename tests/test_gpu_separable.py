@@ -159,3 +159,26 @@ def test_two_pass_adjoint(lib, res, nsub, mod, k):
         assert O.rel_l2(a2, a3) < 1e-5
     finally:
         N.load().oopao_pwfs_plan_destroy(h)
+
+
+@pytest.mark.parametrize('res,nsub,mod,k', [(120, 20, 3, 48), (240, 40, 5, 96)])
+def test_every_two_pass_plan(lib, res, nsub, mod, k):
+    """Every compile-time two-pass plan of the size (radix orders, columns per
+    CTA, shared or separate exchange buffers) and a spread of slot counts give
+    the three-pass frames."""
+    N = lib
+    h, geom, tt, inten, pupil = sensor(N, res, nsub, mod, k)
+    try:
+        phase = np.random.default_rng(13).standard_normal((2, res, res)) * pupil
+        N.call('oopao_pwfs_set_separable', h, 0)
+        f3, _ = measure(N, h, phase, geom.N, geom.cam, want_raw=False)
+        for sp in range(1, N.call('oopao_pwfs_num_separable', h) + 1):
+            N.call('oopao_pwfs_set_separable', h, sp)
+            assert N.call('oopao_pwfs_separable', h) == 1
+            for ks in (0, 1, 3, k // 2):
+                N.call('oopao_pwfs_set_launch', h, 0, 0, 0, ks)
+                f2, _ = measure(N, h, phase, geom.N, geom.cam, want_raw=False)
+                assert O.rel_l2(f2, f3) < TOL_PATHS, (sp, ks)
+            N.call('oopao_pwfs_set_launch', h, 0, 0, 0, 0)
+    finally:
+        N.load().oopao_pwfs_plan_destroy(h)
