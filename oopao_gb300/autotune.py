@@ -216,6 +216,8 @@ def tune_dm(dm, batches=(1, 4, 16, 32, 64, 128, 300), reps=5, force=False, verbo
                 sep_max = B
             else:
                 break
+        if sep_max == batches[-1]:
+            sep_max = 1 << 30   # the separable projection won every timed batch
     rule = []
     if has_tc:
         for B in batches:

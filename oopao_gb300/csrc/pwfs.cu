@@ -111,6 +111,11 @@ struct oopao_pwfs_plan {
   float2* d_mrow;                 // [n] factor along a row (column frequency)
   float2* d_mcol;                 // [n] factor along a column (row frequency)
   int sep_cols_ctas;              // resident column-pass CTAs on this device
+  // the two-pass plan of the tangent and adjoint passes: the first
+  // candidate, whatever the measure calls were tuned to (their kernel forms
+  // differ), and its resident column-pass CTAs
+  const struct SepPasses* sep_ad;
+  int sep_ad_ctas;
   // signal processing
   int sp_mode, nq, n2d, n_signal, cam2;
   int q_r0[4], q_c0[4];
@@ -662,15 +667,15 @@ bool factor_mask(const float2* m, int n, std::vector<float2>* mrow, std::vector<
   return true;
 }
 
-// Opt the plan's two-pass kernels into their shared memory and record the
-// resident column-pass CTAs on this device.
-cudaError_t sep_attrs(oopao_pwfs_plan* p) {
-  const SepPasses* s = p->sep;
+// Opt a two-pass plan's kernels into their shared memory for pupils of
+// `res` pixels and return in *ctas its resident column-pass CTAs on this
+// device.
+cudaError_t sep_attrs_for(const SepPasses* s, int res, int* ctas) {
   cudaError_t e = cudaFuncSetAttribute(s->rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_rows);
   for (int m = 0; m < 3 && e == cudaSuccess; m++)
-    e = cudaFuncSetAttribute(s->cols[m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_cols(p->res));
+    e = cudaFuncSetAttribute(s->cols[m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_cols(res));
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(s->cols_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_cols(p->res));
+    e = cudaFuncSetAttribute(s->cols_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_cols(res));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(s->rows_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_rows);
   int dev = 0, sms = 0, occ = 0;
@@ -678,8 +683,14 @@ cudaError_t sep_attrs(oopao_pwfs_plan* p) {
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e == cudaSuccess)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, s->cols[kSepIntensity], s->t * s->l_cols,
-                                                      s->smem_cols(p->res));
-  if (e == cudaSuccess) p->sep_cols_ctas = sms * std::max(occ, 1);
+                                                      s->smem_cols(res));
+  if (e == cudaSuccess) *ctas = sms * std::max(occ, 1);
+  return e;
+}
+
+cudaError_t sep_attrs(oopao_pwfs_plan* p) {
+  cudaError_t e = sep_attrs_for(p->sep, p->res, &p->sep_cols_ctas);
+  if (e == cudaSuccess) e = sep_attrs_for(p->sep_ad, p->res, &p->sep_ad_ctas);
   return e;
 }
 
@@ -832,6 +843,7 @@ extern "C" int oopao_pwfs_plan_create(oopao_pwfs_plan** out, int res, int n, int
   {
     const SepPasses* sc = nullptr;
     p->sep = sep_candidates(n, &sc) > 0 ? sc : nullptr;
+    p->sep_ad = p->sep;
     p->sep_on = true;
   }
   if (e == cudaSuccess) e = sep_setup(p, mask_host);
@@ -1061,9 +1073,10 @@ bool sep_applies(const oopao_pwfs_plan* p, bool focal, bool raw) {
 // points, with one CTA's time of tail.  Against a sweep of every divisor on
 // GB300 (20x20 at batch 1/16/100, 40x40 at batch 1/4/16) it picks the
 // fastest or one within 3%.
-int sep_ksplit(const oopao_pwfs_plan* p, int bc, int cap, bool use_set = true) {
+int sep_ksplit(const oopao_pwfs_plan* p, int bc, int cap, bool use_set = true, bool ad = false) {
   if (use_set && p->ksplit > 0 && p->ksplit <= cap) return p->ksplit;
-  const int blocks = p->n / p->sep->l_cols, resident = std::max(1, p->sep_cols_ctas);
+  const SepPasses* s = ad ? p->sep_ad : p->sep;
+  const int blocks = p->n / s->l_cols, resident = std::max(1, ad ? p->sep_ad_ctas : p->sep_cols_ctas);
   int best = 1;
   double best_t = 1e300;
   for (int d = 1; d <= p->k && d <= cap; d++) {
@@ -1654,7 +1667,7 @@ namespace {
 // does not fit.
 int jvp_sep(const oopao_pwfs_plan* p, const float* opd0, int opd0_batch, const float* dopd, double phase_scale,
             int batch, float* dframe, char* base, size_t usable, cudaStream_t st) {
-  const SepPasses* s = p->sep;
+  const SepPasses* s = p->sep_ad;
   const int n = p->n, res = p->res, k = p->k, cam = p->cam, ng = p->ngroups;
   float2* g = (float2*)base;  // [k][n][n] operating-point fields
   float2* w0 = g + (size_t)k * n * n;
@@ -1666,16 +1679,16 @@ int jvp_sep(const oopao_pwfs_plan* p, const float* opd0, int opd0_batch, const f
   bc = (int)std::min<size_t>((size_t)bc, std::max<size_t>(1, p->l2_budget / sep_chunk_bytes(p, 1, 1, true)));
   // slot counts from the model: a count set for measure calls (autotuner) was
   // timed on another batch and another kernel form
-  int ks = sep_ksplit(p, bc, kMaxSlotsBinned, false);
+  int ks = sep_ksplit(p, bc, kMaxSlotsBinned, false, true);
   while (bc > 1 && sep_chunk_bytes(p, bc, ks, true) > avail) {
     bc = (bc + 1) / 2;
-    ks = sep_ksplit(p, bc, kMaxSlotsBinned, false);
+    ks = sep_ksplit(p, bc, kMaxSlotsBinned, false, true);
   }
   if (sep_chunk_bytes(p, bc, ks, true) > avail) return OOPAO_ERR_WORKSPACE;
   float2* y = (float2*)chunk;
   float2* fld = y + (size_t)bc * ng * res * n;
   float* part = (float*)(fld + (size_t)bc * res * res);
-  const int ks0 = sep_ksplit(p, 1, kMaxSlotsBinned, false);
+  const int ks0 = sep_ksplit(p, 1, kMaxSlotsBinned, false, true);
   int launches = 0;
   for (int b0 = 0; b0 < batch; b0 += bc) {
     const int nb = std::min(bc, batch - b0);
@@ -1715,7 +1728,7 @@ extern "C" int oopao_pwfs_jvp(const oopao_pwfs_plan* p, const float* opd0, int o
   uintptr_t base = ((uintptr_t)ws + 255) & ~(uintptr_t)255;
   OOPAO_CHECK_ARG(ws_bytes > base - (uintptr_t)ws, "workspace too small");
   const size_t usable = ws_bytes - (base - (uintptr_t)ws);
-  if (sep_applies(p, false, false)) {
+  if (sep_applies(p, false, false) && p->sep_ad->l_cols % p->bin == 0) {
     const int r = jvp_sep(p, opd0, opd0_batch, dopd, phase_scale, batch, dframe, (char*)base, usable, st);
     if (r != OOPAO_ERR_WORKSPACE) return r;  // else the three-pass tangent below
   }
@@ -1791,11 +1804,11 @@ namespace {
 // not fit.
 int vjp_sep(const oopao_pwfs_plan* p, const float* opd, const float* fbar, double phase_scale, int batch,
             float* opd_bar, char* base, size_t usable, cudaStream_t st) {
-  const SepPasses* s = p->sep;
+  const SepPasses* s = p->sep_ad;
   const int n = p->n, res = p->res, k = p->k, cam = p->cam, ng = p->ngroups;
   const int rblocks = ceil_div(res, s->l_rows);
   auto row_slots = [&](int bc) {
-    const int want = ceil_div(8 * std::max(1, p->sep_cols_ctas), rblocks * bc);
+    const int want = ceil_div(8 * std::max(1, p->sep_ad_ctas), rblocks * bc);
     int best = 1;
     for (int d = 1; d <= k && d <= kMaxSlotsBinned; d++) {
       if (k % d) continue;
@@ -1822,7 +1835,7 @@ int vjp_sep(const oopao_pwfs_plan* p, const float* opd, const float* fbar, doubl
   int launches = 0;
   for (int b0 = 0; b0 < batch; b0 += bc) {
     const int nb = std::min(bc, batch - b0);
-    const int ksc = sep_ksplit(p, nb, kMaxSlotsBinned, false);
+    const int ksc = sep_ksplit(p, nb, kMaxSlotsBinned, false, true);
     pwfs_field<<<dim3(ceil_div(res * res, 256), nb), 256, 0, st>>>(opd + (size_t)b0 * res * res, (float)phase_scale,
                                                                    p->d_amp, fld, res * res);
     SepRowsArgs ra{p->d_tw, fld, p->d_growfac, p->d_mrow, y, res, ng, p->off};

@@ -306,10 +306,12 @@ class DeformableMirror:
         return out
 
     # Batches above this go to the BF16 tensor-core GEMM even when the IFs
-    # factorise (GB300, 40x40: separable 21 us against 46 us at 16 columns,
-    # 74 us against 49 us at 64; the FP32 dense path is slower than the
-    # separable one at every batch).
-    SEPARABLE_MAX_BATCH_VS_TC = 32
+    # factorise.  Measured on GB300 the separable projection (fused kernel up
+    # to 15 columns, then the tiled FP32 GEMM of the second contraction) is
+    # faster at every batch: 80x80 at 300 columns 0.60 ms against 1.30 ms,
+    # 40x40 0.097 against 0.128 ms; autotune.tune_dm measures the cut-over
+    # per mirror.
+    SEPARABLE_MAX_BATCH_VS_TC = 1 << 30
 
     def projection_path(self, B=1):
         """Path of a projection of B coefficient vectors: 'separable', 'bf16'

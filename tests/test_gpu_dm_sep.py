@@ -33,9 +33,11 @@ def _rel(a, b):
 def test_separable_projection(kw, batch):
     tel, dm = _dm(**kw)
     assert dm.projection_path() == 'separable'
-    # large batches of a BF16-IF mirror go to the tensor-core GEMM
+    # factorising IFs take the separable projection at every batch (the
+    # tiled FP32 GEMM beats the BF16 tensor-core one); a BF16-IF mirror keeps
+    # the tensor-core path for batches above its cut-over
     path = dm.projection_path(batch)
-    assert path == ('bf16' if kw.get('if_dtype') == 'bf16' and batch > dm.SEPARABLE_MAX_BATCH_VS_TC else 'separable')
+    assert path == ('bf16' if kw.get('if_dtype') == 'bf16' and batch > dm.separable_max_batch else 'separable')
     tol = 2e-3 if path == 'bf16' else 1e-6
     rng = np.random.default_rng(batch)
     coefs = rng.standard_normal((dm.nValidAct, batch)) * 1e-7
@@ -79,8 +81,8 @@ def test_misregistered_projection_path(mr, path):
     assert _rel(out, ref) < 1e-6
 
 
-@pytest.mark.parametrize('nx, ny, batch', [(12, 9, 2), (150, 60, 2), (300, 70, 3)],
-                         ids=['one_launch', 'one_launch_96k', 'two_launches'])
+@pytest.mark.parametrize('nx, ny, batch', [(12, 9, 2), (150, 60, 2), (300, 70, 3), (150, 60, 40), (12, 9, 17)],
+                         ids=['one_launch', 'one_launch_96k', 'two_launches', 'tiled_96k', 'tiled'])
 def test_separable_cabi(nx, ny, batch):
     """oopao_dm_opd_sep_f32 on synthetic factors: a grid whose coefficient map
     fits in shared memory (one launch) and one that does not (two), with
