@@ -79,25 +79,34 @@ def test_tc_projection_with_base(modes):
 
 
 def test_bf16_dm_signal_within_tolerance():
+    """The BF16 tensor-core IF path against the reference's own Pyramid
+    (golden c1: a DM shape's signal and push-pull IM columns of three modes,
+    made by the unmodified reference in float64): the BF16 IF bound, 2e-3
+    relative L2."""
     import contextlib
     import io
     import oopao_gb300 as og
+    from tests import goldens as G
+    d = G.load('c1')
     with contextlib.redirect_stdout(io.StringIO()):
         tel = og.Telescope(resolution=120, diameter=8.0, samplingTime=1e-3)
         ngs = og.Source(optBand='V0', magnitude=8)
         ngs * tel
-        dm32 = og.DeformableMirror(tel, nSubap=20)
-        dm16 = og.DeformableMirror(tel, nSubap=20, if_dtype='bf16')
-        wfs = og.Pyramid(nSubap=20, telescope=tel, modulation=3, lightRatio=0.5, nTheta_user_defined=48)
-    c = np.random.default_rng(2).standard_normal(dm32.nValidAct) * 50e-9
-    dm32.coefs = c
-    ngs ** tel * dm32 * wfs
-    s32 = wfs.signal.copy()
-    dm16.coefs = c
+        dm16 = og.DeformableMirror(tel, nSubap=20, mechCoupling=0.35, if_dtype='bf16')
+        wfs = og.Pyramid(nSubap=20, telescope=tel, modulation=3, lightRatio=0.5, nTheta_user_defined=48,
+                         max_batch=64)
+    # the factorising IFs would take the exact separable projection: force the
+    # tensor-core GEMM over the BF16 IF matrix (the GEMV at one column)
+    dm16.separable_projection = False
+    assert dm16.projection_path(1) == 'bf16' and dm16.projection_path(64) == 'bf16'
+    dm16.coefs = d['dm_coefs']
     ngs ** tel * dm16 * wfs
     assert dm16.tensor_core_status() == 0
-    assert O.rel_l2(wfs.signal, s32) < 2e-3
-    m2c = np.eye(dm32.nValidAct)[:, :40]
-    D32 = og.InteractionMatrix(ngs, tel, dm32, wfs, m2c, 1e-8, single_pass=False, invert=False).D
-    D16 = og.InteractionMatrix(ngs, tel, dm16, wfs, m2c, 1e-8, single_pass=False, invert=False).D
-    assert O.rel_l2(D16, D32) < 2e-3
+    assert O.rel_l2(wfs.signal, d['dm_signal']) < 2e-3
+    # the golden IM has three modes: batches of up to 4 columns take the
+    # BF16 GEMV; a fixed 64-column tile forces the tcgen05 GEMM as well
+    for rule in ([], [(1 << 30, 64)]):
+        dm16.tc_tile_rule = rule
+        D16 = og.InteractionMatrix(ngs, tel, dm16, wfs, d['im_m2c'], 1e-8, single_pass=False, invert=False).D
+        assert dm16.tensor_core_status() == 0
+        assert O.rel_l2(D16, d['im_pp_D']) < 2e-3, rule
