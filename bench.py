@@ -1036,7 +1036,9 @@ def run_ours(args):
         dist.init_process_group('nccl')
     from oopao_gb300 import _native as N
     from oopao_gb300.calibration import InteractionMatrix, _signals_batched
-    tel, ngs, dm, wfs = build_system(local)
+    # every mode of one sign in one launch sequence (measured: 68.5k frames/s
+    # against 66.6k in chunks of 100)
+    tel, ngs, dm, wfs = build_system(local, max_batch=NMODES)
     m2c = reference_kl_c1(NMODES)
     dev = wfs._dev
     m2c_dev = torch.as_tensor(m2c.astype(np.float32), device=dev)
