@@ -91,18 +91,25 @@ def test_separable_factors_rebuild_the_modes(kw):
     """The drop-in DM's separable factors (gx, gy, cell map) reproduce its
     dense float64 Gaussian IFs, and a rotated or anamorphic grid is refused
     (host only)."""
-    import types
     from oopao_gb300.deformable_mirror import DeformableMirror as DM
     from oopao_gb300.mis_registration import MisRegistration
     res, ns = 48, 8
     mr = MisRegistration(dict(dict.fromkeys(O.MISREG_FIELDS, 0.0), **kw.get('mr', {})))
-    fake = types.SimpleNamespace(resolution=res, nActAlongDiameter=ns, mechCoupling=0.35, misReg=mr,
-                                 sign=kw.get('sign', 1), flip_lr=kw.get('flip_lr', False),
-                                 flip_=kw.get('flip_', False), floating_precision=64)
+    def host_dm(**attrs):
+        # the DM's host methods on an instance built without a GPU
+        d = object.__new__(DM)
+        d._modes = None
+        d._modes_t_dev = None
+        for k, v in attrs.items():
+            setattr(d, k, v)
+        return d
+
+    attrs = dict(resolution=res, nActAlongDiameter=ns, mechCoupling=0.35, misReg=mr, sign=kw.get('sign', 1),
+                 flip_lr=kw.get('flip_lr', False), flip_=kw.get('flip_', False), floating_precision=64)
     u0x, u0y, _ = O.dm_actuator_pixels(res, 8.0, ns, 0.0, mr.__dict__)
+    fake = host_dm(**attrs)
     fake.modes = DM._gaussian_modes(fake, u0x, u0y)
-    fake32 = types.SimpleNamespace(**vars(fake))
-    fake32.floating_precision = 32
+    fake32 = host_dm(**dict(attrs, floating_precision=32))
     fake32.modes = DM._gaussian_modes(fake32, u0x, u0y)
     assert fake32.modes.dtype == np.float32 and DM._separable_factors(fake32, u0x, u0y) is not None
     gx, gy, cells = DM._separable_factors(fake, u0x, u0y)
