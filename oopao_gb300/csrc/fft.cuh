@@ -76,6 +76,21 @@ struct Dft<2, INV> {
   }
 };
 
+// Radix 3 with the outputs as FMAs on the half-sum: 12 instructions against
+// 14 for the generic odd form (whose sine term is a separate product).
+template <bool INV>
+struct Dft<3, INV> {
+  static __device__ __forceinline__ void run(float2* v) {
+    const float s = INV ? -rad_sin(3, 1) : rad_sin(3, 1);
+    const float2 a = cadd(v[1], v[2]), b = csub(v[1], v[2]);
+    const float2 x0 = v[0];
+    const float2 h = make_float2(fmaf(rad_cos(3, 1), a.x, x0.x), fmaf(rad_cos(3, 1), a.y, x0.y));
+    v[0] = cadd(x0, a);
+    v[1] = make_float2(fmaf(s, b.y, h.x), fmaf(-s, b.x, h.y));
+    v[2] = make_float2(fmaf(-s, b.y, h.x), fmaf(s, b.x, h.y));
+  }
+};
+
 template <bool INV>
 struct Dft<4, INV> {
   static __device__ __forceinline__ void run(float2* v) {

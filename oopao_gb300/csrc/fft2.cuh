@@ -78,6 +78,12 @@ __device__ __forceinline__ void dft_composite(float2* v) {
       const int t = (b * k1) % R;
       if (t == 0) {
         y[k1 * B + b] = u[k1];
+      } else if (4 * t == R) {  // W_R^{R/4}: -i forward, +i inverse
+        y[k1 * B + b] = mul_mi<INV>(u[k1]);
+      } else if (2 * t == R) {
+        y[k1 * B + b] = make_float2(-u[k1].x, -u[k1].y);
+      } else if (4 * t == 3 * R) {
+        y[k1 * B + b] = mul_mi<!INV>(u[k1]);
       } else {
         const float c = rad_cos(R, t), s = INV ? rad_sin(R, t) : -rad_sin(R, t);
         y[k1 * B + b] = cmul(u[k1], make_float2(c, s));
