@@ -112,6 +112,105 @@ __device__ __forceinline__ void dft(float2* v) {
   }
 }
 
+// ---- transforms of lines whose inputs are zero past the first NZ ----
+// Split R = A*B used on the input side (u[a] = v[a*B + b]): B large, so that
+// most of the A-point sub-transforms see at most one non-zero input.
+template <int R>
+struct PruneSplit { static constexpr int A = 0, B = 0; };
+template <> struct PruneSplit<8> { static constexpr int A = 2, B = 4; };
+template <> struct PruneSplit<12> { static constexpr int A = 3, B = 4; };
+template <> struct PruneSplit<16> { static constexpr int A = 2, B = 8; };
+template <> struct PruneSplit<24> { static constexpr int A = 3, B = 8; };
+template <> struct PruneSplit<48> { static constexpr int A = 4, B = 12; };
+
+// A-point DFT of u whose entries past the first NZ are zero (not read).
+template <int A, int NZ, bool INV>
+__device__ __forceinline__ void dft_lead(float2* u) {
+  if constexpr (NZ >= A) {
+    dft<A, INV>(u);
+  } else if constexpr (NZ == 1) {
+#pragma unroll
+    for (int k = 1; k < A; k++) u[k] = u[0];
+  } else {
+    float2 y[A];
+#pragma unroll
+    for (int k = 0; k < A; k++) {
+      float2 acc = u[0];
+#pragma unroll
+      for (int a = 1; a < NZ; a++) {
+        const int t = (a * k) % A;
+        if (t == 0) {
+          acc = cadd(acc, u[a]);
+        } else {
+          const float c = rad_cos(A, t), sn = INV ? rad_sin(A, t) : -rad_sin(A, t);
+          acc.x = fmaf(u[a].x, c, fmaf(-u[a].y, sn, acc.x));
+          acc.y = fmaf(u[a].x, sn, fmaf(u[a].y, c, acc.y));
+        }
+      }
+      y[k] = acc;
+    }
+#pragma unroll
+    for (int k = 0; k < A; k++) u[k] = y[k];
+  }
+}
+
+template <int R, int NZ, bool INV, int b>
+__device__ __forceinline__ void prune_front_stage(const float2* v, float2* y) {
+  constexpr int A = PruneSplit<R>::A, B = PruneSplit<R>::B;
+  if constexpr (b < B) {
+    constexpr int nz = NZ > b ? (NZ - b + B - 1) / B : 0;  // inputs a*B + b < NZ
+    if constexpr (nz == 0) {
+#pragma unroll
+      for (int k1 = 0; k1 < A; k1++) y[k1 * B + b] = make_float2(0.f, 0.f);
+    } else {
+      float2 u[A];
+#pragma unroll
+      for (int a = 0; a < nz; a++) u[a] = v[a * B + b];
+      dft_lead<A, nz, INV>(u);
+#pragma unroll
+      for (int k1 = 0; k1 < A; k1++) {
+        const int t = (b * k1) % R;
+        if (t == 0) {
+          y[k1 * B + b] = u[k1];
+        } else if (4 * t == R) {
+          y[k1 * B + b] = mul_mi<INV>(u[k1]);
+        } else if (2 * t == R) {
+          y[k1 * B + b] = make_float2(-u[k1].x, -u[k1].y);
+        } else if (4 * t == 3 * R) {
+          y[k1 * B + b] = mul_mi<!INV>(u[k1]);
+        } else {
+          const float c = rad_cos(R, t), sn = INV ? rad_sin(R, t) : -rad_sin(R, t);
+          y[k1 * B + b] = cmul(u[k1], make_float2(c, sn));
+        }
+      }
+    }
+    prune_front_stage<R, NZ, INV, b + 1>(v, y);
+  }
+}
+
+// R-point DFT of v whose entries v[m], m >= NZ, are zero (only the first NZ
+// are read).  Same result as dft<R> on the zero-padded line.
+template <int R, int NZ, bool INV>
+__device__ __forceinline__ void dft_front(float2* v) {
+  constexpr int A = PruneSplit<R>::A, B = PruneSplit<R>::B;
+  static_assert(NZ >= R || A * B == R, "no pruning split for this radix");
+  if constexpr (NZ >= R) {
+    dft<R, INV>(v);
+  } else {
+    float2 y[R];
+    prune_front_stage<R, NZ, INV, 0>(v, y);
+#pragma unroll
+    for (int k1 = 0; k1 < A; k1++) {
+      float2 w[B];
+#pragma unroll
+      for (int b = 0; b < B; b++) w[b] = y[k1 * B + b];
+      dft<B, INV>(w);
+#pragma unroll
+      for (int k2 = 0; k2 < B; k2++) v[k1 + A * k2] = w[k2];
+    }
+  }
+}
+
 // Exchange-buffer slot of stage-A output index p (radix RA first stage).
 template <int RA>
 __device__ __forceinline__ int xslot(int p) {

@@ -694,16 +694,35 @@ cudaError_t sep_attrs(oopao_pwfs_plan* p) {
   return e;
 }
 
+// A two-pass plan serves pupils of `res` pixels when its column pass fits in
+// shared memory, the 16-byte tile copies see an even pupil, and the pupil
+// lies within the stage-A inputs the plan reads (res <= nz * r2).
+bool sep_fits(const SepPasses* s, int res) {
+  return res % 2 == 0 && s->smem_cols(res) <= kSmemLimit && (res + s->r2 - 1) / s->r2 <= s->nz;
+}
+
 // Two-pass set-up for mask 0 of the plan: factorise it, upload the factors
 // and prepare the kernels.  A mask that does not factorise (or an n without
 // a two-pass plan) leaves mask_sep false.
 cudaError_t sep_setup(oopao_pwfs_plan* p, const float* mask_host) {
   p->mask_sep = false;
   // 16-byte tile copies need an even pupil; the column pass must fit in shared memory
-  if (!p->sep || p->res % 2 || p->sep->smem_cols(p->res) > kSmemLimit)
-    return cudaSuccess;
+  if (!p->sep || !sep_fits(p->sep, p->res)) return cudaSuccess;
   std::vector<float2> mrow, mcol;
   if (!factor_mask(reinterpret_cast<const float2*>(mask_host), p->n, &mrow, &mcol)) return cudaSuccess;
+  // The passes place the pupil at rows and columns [0, res) of the grid
+  // instead of [off, off+res): F(x) = exp(-2 pi i u off/N) F(x shifted by
+  // off), so the shift folds into each factor as that linear phase and the
+  // outputs are unchanged.  The forward transforms then see their non-zero
+  // inputs at the start of each line.
+  for (int u = 0; u < p->n; u++) {
+    const long long m = ((long long)u * p->off) % p->n;
+    const double a = -2.0 * M_PI * (double)m / p->n, cr = cos(a), ci = sin(a);
+    for (std::vector<float2>* f : {&mrow, &mcol}) {
+      const double fr = (*f)[u].x, fi = (*f)[u].y;
+      (*f)[u] = make_float2((float)(fr * cr - fi * ci), (float)(fr * ci + fi * cr));
+    }
+  }
   cudaError_t e = cudaSuccess;
   if (!p->d_mrow) e = cudaMalloc((void**)&p->d_mrow, sizeof(float2) * p->n);
   if (e == cudaSuccess && !p->d_mcol) e = cudaMalloc((void**)&p->d_mcol, sizeof(float2) * p->n);
@@ -1131,12 +1150,12 @@ int measure_sep(const oopao_pwfs_plan* p, const float* opd, double phase_scale, 
     pwfs_field<<<dim3(ceil_div(res * res, 256), nb), 256, 0, st>>>(opd + (size_t)b0 * res * res, (float)phase_scale,
                                                                    p->d_amp, field, res * res);
     mark(0);
-    SepRowsArgs ra{p->d_tw, field, p->d_growfac, p->d_mrow, y, res, ng, p->off};
+    SepRowsArgs ra{p->d_tw, field, p->d_growfac, p->d_mrow, y, res, ng, 0 /* support at row/column 0 */};
     mark(0);
     s->rows<<<dim3(ceil_div(res, s->l_rows), ng, nb), s->t * s->l_rows, s->smem_rows, st>>>(ra);
     mark(0);
     SepColsArgs ca{p->d_tw, p->d_mcol, y, p->d_group, p->d_colfac, weights_of(p), nullptr, nullptr,
-                   fused ? nullptr : part, fused ? part : nullptr, res, p->off, ng, k / ks, ks, p->bin, cam};
+                   fused ? nullptr : part, fused ? part : nullptr, res, 0 /* support at row/column 0 */, ng, k / ks, ks, p->bin, cam};
     mark(1);
     s->cols[kSepIntensity]<<<dim3(n / s->l_cols, ks, nb), s->t * s->l_cols, s->smem_cols(res), st>>>(ca);
     mark(1);
@@ -1695,19 +1714,19 @@ int jvp_sep(const oopao_pwfs_plan* p, const float* opd0, int opd0_batch, const f
     const float* o0 = opd0 + (opd0_batch == 1 ? 0 : (size_t)b0 * res * res);
     if (b0 == 0 || opd0_batch != 1) {
       pwfs_field<<<dim3(ceil_div(res * res, 256), 1), 256, 0, st>>>(o0, (float)phase_scale, p->d_amp, w0, res * res);
-      SepRowsArgs ra{p->d_tw, w0, p->d_growfac, p->d_mrow, y, res, ng, p->off};
+      SepRowsArgs ra{p->d_tw, w0, p->d_growfac, p->d_mrow, y, res, ng, 0 /* support at row/column 0 */};
       s->rows<<<dim3(ceil_div(res, s->l_rows), ng, 1), s->t * s->l_rows, s->smem_rows, st>>>(ra);
       SepColsArgs ca{p->d_tw, p->d_mcol, y, p->d_group, p->d_colfac, nullptr, nullptr, g, nullptr, nullptr,
-                     res, p->off, ng, k / ks0, ks0, p->bin, cam};
+                     res, 0 /* support at row/column 0 */, ng, k / ks0, ks0, p->bin, cam};
       s->cols[kSepStore]<<<dim3(n / s->l_cols, ks0, 1), s->t * s->l_cols, s->smem_cols(res), st>>>(ca);
       launches += 3;
     }
     pwfs_field_tangent<<<dim3(ceil_div(res * res, 256), nb), 256, 0, st>>>(
         o0, dopd + (size_t)b0 * res * res, (float)phase_scale, p->d_amp, fld, res * res, 0);
-    SepRowsArgs ra{p->d_tw, fld, p->d_growfac, p->d_mrow, y, res, ng, p->off};
+    SepRowsArgs ra{p->d_tw, fld, p->d_growfac, p->d_mrow, y, res, ng, 0 /* support at row/column 0 */};
     s->rows<<<dim3(ceil_div(res, s->l_rows), ng, nb), s->t * s->l_rows, s->smem_rows, st>>>(ra);
     SepColsArgs ca{p->d_tw, p->d_mcol, y, p->d_group, p->d_colfac, weights_of(p), g, nullptr, nullptr, part,
-                   res, p->off, ng, k / ks, ks, p->bin, cam};
+                   res, 0 /* support at row/column 0 */, ng, k / ks, ks, p->bin, cam};
     s->cols[kSepTangent]<<<dim3(n / s->l_cols, ks, nb), s->t * s->l_cols, s->smem_cols(res), st>>>(ca);
     pwfs_reduce_binned<<<dim3(ceil_div(cam * cam, 256), nb), 256, 0, st>>>(part, dframe + (size_t)b0 * cam * cam,
                                                                            cam * cam, ks);
@@ -1838,10 +1857,10 @@ int vjp_sep(const oopao_pwfs_plan* p, const float* opd, const float* fbar, doubl
     const int ksc = sep_ksplit(p, nb, kMaxSlotsBinned, false, true);
     pwfs_field<<<dim3(ceil_div(res * res, 256), nb), 256, 0, st>>>(opd + (size_t)b0 * res * res, (float)phase_scale,
                                                                    p->d_amp, fld, res * res);
-    SepRowsArgs ra{p->d_tw, fld, p->d_growfac, p->d_mrow, y, res, ng, p->off};
+    SepRowsArgs ra{p->d_tw, fld, p->d_growfac, p->d_mrow, y, res, ng, 0 /* support at row/column 0 */};
     s->rows<<<dim3(rblocks, ng, nb), s->t * s->l_rows, s->smem_rows, st>>>(ra);
     SepAdjArgs ca{p->d_tw, p->d_mcol, p->d_mrow, y, p->d_group, p->d_colfac, p->d_growfac, weights_of(p),
-                  fbar + (size_t)b0 * cam * cam, fld, v, part, res, p->off, ng, k / ksc, ksc, p->bin, cam};
+                  fbar + (size_t)b0 * cam * cam, fld, v, part, res, 0 /* support at row/column 0 */, ng, k / ksc, ksc, p->bin, cam};
     s->cols_adj<<<dim3(n / s->l_cols, ksc, nb), s->t * s->l_cols, s->smem_cols(res), st>>>(ca);
     SepAdjArgs rb = ca;
     rb.slot_pts = k / ksr;
@@ -1985,7 +2004,7 @@ extern "C" int oopao_pwfs_set_separable(oopao_pwfs_plan* p, int enable) {
   if (p->sep != c + (enable - 1)) {
     const SepPasses* prev = p->sep;
     p->sep = c + (enable - 1);
-    if (p->res % 2 || p->sep->smem_cols(p->res) > kSmemLimit) {
+    if (!sep_fits(p->sep, p->res)) {
       p->sep = prev;
       oopao_set_last_error("that two-pass plan does not fit this pupil", __FILE__, __LINE__);
       return OOPAO_ERR_UNSUPPORTED;

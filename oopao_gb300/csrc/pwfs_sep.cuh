@@ -38,7 +38,9 @@
 // SHARE: x2 is x1 (one exchange buffer, one more barrier; needs one stage-B
 // butterfly per thread).  before_last() runs just before the barrier that
 // ends the forward half.
-template <int N, int R1, int R2, int T, int RP1, int RP2, bool SHARE, class Load, class Filt, class Store,
+// NZ: the line's inputs j + m*R2 are zero for m >= NZ (the pupil sits at
+// the start of the line), so stage A reads and transforms only the first NZ.
+template <int N, int R1, int R2, int T, int RP1, int RP2, bool SHARE, int NZ, class Load, class Filt, class Store,
           class AfterA, class BeforeLast>
 __device__ __forceinline__ void sep_chain_x(int t, float2* x1, float2* x2, const float2* tw, const float2* twi,
                                             Load load, Filt filt, Store store, AfterA after_a,
@@ -52,9 +54,15 @@ __device__ __forceinline__ void sep_chain_x(int t, float2* x1, float2* x2, const
     const int j = t + p * T;
     if (j < R2) {
       float2 v[R1];
+      if constexpr (NZ < R1) {
 #pragma unroll
-      for (int m = 0; m < R1; m++) v[m] = load(p, m, j);
-      dft<R1, false>(v);
+        for (int m = 0; m < NZ; m++) v[m] = load(p, m, j);
+        dft_front<R1, NZ, false>(v);
+      } else {
+#pragma unroll
+        for (int m = 0; m < R1; m++) v[m] = load(p, m, j);
+        dft<R1, false>(v);
+      }
 #pragma unroll
       for (int q = 0; q < R1; q++) x1[j * RP1 + q] = v[q];
     }
@@ -105,8 +113,8 @@ __device__ __forceinline__ void sep_chain_x(int t, float2* x1, float2* x2, const
 template <int N, int R1, int R2, int T, int RP1, int RP2, class Load, class Filt, class Store, class AfterA>
 __device__ __forceinline__ void sep_chain(int t, float2* x1, float2* x2, const float2* tw, const float2* twi,
                                           Load load, Filt filt, Store store, AfterA after_a) {
-  sep_chain_x<N, R1, R2, T, RP1, RP2, (R1 + T - 1) / T == 1>(t, x1, x2, tw, twi, load, filt, store, after_a,
-                                                               [] {});
+  sep_chain_x<N, R1, R2, T, RP1, RP2, (R1 + T - 1) / T == 1, R1>(t, x1, x2, tw, twi, load, filt, store, after_a,
+                                                                   [] {});
 }
 
 struct SepRowsArgs {
@@ -119,7 +127,7 @@ struct SepRowsArgs {
 };
 
 // Pass 1: filtered rows (j-fastest thread mapping: line = tid / T).
-template <int N, int R1, int R2, int T, int L>
+template <int N, int R1, int R2, int T, int L, int NZ>
 __global__ void __launch_bounds__(T* L) pwfs_srows(SepRowsArgs a) {
   constexpr int R1P = pad_odd(R1), R2P = pad_odd(R2);
   constexpr int LS1 = xchg_stride(R2 * R1P, T, L, R1P, R2, R1);
@@ -146,7 +154,7 @@ __global__ void __launch_bounds__(T* L) pwfs_srows(SepRowsArgs a) {
   const float2* fld = a.field + ((size_t)b * res + (active ? row : 0)) * res;
   const float2* rf = a.rowfac + (size_t)g * res;
   float2* y = a.y + (((size_t)b * a.ng + g) * res + row) * N;
-  sep_chain<N, R1, R2, T, R1P, R2P>(
+  sep_chain_x<N, R1, R2, T, R1P, R2P, ALIAS, NZ>(
       t, b1 + l * LS1, b2 + l * LS2, tw, twi,
       [&](int, int m, int j) {
         const int jc = j + m * R2 - off;
@@ -159,7 +167,7 @@ __global__ void __launch_bounds__(T* L) pwfs_srows(SepRowsArgs a) {
           for (int q = 0; q < R1; q++) y[j + q * R2] = v[q];
         }
       },
-      [] {});
+      [] {}, [] {});
 }
 
 struct SepColsArgs {
@@ -209,7 +217,7 @@ struct SepColsSmem {
   static size_t bytes(int res) { return sizeof(float2) * (kTiles + tile(res)); }
 };
 
-template <int N, int R1, int R2, int T, int L, int MODE, int MAXREG, bool SHARE>
+template <int N, int R1, int R2, int T, int L, int MODE, int MAXREG, bool SHARE, int NZ>
 __global__ void __launch_bounds__(T* L) __maxnreg__(MAXREG) pwfs_scols(SepColsArgs a) {
   using S = SepColsSmem<N, R1, R2, T, L, SHARE>;
   constexpr int R1P = S::LAY1 >> 16, LS1 = S::LS1;
@@ -269,7 +277,7 @@ __global__ void __launch_bounds__(T* L) __maxnreg__(MAXREG) pwfs_scols(SepColsAr
     const float w = a.weights ? a.weights[kk] : 1.f;
     const float2* gi = (MODE == kSepTangent) ? a.g0 + (size_t)kk * N * N + c : nullptr;
     float2* go = (MODE == kSepStore) ? a.gout + (size_t)kk * N * N + c : nullptr;
-    sep_chain_x<N, R1, R2, T, R1P, R2P, SHARE>(
+    sep_chain_x<N, R1, R2, T, R1P, R2P, SHARE, NZ>(
         t, b1 + l * LS1, b2 + l * LS2, tw, twi,
         [&](int, int m, int j) {
           const int i = j + m * R2 - off;
@@ -370,7 +378,7 @@ struct SepAdjArgs {
 
 // Two chains per point with Gbar held between them: 128 registers keep it
 // (with 96 it spilled ~300 bytes per thread).
-template <int N, int R1, int R2, int T, int L>
+template <int N, int R1, int R2, int T, int L, int NZ>
 __global__ void __maxnreg__(128) pwfs_scols_adj(SepAdjArgs a) {
   using S = SepColsSmem<N, R1, R2, T, L>;
   constexpr int R1P = S::LAY1 >> 16, LS1 = S::LS1;
@@ -414,7 +422,7 @@ __global__ void __maxnreg__(128) pwfs_scols_adj(SepAdjArgs a) {
     const float2* cf = tile + res * L;
     const float w2 = 2.f * (a.weights ? a.weights[kk] : 1.f);
     float2 gb[PBA][R1];  // Gbar of this column, rows j + q*R2
-    sep_chain<N, R1, R2, T, R1P, R2P>(
+    sep_chain_x<N, R1, R2, T, R1P, R2P, ALIAS, NZ>(
         t, b1 + l * LS1, b2 + l * LS2, tw, twi,
         [&](int, int m, int j) {
           const int i = j + m * R2 - off;
@@ -430,7 +438,8 @@ __global__ void __maxnreg__(128) pwfs_scols_adj(SepAdjArgs a) {
         },
         [&] {
           if (kk + 1 < kend) issue(kk + 1);
-        });
+        },
+        [] {});
     if (ALIAS) __syncthreads();  // the first chain's last exchange reads are done
     float2* vo = a.v + ((size_t)b * gridDim.y * a.slot_pts + kk) * res * N + c;
     const float2* cfg = a.colfac + (size_t)kk * res;
@@ -526,6 +535,7 @@ __global__ void __maxnreg__(128) pwfs_srows_adj(SepAdjArgs a) {
 
 struct SepPasses {
   int n, r1, r2, t, l_rows, l_cols;
+  int nz;  // stage-A inputs read per butterfly: the pupil must satisfy res <= nz * r2
   void (*rows)(SepRowsArgs);
   void (*cols[3])(SepColsArgs);  // indexed by kSepIntensity / kSepTangent / kSepStore
   void (*cols_adj)(SepAdjArgs);
@@ -535,7 +545,11 @@ struct SepPasses {
 };
 
 // MAXREG caps the column pass's registers per thread (its occupancy).
-template <int N, int R1, int R2, int T, int LR, int LC, int MAXREG, bool SHARE = (R1 + T - 1) / T == 1>
+// NZ: non-zero inputs per stage-A butterfly (the pupil occupies at most half
+// of a line, res <= N/2, so at most ceil(R1/2) of the R1 inputs j + m*R2
+// fall inside it).
+template <int N, int R1, int R2, int T, int LR, int LC, int MAXREG, bool SHARE = (R1 + T - 1) / T == 1,
+          int NZ = (R1 + 1) / 2>
 SepPasses make_sep() {
   static_assert(N % LC == 0, "column blocks must tile N");
   constexpr int R1P = pad_odd(R1), R2P = pad_odd(R2);
@@ -549,11 +563,12 @@ SepPasses make_sep() {
   static_assert((size_t)LC * LSC * 2 >= (size_t)LC * N, "exchange too small for the binning rows");
   SepPasses s;
   s.n = N; s.r1 = R1; s.r2 = R2; s.t = T; s.l_rows = LR; s.l_cols = LC;
-  s.rows = pwfs_srows<N, R1, R2, T, LR>;
-  s.cols[kSepIntensity] = pwfs_scols<N, R1, R2, T, LC, kSepIntensity, MAXREG, SHARE>;
-  s.cols[kSepTangent] = pwfs_scols<N, R1, R2, T, LC, kSepTangent, MAXREG, SHARE>;
-  s.cols[kSepStore] = pwfs_scols<N, R1, R2, T, LC, kSepStore, MAXREG, SHARE>;
-  s.cols_adj = pwfs_scols_adj<N, R1, R2, T, LC>;
+  s.nz = NZ;
+  s.rows = pwfs_srows<N, R1, R2, T, LR, NZ>;
+  s.cols[kSepIntensity] = pwfs_scols<N, R1, R2, T, LC, kSepIntensity, MAXREG, SHARE, NZ>;
+  s.cols[kSepTangent] = pwfs_scols<N, R1, R2, T, LC, kSepTangent, MAXREG, SHARE, NZ>;
+  s.cols[kSepStore] = pwfs_scols<N, R1, R2, T, LC, kSepStore, MAXREG, SHARE, NZ>;
+  s.cols_adj = pwfs_scols_adj<N, R1, R2, T, LC, NZ>;
   s.rows_adj = pwfs_srows_adj<N, R1, R2, T, LR>;
   s.smem_rows = sizeof(float2) * (3 * (size_t)N + (size_t)LR * LSR);
   s.smem_cols = &SepColsSmem<N, R1, R2, T, LC, SHARE>::bytes;
