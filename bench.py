@@ -1130,9 +1130,12 @@ def run_ours(args):
     # per-variant capture when the variant's kernel differs (persistent column pass)
     tr = load_traffic('%s@v%d' % (top, variant)) or load_traffic(top)
     traffic = None
-    if tr is not None:
+    if tr is not None and 'dram_bytes_per_unit' in tr:
         # committed ncu capture: DRAM bytes per (item, point) unit, scaled to one launch here
         traffic = float(tr['dram_bytes_per_unit']) * units / max(nl, 1)
+    elif tr is not None and 'dram_bytes_per_group_item' in tr and two_pass:
+        # the row pass: per (item, row-transform group)
+        traffic = float(tr['dram_bytes_per_group_item']) * items * ng / max(nl, 1)
     share = totals[top] / max(sum(totals.values()), 1e-12)
 
     # ---- end to end through the public API (host M2C in, host vault out)
