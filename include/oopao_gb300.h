@@ -399,6 +399,29 @@ int oopao_gsc_optical_gains(const oopao_gsc_plan* plan, const float* frames, int
  * is also the row sum of its basis product). */
 int oopao_gsc_read(const oopao_gsc_plan* plan, int what, void* dst, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Detector readout, the stages without random draws (the noise draws are
+ * made by the caller between the calls).  frames: device float32
+ * [nframes][npix], rewritten in place; one frame per CTA.
+ * ------------------------------------------------------------------------ */
+/* Detector.set_saturation (OOPAO/Detector.py:219-224): max_out device
+ * float32 [nframes] receives each frame's maximum before the clip to
+ * [0, fwc] (the saturation percentage and warning are the caller's). */
+int oopao_det_saturate(float* frames, int nframes, int npix, float fwc, float* max_out, void* stream);
+/* The end of Detector.readout (OOPAO/Detector.py:304-318), in its order:
+ * frame *= gain (pass 1 for an EMCCD, whose gain acts earlier); if bits > 0
+ * the ADC of digitalization (:226-238): fwc <= 0 scales by 2^bits over the
+ * frame maximum, else frame / fwc * (2^bits - 1) clipped to
+ * [clip_zero ? 0 : -inf, 2^bits - 1]; log10 if log_scale; the cast to the
+ * output precision of set_output_precision (:192-213), out_bits 8/16/32/64
+ * for the unsigned types (truncation toward zero, values outside the type
+ * wrap modulo 2^out_bits) or 0 for floating point; minus bg_map (device
+ * float32 [npix] or NULL, remove_bakground :266-271).  max_out (device
+ * float32 [nframes] or NULL) receives each frame's maximum after the gain,
+ * for the ADC saturation warning. */
+int oopao_det_readout_tail(float* frames, int nframes, int npix, float gain, int bits, float fwc, int clip_zero,
+                           int log_scale, int out_bits, const float* bg_map, float* max_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

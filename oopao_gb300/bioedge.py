@@ -386,7 +386,7 @@ class BioEdge:
             else:
                 self.modulation = self.calibModulation
                 f, _ = self._measure_frames(self.src.device_opd(self._dev), 2 * np.pi / self.src.wavelength)
-                f = self.cam._integrate_device(f)
+                f = self.cam._integrate_device(f, dt=self.telescope.samplingTime)
                 frame = f[0].to('cpu', torch.float64).numpy()
                 self.cam._set_device_frame(f)
             self._select_valid(frame)
@@ -428,7 +428,7 @@ class BioEdge:
         single = opd.ndim == 2
         want_raw = self.keep_raw_data and (single or opd.shape[0] == 1)
         frame, raw = self._measure_frames(opd, scale, want_raw=want_raw)
-        frame = self.cam._integrate_device(frame)
+        frame = self.cam._integrate_device(frame, dt=self.telescope.samplingTime)
         self.cam._set_device_frame(frame)
         self._raw_dev = raw
         self._raw_host = None

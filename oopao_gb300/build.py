@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, 'csrc')
 LIBDIR = os.path.join(HERE, '_lib')
 OBJDIR = os.path.join(HERE, '_lib', 'obj')
 LIBNAME = 'liboopao_gb300.so'
-SOURCES = ['capi.cu', 'pwfs.cu', 'pwfs_sep.cu', 'dm.cu', 'dm_sep.cu', 'dm_tc.cu', 'cl.cu', 'atm.cu', 'gsc.cu']
+SOURCES = ['capi.cu', 'pwfs.cu', 'pwfs_sep.cu', 'dm.cu', 'dm_sep.cu', 'dm_tc.cu', 'cl.cu', 'atm.cu', 'gsc.cu', 'det.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
 

@@ -144,7 +144,7 @@ def _signals_batched(ngs, tel, dm, wfs, commands, phase_offset=None):
         if phase_offset is not None:
             opd = opd + torch.as_tensor(np.asarray(phase_offset) / scale, dtype=torch.float32, device=dev)
         frame, _ = wfs._measure_frames(opd, scale)
-        frame = wfs.cam._integrate_device(frame)
+        frame = wfs.cam._integrate_device(frame, dt=wfs.telescope.samplingTime)
         _, sig = wfs._signals(frame)
         out.append(sig)
     return torch.cat(out, dim=0)

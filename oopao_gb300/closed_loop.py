@@ -114,6 +114,10 @@ class ClosedLoop:
                  max_steps=100000, science=False, gsc=None, M2C=None, og_start=0):
         if frame_delay not in (1, 2):
             raise OopaoError('frame_delay must be 1 or 2')
+        if not wfs.cam._is_plain():
+            raise OopaoError('the captured loop reads the noise-free sensor frame: its camera must have the '
+                             'default Detector settings (no noise, integration time, ADC or background; QE 1, '
+                             'gain 1)')
         self.tel, self.ngs, self.dm, self.wfs = tel, ngs, dm, wfs
         self.dev = wfs._dev
         self.gain = float(gain)

@@ -17,6 +17,7 @@ tests never depend on a random-number stream.
 """
 import contextlib
 import io
+import json
 import os
 import sys
 
@@ -604,6 +605,49 @@ def case_gsc(OOPAO, name, res, n_subap, modulation, n_modes, light_ratio=0.5, se
     print(name, 'N', rec['N'], 'modes', n_modes, 'og', rec['og'][:4])
 
 
+DETECTOR_CASES = {
+    # integration over 3 loop steps, saturation, CCD gain, 12-bit ADC (floating-point output)
+    'int3_fwc_adc12': dict(integrationTime=3e-3, FWC=20000, bits=12, gain=2),
+    # 16-bit ADC with a full well: unsigned 16-bit output clipped at 0
+    'adc16_fwc': dict(bits=16, FWC=50000),
+    # 8-bit ADC without full well: scaled by the frame maximum, unsigned 8-bit output
+    'adc8_nofwc': dict(bits=8),
+    # log scale and background-map removal, floating-point output
+    'log_bg': dict(log_scale=True, gain=3),
+    # CMOS with hardware binning (applied twice by the reference) and a gain
+    'cmos_bin2': dict(sensor='CMOS', binning=2, gain=2),
+    # integration over 2 steps, no other effect
+    'int2_plain': dict(integrationTime=2e-3),
+}
+
+
+def case_detector(OOPAO, name='detector_tiny', n=12, steps=7, seed=13):
+    """The reference Detector's integrate/readout on seeded frames, one loop
+    step (1 ms) at a time as the sensor drives it (OOPAO/Pyramid.py:1179-1201),
+    for settings without random draws; the camera frame after every step."""
+    from OOPAO.Detector import Detector
+    rng = np.random.default_rng(seed)
+    frames = rng.exponential(4000.0, (steps, n, n))
+    frames[:, 3, 4] = 30000.0   # a pixel above the full wells once summed
+    bg = rng.uniform(0.0, 50.0, (n, n))
+    rec = dict(frames=frames, bg=bg, dt=1e-3,
+               params=json.dumps(dict(n=n, steps=steps, seed=seed, cases=DETECTOR_CASES)))
+    for tag, kw in DETECTOR_CASES.items():
+        with _quiet():
+            det = Detector(nRes=n, **kw)
+            if tag == 'log_bg':
+                det.backgroundMap = bg
+            out = []
+            for i in range(steps):
+                det._integrated_time += 1e-3
+                det.integrate(frames[i].copy())
+                out.append(np.array(det.frame, dtype=np.float64))
+        rec[tag] = np.array(out)
+        rec[tag + '_dtype'] = str(np.asarray(det.frame).dtype)
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **rec)
+    print(name, {t: (rec[t].shape, rec[t + '_dtype']) for t in DETECTOR_CASES})
+
+
 BIOEDGE_CASES = [
     ('bioedge_tiny', (24, 4, 3, 0.5), {}),
     ('bioedge_grey', (32, 4, 2, 0.3), dict(grey_width=1.0, quadrants_numbering=[2, 3, 0, 1], n_pix_separation=4,
@@ -657,6 +701,8 @@ def main():
         case_misreg(OOPAO)
     if not only or 'im_offset_tiny' in only:
         case_im_offset(OOPAO)
+    if not only or 'detector_tiny' in only:
+        case_detector(OOPAO)
     if not only or any(n in only for n, _ in KL_CASES):
         from refimport import install_kl_shims
         install_kl_shims()
