@@ -9,17 +9,23 @@
 // accumulate into the same FP32 tile, so the coefficients keep ~16
 // significant bits and the only BF16 rounding left is the IF storage.
 //
-// One CTA computes a 128 x BN tile: a TMA producer thread streams 128x64 A
-// and two BNx64 B tiles (128-byte swizzle) through a 4-stage mbarrier ring,
-// one thread issues tcgen05.mma (kind::f16, M=128, N=BN, K=16) into a TMEM
-// accumulator, and the four warps read the accumulator back with
-// tcgen05.ld (32 lanes x 16 columns per load) and store FP32, coalesced
-// along pixels.  Every mbarrier wait is bounded: on time-out the CTA records
-// a code in the error word, stops issuing work and still frees its TMEM.
+// A persistent CTA per SM walks the 128 x BN output tiles.  One thread
+// streams 128x64 A and two BNx64 B tiles (hi, then lo; 128-byte swizzle)
+// through a 4-stage mbarrier ring; one thread issues tcgen05.mma (kind::f16,
+// M=128, K=16) with N = 2*BN, so each instruction multiplies the A tile by the
+// hi and the lo coefficients at once (A is read from shared memory once for
+// both) into a 2*BN-column TMEM accumulator; four epilogue warps read the
+// accumulator back with tcgen05.ld (32 lanes x 16 columns per load), add the
+// hi and lo halves and store FP32, coalesced along pixels.  Two accumulators
+// (4*BN of the 512 TMEM columns) let the epilogue of one tile overlap the
+// MMAs of the next.  Every mbarrier wait is bounded, and every role gives up
+// as soon as another has recorded an error: the CTA then drains its loads in
+// flight, still frees its TMEM and exits.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "common.cuh"
@@ -31,12 +37,15 @@ constexpr int kBM = 128;     // pixels per tile = TMEM lanes
 constexpr int kBK = 64;      // actuators per stage: one 128-byte swizzle row of BF16
 constexpr int kUK = 16;      // K of one tcgen05.mma kind::f16
 constexpr int kStages = 4;
-constexpr int kThreads = 128;
+constexpr int kEpiWarps = 4;                 // one per quarter of the TMEM lanes
+constexpr int kThreads = 64 + 32 * kEpiWarps;  // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 
 struct TcParams {
   int n_pix, batch;
   int nk;         // K tiles
   int batch_pad;  // row offset of the lo coefficients
+  int tiles_n;    // batch tiles per pixel tile
+  int tiles;      // all tiles
   float scale;
   const float* base;
   float* out;
@@ -45,11 +54,31 @@ struct TcParams {
 
 using tma::mbar_expect_tx;
 using tma::mbar_init;
-using tma::mbar_wait;
 using tma::smem_u32;
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
   tma::load_2d(dst, map, bar, x, y);
+}
+
+// Bounded wait for phase `parity` that also gives up once any role of the
+// launch has recorded an error (checked every 1024 polls); false then, and
+// `code` in *err on a time-out of its own.
+__device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, int* err, int code) {
+  const long long t0 = clock64();
+  for (unsigned i = 1;; i++) {
+    if (tma::mbar_try_wait(bar, parity)) return true;
+    if ((i & 1023u) == 0) {
+      if (*(volatile int*)err != 0) return false;
+      if (clock64() - t0 > tma::kWaitCycles) {
+        atomicExch(err, code);
+        return false;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 // Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
@@ -92,8 +121,9 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r) {
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
         "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
+
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 template <int BN>
 constexpr size_t tc_smem_bytes() {
@@ -103,33 +133,37 @@ constexpr size_t tc_smem_bytes() {
 template <int BN>
 __global__ void __launch_bounds__(kThreads, 1)
     dm_tc_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_b, TcParams p) {
+  constexpr int NC = 2 * BN;                     // accumulator columns of a tile: hi products, then lo products
+  constexpr uint32_t kTmemCols = 2 * NC;         // two accumulators (a power of two, <= 512)
   constexpr int A_BYTES = kBM * kBK * 2;
-  constexpr int B_BYTES = 2 * BN * kBK * 2;  // hi tile, then lo tile
+  constexpr int B_BYTES = 2 * BN * kBK * 2;      // hi rows, then lo rows: one 2*BN-row operand
   constexpr int B_HALF = BN * kBK * 2;
+  static_assert(NC <= 256 && kTmemCols <= 512, "tile too wide for one MMA or for TMEM");
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   unsigned char* sa = smem;
   unsigned char* sb = smem + kStages * A_BYTES;
   uint64_t* full = reinterpret_cast<uint64_t*>(sb + kStages * B_BYTES);
   uint64_t* empty = full + kStages;
-  uint64_t* done = empty + kStages;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  uint64_t* tfull = empty + kStages;   // [2] accumulator ready for the epilogue
+  uint64_t* tempty = tfull + 2;        // [2] accumulator read back, free for the next tile
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 2);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // x = batch tile, so the CTAs that share one 128-pixel IF tile run
-  // together and the tile is read from HBM once, then from L2
-  const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * BN;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(done, 1);
+    for (int a = 0; a < 2; a++) {
+      mbar_init(&tfull[a], 1);
+      mbar_init(&tempty[a], kEpiWarps);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"((uint32_t)BN)
+                 "r"(kTmemCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -138,70 +172,104 @@ __global__ void __launch_bounds__(kThreads, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
+  // Tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...; t = pixel tile * tiles_n
+  // + batch tile, so the CTAs that share one 128-pixel IF tile run together
+  // and the tile is read from HBM once, then from L2.
   int issued = 0;  // loads issued by the producer (warp 0, lane 0)
   if (warp == 0 && lane == 0) {
-    // TMA producer
-    for (int kb = 0; kb < p.nk; kb++) {
-      const int s = kb % kStages;
-      if (!mbar_wait(&empty[s], ((kb / kStages) & 1) ^ 1, p.err, 1)) break;
-      issued = kb + 1;
-      mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
-      tma_load_2d(sa + s * A_BYTES, &tma_a, &full[s], kb * kBK, m0);
-      tma_load_2d(sb + s * B_BYTES, &tma_b, &full[s], kb * kBK, n0);
-      tma_load_2d(sb + s * B_BYTES + B_HALF, &tma_b, &full[s], kb * kBK, p.batch_pad + n0);
+    // TMA producer, one ring over all tiles of the CTA
+    int it = 0;
+    for (int t = blockIdx.x; t < p.tiles; t += gridDim.x) {
+      const int m0 = (t / p.tiles_n) * kBM, n0 = (t % p.tiles_n) * BN;
+      bool ok = true;
+      for (int kb = 0; kb < p.nk; kb++, it++) {
+        const int s = it % kStages;
+        if (!wait_or_abort(&empty[s], ((it / kStages) & 1) ^ 1, p.err, 1)) {
+          ok = false;
+          break;
+        }
+        issued = it + 1;
+        mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
+        tma_load_2d(sa + s * A_BYTES, &tma_a, &full[s], kb * kBK, m0);
+        tma_load_2d(sb + s * B_BYTES, &tma_b, &full[s], kb * kBK, n0);
+        tma_load_2d(sb + s * B_BYTES + B_HALF, &tma_b, &full[s], kb * kBK, p.batch_pad + n0);
+      }
+      if (!ok) break;
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
-    constexpr uint32_t idesc = make_idesc(kBM, BN);
-    for (int kb = 0; kb < p.nk; kb++) {
-      const int s = kb % kStages;
-      if (!mbar_wait(&full[s], (kb / kStages) & 1, p.err, 2)) break;
+    constexpr uint32_t idesc = make_idesc(kBM, NC);
+    int it = 0, local = 0;
+    for (int t = blockIdx.x; t < p.tiles; t += gridDim.x, local++) {
+      const int acc = local & 1;
+      if (!wait_or_abort(&tempty[acc], ((local >> 1) & 1) ^ 1, p.err, 2)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t a0 = smem_u32(sa + s * A_BYTES), b0 = smem_u32(sb + s * B_BYTES);
+      const uint32_t d = tmem + (uint32_t)(acc * NC);
+      bool ok = true;
+      for (int kb = 0; kb < p.nk; kb++, it++) {
+        const int s = it % kStages;
+        if (!wait_or_abort(&full[s], (it / kStages) & 1, p.err, 3)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t a0 = smem_u32(sa + s * A_BYTES), b0 = smem_u32(sb + s * B_BYTES);
 #pragma unroll
-      for (int k = 0; k < kBK / kUK; k++) {
-        const uint64_t ad = sw128_desc(a0 + k * kUK * 2);
-        mma_bf16(tmem, ad, sw128_desc(b0 + k * kUK * 2), idesc, (kb | k) ? 1u : 0u);
-        mma_bf16(tmem, ad, sw128_desc(b0 + B_HALF + k * kUK * 2), idesc, 1u);
+        for (int k = 0; k < kBK / kUK; k++)
+          mma_bf16(d, sw128_desc(a0 + k * kUK * 2), sw128_desc(b0 + k * kUK * 2), idesc, (kb | k) ? 1u : 0u);
+        mma_commit(&empty[s]);
       }
-      mma_commit(&empty[s]);
+      if (!ok) break;
+      mma_commit(&tfull[acc]);
     }
-    mma_commit(done);
-  }
-  __syncwarp();
-
-  // epilogue: warp w owns TMEM lanes (pixels) 32w .. 32w+31
-  const bool ok = mbar_wait(done, 0, p.err, 3);
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (__all_sync(0xffffffffu, ok)) {
-    const int pix = m0 + warp * 32 + lane;
+  } else if (warp >= 2) {
+    // epilogue: warp w reads TMEM lanes (pixels) 32 (w % 4) .. 32 (w % 4) + 31
+    const int q = warp & 3;
+    int local = 0;
+    for (int t = blockIdx.x; t < p.tiles; t += gridDim.x, local++) {
+      const int acc = local & 1;
+      const bool ok = wait_or_abort(&tfull[acc], (local >> 1) & 1, p.err, 4);
+      if (!__all_sync(0xffffffffu, ok)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int m0 = (t / p.tiles_n) * kBM, n0 = (t % p.tiles_n) * BN;
+      const int pix = m0 + q * 32 + lane;
+      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * NC);
 #pragma unroll 1
-    for (int c0 = 0; c0 < BN; c0 += 16) {
-      uint32_t r[16];
-      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
-      if (pix < p.n_pix) {
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        uint32_t hi[16], lo[16];
+        tmem_ld16(taddr + (uint32_t)c0, hi);
+        tmem_ld16(taddr + (uint32_t)(BN + c0), lo);
+        tmem_ld_wait();
+        if (pix < p.n_pix) {
 #pragma unroll
-        for (int j = 0; j < 16; j++) {
-          const int b = n0 + c0 + j;
-          if (b < p.batch) {
-            const size_t o = (size_t)b * p.n_pix + pix;
-            p.out[o] = __uint_as_float(r[j]) * p.scale + (p.base ? p.base[o] : 0.f);
+          for (int j = 0; j < 16; j++) {
+            const int b = n0 + c0 + j;
+            if (b < p.batch) {
+              const size_t o = (size_t)b * p.n_pix + pix;
+              const float v = __uint_as_float(hi[j]) + __uint_as_float(lo[j]);
+              p.out[o] = v * p.scale + (p.base ? p.base[o] : 0.f);
+            }
           }
         }
       }
+      // this warp's reads of the accumulator are done: the MMA may overwrite it
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[acc]);
     }
   }
-  if (!ok && warp == 0 && lane == 0) {
-    // a wait timed out: give each stage's last issued load a bounded
-    // chance to land before the CTA's shared memory is released
+  __syncwarp();
+  if (warp == 0 && lane == 0 && *(volatile int*)p.err != 0) {
+    // an error stopped the CTA: give each stage's last issued load a
+    // bounded chance to land before the CTA's shared memory is released
     for (int kb = issued - 1; kb >= 0 && kb >= issued - kStages; kb--)
-      mbar_wait(&full[kb % kStages], (kb / kStages) & 1, nullptr, 0);
+      tma::mbar_wait(&full[kb % kStages], (kb / kStages) & 1, nullptr, 0);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)BN) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
   }
 }
 
@@ -343,9 +411,12 @@ int launch_tc(const void* modes, const void* coefs_t, int n_pix, int n_act_pad, 
   if (s) return s;
   const size_t smem = tc_smem_bytes<BN>();
   OOPAO_CUDA_TRY(cudaFuncSetAttribute(dm_tc_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  TcParams p{n_pix, batch, n_act_pad / kBK, batch_pad, scale, base, out, err};
-  dim3 grid(batch_pad / BN, ceil_div(n_pix, kBM));
-  dm_tc_kernel<BN><<<grid, kThreads, smem, st>>>(ta, tb, p);
+  const int tiles_n = batch_pad / BN, tiles = tiles_n * ceil_div(n_pix, kBM);
+  int dev = 0, sms = 0;
+  OOPAO_CUDA_TRY(cudaGetDevice(&dev));
+  OOPAO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  TcParams p{n_pix, batch, n_act_pad / kBK, batch_pad, tiles_n, tiles, scale, base, out, err};
+  dm_tc_kernel<BN><<<std::min(tiles, sms), kThreads, smem, st>>>(ta, tb, p);
   return OOPAO_OK;
 }
 
