@@ -532,7 +532,8 @@ def config4_leg(n_modes=500, n_screens=64, n_steps=200, sigma=50e-9, n_fd=4, see
 
 def dm_projection(peaks):
     """DM influence-function projection OPD = modes @ coefs at the 20x20,
-    40x40 and 80x80 sizes: FP32 CUDA-core path vs BF16 tcgen05 path, per
+    40x40 and 80x80 sizes: FP32 CUDA-core path vs BF16 tcgen05 path vs the
+    FP32-accuracy tcgen05 path (three TF32 products, batches from 16), per
     batch, and the separable projection of Gaussian IFs on the same actuator
     grid ('separable': factors [n_side+1][res], the DM's default path).
     Modes and factors are seeded device-random (timing does not depend on
@@ -551,6 +552,9 @@ def dm_projection(peaks):
         mt = torch.randn((n_act, n_pix), device='cuda', generator=g)
         mb = torch.empty((n_pix, n_pad), dtype=torch.bfloat16, device='cuda')
         N.call('oopao_dm_modes_bf16', mt, n_act, n_pix, n_pad, mb, st)
+        n_pad32 = (n_act + 31) // 32 * 32
+        m2 = torch.empty((2, n_pix, n_pad32), dtype=torch.float32, device='cuda')
+        N.call('oopao_dm_modes_tf32x2', mt, n_act, n_pix, n_pad32, m2, st)
         n_grid = int(name.split('x')[0]) + 1
         gxs = torch.randn((n_grid, n_side), device='cuda', generator=g)
         gys = torch.randn((n_grid, n_side), device='cuda', generator=g)
@@ -564,11 +568,16 @@ def dm_projection(peaks):
             ws = torch.zeros(nb, dtype=torch.uint8, device='cuda')
             nbs = lib.oopao_dm_sep_workspace_bytes(n_grid, n_side, B)
             wss = torch.zeros(nbs, dtype=torch.uint8, device='cuda')
+            nbt = lib.oopao_dm_tf32_workspace_bytes(n_pad32, B)
+            wst = torch.zeros(nbt, dtype=torch.uint8, device='cuda')
             runs = {'fp32': lambda: N.call('oopao_dm_opd_acc_f32', mt, c, n_act, n_pix, B, 1.0, None, o, st),
                     'bf16_tc': lambda: N.call('oopao_dm_opd_bf16', mb, n_pad, c, n_act, n_pix, B, 1.0, None, o, ws,
                                               nb, st),
                     'separable': lambda: N.call('oopao_dm_opd_sep_f32', gxs, gys, cells, n_grid, n_grid, c, n_act,
                                                 n_side, B, 1.0, None, o, wss, nbs, st)}
+            if B >= 16:
+                runs['tf32x3_tc'] = lambda: N.call('oopao_dm_opd_tf32x3', m2, n_pad32, c, n_act, n_pix, B, 1.0, None,
+                                                   o, wst, nbt, st)
             row = {'batch': B}
             for key, fn in runs.items():
                 reps = 20
@@ -585,18 +594,19 @@ def dm_projection(peaks):
                     row[key] = {'ms': ms, 'dense_equivalent_tflops': 2.0 * n_pix * n_act * B / ms / 1e9,
                                 'tflops': 2.0 * n_grid * n_side * (n_grid + n_side) * B / ms / 1e9}
                     continue
-                if_bytes = n_pix * n_act * 4 if key == 'fp32' else n_pix * n_pad * 2
+                if_bytes = {'fp32': n_pix * n_act * 4, 'bf16_tc': n_pix * n_pad * 2,
+                            'tf32x3_tc': 2 * n_pix * n_pad32 * 4}[key]
                 row[key] = {'ms': ms, 'tflops': 2.0 * n_pix * n_act * B / ms / 1e9,
                             'if_gbs': if_bytes / ms / 1e6}
                 if key == 'bf16_tc' and peaks.get('bf16_tflops'):
                     row[key]['tensor_frac_of_measured_bf16'] = row[key]['tflops'] / peaks['bf16_tflops']
                 if peaks.get('hbm_gbs'):
                     row[key]['hbm_frac_of_measured'] = row[key]['if_gbs'] / peaks['hbm_gbs']
-            row['tc_error_word'] = int(ws[:4].view(torch.int32).item())
+            row['tc_error_word'] = int(ws[:4].view(torch.int32).item()) | int(wst[:4].view(torch.int32).item())
             rows.append(row)
         out[name] = {'n_pix': n_pix, 'n_act': n_act, 'if_bf16_mb': n_pix * n_pad * 2 / 1e6,
                      'l2_resident': n_pix * n_pad * 2 < 120e6, 'rows': rows}
-        del mt, mb
+        del mt, mb, m2
         torch.cuda.empty_cache()
     return out
 
@@ -1275,15 +1285,24 @@ def run_case(args):
         dm.separable_projection = False
         c = torch.randn((dm.nValidAct, args.batch), device='cuda', generator=g) * 50e-9
         o = torch.empty((args.batch, 240, 240), device='cuda')
+        # the same IFs in FP32 for the FP32-accuracy tensor-core path
+        pad32 = (dm.nValidAct + 31) // 32 * 32
+        m2 = torch.empty((2, 240 * 240, pad32), device='cuda')
+        N.call('oopao_dm_modes_tf32x2', dm._modes_t, dm.nValidAct, 240 * 240, pad32, m2, N.stream_handle())
+        nbt = N.load().oopao_dm_tf32_workspace_bytes(pad32, args.batch)
+        wst = torch.zeros(nbt, dtype=torch.uint8, device='cuda')
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_push('case')
         for _ in range(args.reps):
             dm.opd_device(c, out=o)
             N.call('oopao_dm_opd_acc_f32', dm._modes_t, c, dm.nValidAct, 240 * 240, args.batch, 1.0, None, o,
                    N.stream_handle())
+            N.call('oopao_dm_opd_tf32x3', m2, pad32, c, dm.nValidAct, 240 * 240, args.batch, 1.0, None, o, wst, nbt,
+                   N.stream_handle())
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_pop()
-        out = {'case': args.case, 'batch': args.batch, 'reps': args.reps, 'tc_status': dm.tensor_core_status()}
+        out = {'case': args.case, 'batch': args.batch, 'reps': args.reps, 'tc_status': dm.tensor_core_status(),
+               'tf32_status': int(wst[:4].view(torch.int32).item())}
     elif args.case == 'clgsc':
         out = {'case': args.case, 'cl_gsc_20x20': cl_gsc()}
     elif args.case == 'cl':

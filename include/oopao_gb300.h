@@ -243,6 +243,19 @@ int oopao_dm_opd_bf16(const void* modes, int n_act_pad, const float* coefs, int 
 int oopao_dm_opd_bf16_tiled(const void* modes, int n_act_pad, const float* coefs, int n_act, int n_pix, int batch,
                             float scale, const float* base, float* opd, void* workspace, size_t workspace_bytes,
                             int tile_n, void* stream);
+/* The projection at FP32 accuracy on the tensor cores (tcgen05
+ * kind::tf32), for IFs that neither factorise nor are stored in BF16.
+ * oopao_dm_modes_tf32x2: modes_t [n_act][n_pix] f32 -> out device f32
+ * [2][n_pix][n_act_pad] (n_act_pad a multiple of 32): the IFs rounded to TF32,
+ * then the FP32 remainders.  oopao_dm_opd_tf32x3: opd = (modes @ coefs)^T *
+ * scale (+ base) from three TF32 products (hi*hi + hi*lo + lo*hi, FP32
+ * accumulation), relative error ~1e-6 against float64; same layouts and
+ * workspace rules as oopao_dm_opd_bf16 (the error word at its head). */
+int oopao_dm_modes_tf32x2(const float* modes_t, int n_act, int n_pix, int n_act_pad, float* out, void* stream);
+size_t oopao_dm_tf32_workspace_bytes(int n_act_pad, int batch);
+int oopao_dm_opd_tf32x3(const float* modes2, int n_act_pad, const float* coefs, int n_act, int n_pix, int batch,
+                        float scale, const float* base, float* opd, void* workspace, size_t workspace_bytes,
+                        void* stream);
 
 /* Separable influence functions (DeformableMirror.modesComputation,
  * OOPAO/DeformableMirror.py:572-600, with anamorphosisAngle = 0 on a

@@ -87,6 +87,10 @@ SIGNATURES = {
     'oopao_gsc_optical_gains': (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                         c_size_t, c_void_p]),
     'oopao_gsc_read': (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
+    'oopao_dm_modes_tf32x2': (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p]),
+    'oopao_dm_tf32_workspace_bytes': (c_size_t, [c_int, c_int]),
+    'oopao_dm_opd_tf32x3': (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_float, c_void_p, c_void_p,
+                                    c_void_p, c_size_t, c_void_p]),
     'oopao_det_saturate': (c_int, [c_void_p, c_int, c_int, c_float, c_void_p, c_void_p]),
     'oopao_det_readout_tail': (c_int, [c_void_p, c_int, c_int, c_float, c_int, c_float, c_int, c_int, c_int,
                                        c_void_p, c_void_p, c_void_p]),

@@ -176,20 +176,24 @@ def tune_dm(dm, batches=(1, 4, 16, 32, 64, 128, 300), reps=5, force=False, verbo
     """Choose the DM's projection path per batch size: the separable
     projection (Gaussian IFs that factorise) against the BF16 tensor-core
     GEMM with the library's tile rule or a 64- or 128-column batch tile
-    (if_dtype='bf16').  Sets
+    (if_dtype='bf16'); for FP32 IFs without factors, the CUDA-core FP32 GEMM
+    against the FP32-accuracy tensor-core GEMM (three TF32 products).  Sets
     dm.separable_max_batch (the largest timed batch the separable projection
-    wins, when it wins every smaller one) and dm.tc_tile_rule; returns
-    {batch: {path: ms}}."""
+    wins, when it wins every smaller one), dm.tc_tile_rule and
+    dm.tf32_min_batch (the smallest timed batch from which the TF32 GEMM wins
+    every larger one, None if it never does); returns {batch: {path: ms}}."""
     cache = _load()
     key = _dm_key(dm, ','.join(str(b) for b in batches))
     if not force and key in cache:
         e = cache[key]
         dm.separable_max_batch = int(e['separable_max_batch'])
         dm.tc_tile_rule = [tuple(r) for r in e['tc_tile_rule']]
+        dm.tf32_min_batch = e.get('tf32_min_batch', dm.tf32_min_batch)
         return e['ms']
     has_sep = dm._sep is not None
     has_tc = dm._modes_bf16 is not None
-    saved = (dm.separable_projection, dm.separable_max_batch, list(dm.tc_tile_rule))
+    has_tf32 = not has_tc and not (has_sep and dm.separable_projection)
+    saved = (dm.separable_projection, dm.separable_max_batch, list(dm.tc_tile_rule), dm.tf32_min_batch)
     out = {}
     g = torch.Generator(device=dm._dev).manual_seed(0)
     for B in batches:
@@ -203,6 +207,10 @@ def tune_dm(dm, batches=(1, 4, 16, 32, 64, 128, 300), reps=5, force=False, verbo
             for tile in (0, 64, 128):   # 0: the library's rule (a GEMV up to 4 columns)
                 dm.tc_tile_rule = [(1 << 30, tile)]
                 row['bf16_%d' % tile] = _time_call(lambda: dm.opd_device(c), reps)
+        if has_tf32:
+            for key, first in (('fp32', None), ('tf32', 1)):
+                dm.tf32_min_batch = first
+                row[key] = _time_call(lambda: dm.opd_device(c), reps)
         out[B] = row
         if verbose:
             print('B=%d' % B, row)
@@ -224,9 +232,18 @@ def tune_dm(dm, batches=(1, 4, 16, 32, 64, 128, 300), reps=5, force=False, verbo
             r = out[B]
             rule.append((B, min((0, 64, 128), key=lambda t: r['bf16_%d' % t])))
         rule.append((1 << 30, rule[-1][1]))
+    tf32_min = saved[3]
+    if has_tf32:
+        tf32_min = None
+        for B in reversed(batches):
+            if out[B]['tf32'] < out[B]['fp32']:
+                tf32_min = B
+            else:
+                break
     dm.separable_max_batch = sep_max
     dm.tc_tile_rule = rule
-    cache[key] = {'separable_max_batch': sep_max, 'tc_tile_rule': rule,
+    dm.tf32_min_batch = tf32_min
+    cache[key] = {'separable_max_batch': sep_max, 'tc_tile_rule': rule, 'tf32_min_batch': tf32_min,
                   'ms': {str(b): r for b, r in out.items()}}
     _save(cache)
     return out

@@ -381,17 +381,17 @@ __global__ void dm_modes_to_bf16(const float* __restrict__ modes_t, int n_act, i
 }
 
 int encode_2d(CUtensorMap* map, const void* base, uint64_t inner, uint64_t rows, uint32_t box_inner,
-              uint32_t box_rows) {
+              uint32_t box_rows, CUtensorMapDataType dtype = CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, uint64_t elem = 2) {
   PFN_cuTensorMapEncodeTiled_v12000 fn = tma::encode_fn();
   if (!fn) {
     oopao_set_last_error("cuTensorMapEncodeTiled is not available from the driver", __FILE__, __LINE__);
     return OOPAO_ERR_CUDA;
   }
   const cuuint64_t dims[2] = {inner, rows};
-  const cuuint64_t strides[1] = {inner * 2};
+  const cuuint64_t strides[1] = {inner * elem};
   const cuuint32_t box[2] = {box_inner, box_rows};
   const cuuint32_t estr[2] = {1, 1};
-  const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+  const CUresult r = fn(map, dtype, 2, const_cast<void*>(base), dims, strides, box, estr,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
@@ -417,6 +417,236 @@ int launch_tc(const void* modes, const void* coefs_t, int n_pix, int n_act_pad, 
   OOPAO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   TcParams p{n_pix, batch, n_act_pad / kBK, batch_pad, tiles_n, tiles, scale, base, out, err};
   dm_tc_kernel<BN><<<std::min(tiles, sms), kThreads, smem, st>>>(ta, tb, p);
+  return OOPAO_OK;
+}
+
+
+// ---- FP32-accuracy projection on the tensor cores: kind::tf32, three products ----
+// The IFs and the coefficients are each split into a TF32 part and its FP32
+// remainder, x = hi + lo with hi = tf32(x) (round to nearest) and lo = x - hi
+// (exact).  A*B = Ahi*Bhi + Ahi*Blo + Alo*Bhi + Alo*Blo; the last term is
+// ~2^-22 of the product and is dropped, the other three accumulate in FP32,
+// and lo itself enters the MMA at TF32 precision, another ~2^-22.  Per K step
+// one MMA of N = 2*BN multiplies Ahi by [Bhi; Blo] into both halves of the
+// accumulator and a second of N = BN adds Alo*Bhi to the hi half; the rest is
+// the persistent pipeline of dm_tc_kernel with FP32 tiles (32 per 128-byte row).
+constexpr int kBK3 = 32;     // FP32 actuators per stage: one 128-byte swizzle row
+constexpr int kUK3 = 8;      // K of one tcgen05.mma kind::tf32
+constexpr int kStages3 = 3;
+
+// Instruction descriptor, kind::tf32: F32 accumulator, TF32 A and B (format
+// code 2), both K-major.
+__host__ __device__ constexpr uint32_t make_idesc_tf32(int m, int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+      ::"r"(tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+template <int BN>
+constexpr size_t tc3_smem_bytes() {
+  return 1024 + (size_t)kStages3 * (2 * kBM + 2 * BN) * kBK3 * 4 + 256;
+}
+
+template <int BN>
+__global__ void __launch_bounds__(kThreads, 1)
+    dm_tc3_kernel(const __grid_constant__ CUtensorMap tma_ahi, const __grid_constant__ CUtensorMap tma_alo,
+                  const __grid_constant__ CUtensorMap tma_b, TcParams p) {
+  constexpr int NC = 2 * BN;
+  constexpr uint32_t kTmemCols = 2 * NC;
+  constexpr int A_BYTES = kBM * kBK3 * 4;        // one of Ahi, Alo
+  constexpr int B_BYTES = 2 * BN * kBK3 * 4;     // Bhi rows, then Blo rows
+  constexpr int B_HALF = BN * kBK3 * 4;
+  constexpr int S_BYTES = 2 * A_BYTES + B_BYTES;
+  static_assert(NC <= 256 && kTmemCols <= 512, "tile too wide for one MMA or for TMEM");
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages3 * S_BYTES);
+  uint64_t* empty = full + kStages3;
+  uint64_t* tfull = empty + kStages3;
+  uint64_t* tempty = tfull + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 2);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages3; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int a = 0; a < 2; a++) {
+      mbar_init(&tfull[a], 1);
+      mbar_init(&tempty[a], kEpiWarps);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  int issued = 0;
+  if (warp == 0 && lane == 0) {
+    int it = 0;
+    for (int t = blockIdx.x; t < p.tiles; t += gridDim.x) {
+      const int m0 = (t / p.tiles_n) * kBM, n0 = (t % p.tiles_n) * BN;
+      bool ok = true;
+      for (int kb = 0; kb < p.nk; kb++, it++) {
+        const int s = it % kStages3;
+        if (!wait_or_abort(&empty[s], ((it / kStages3) & 1) ^ 1, p.err, 1)) {
+          ok = false;
+          break;
+        }
+        issued = it + 1;
+        unsigned char* st = smem + s * S_BYTES;
+        mbar_expect_tx(&full[s], S_BYTES);
+        tma_load_2d(st, &tma_ahi, &full[s], kb * kBK3, m0);
+        tma_load_2d(st + A_BYTES, &tma_alo, &full[s], kb * kBK3, m0);
+        tma_load_2d(st + 2 * A_BYTES, &tma_b, &full[s], kb * kBK3, n0);
+        tma_load_2d(st + 2 * A_BYTES + B_HALF, &tma_b, &full[s], kb * kBK3, p.batch_pad + n0);
+      }
+      if (!ok) break;
+    }
+  } else if (warp == 1 && lane == 0) {
+    constexpr uint32_t idesc2 = make_idesc_tf32(kBM, NC), idesc1 = make_idesc_tf32(kBM, BN);
+    int it = 0, local = 0;
+    for (int t = blockIdx.x; t < p.tiles; t += gridDim.x, local++) {
+      const int acc = local & 1;
+      if (!wait_or_abort(&tempty[acc], ((local >> 1) & 1) ^ 1, p.err, 2)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t d = tmem + (uint32_t)(acc * NC);
+      bool ok = true;
+      for (int kb = 0; kb < p.nk; kb++, it++) {
+        const int s = it % kStages3;
+        if (!wait_or_abort(&full[s], (it / kStages3) & 1, p.err, 3)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t ahi = smem_u32(smem + s * S_BYTES), alo = ahi + A_BYTES, b0 = ahi + 2 * A_BYTES;
+#pragma unroll
+        for (int k = 0; k < kBK3 / kUK3; k++) {
+          const uint64_t bd = sw128_desc(b0 + k * kUK3 * 4);
+          mma_tf32(d, sw128_desc(ahi + k * kUK3 * 4), bd, idesc2, (kb | k) ? 1u : 0u);
+          mma_tf32(d, sw128_desc(alo + k * kUK3 * 4), bd, idesc1, 1u);
+        }
+        mma_commit(&empty[s]);
+      }
+      if (!ok) break;
+      mma_commit(&tfull[acc]);
+    }
+  } else if (warp >= 2) {
+    const int q = warp & 3;
+    int local = 0;
+    for (int t = blockIdx.x; t < p.tiles; t += gridDim.x, local++) {
+      const int acc = local & 1;
+      const bool ok = wait_or_abort(&tfull[acc], (local >> 1) & 1, p.err, 4);
+      if (!__all_sync(0xffffffffu, ok)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int m0 = (t / p.tiles_n) * kBM, n0 = (t % p.tiles_n) * BN;
+      const int pix = m0 + q * 32 + lane;
+      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * NC);
+#pragma unroll 1
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        uint32_t hi[16], lo[16];
+        tmem_ld16(taddr + (uint32_t)c0, hi);
+        tmem_ld16(taddr + (uint32_t)(BN + c0), lo);
+        tmem_ld_wait();
+        if (pix < p.n_pix) {
+#pragma unroll
+          for (int j = 0; j < 16; j++) {
+            const int b = n0 + c0 + j;
+            if (b < p.batch) {
+              const size_t o = (size_t)b * p.n_pix + pix;
+              const float v = __uint_as_float(hi[j]) + __uint_as_float(lo[j]);
+              p.out[o] = v * p.scale + (p.base ? p.base[o] : 0.f);
+            }
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[acc]);
+    }
+  }
+  __syncwarp();
+  if (warp == 0 && lane == 0 && *(volatile int*)p.err != 0) {
+    for (int kb = issued - 1; kb >= 0 && kb >= issued - kStages3; kb--)
+      tma::mbar_wait(&full[kb % kStages3], (kb / kStages3) & 1, nullptr, 0);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+  }
+}
+
+__device__ __forceinline__ float to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+// modes_t [n_act][n_pix] f32 -> [2][n_pix][n_act_pad] f32 (tf32 hi, remainder), zero padded
+__global__ void dm_modes_to_tf32x2(const float* __restrict__ modes_t, int n_act, int n_pix, int n_act_pad,
+                                   float* __restrict__ out) {
+  const size_t plane = (size_t)n_pix * n_act_pad;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= plane) return;
+  const int px = (int)(i / n_act_pad), a = (int)(i % n_act_pad);
+  const float x = a < n_act ? modes_t[(size_t)a * n_pix + px] : 0.f;
+  const float h = to_tf32(x);
+  out[i] = h;
+  out[plane + i] = x - h;
+}
+
+// coefs [n_act][batch] f32 -> [2][batch_pad][n_act_pad] f32 (tf32 hi, remainder), zero padded
+__global__ void dm_coefs_to_tf32x2(const float* __restrict__ coefs, int n_act, int batch, int n_act_pad,
+                                   int batch_pad, float* __restrict__ out) {
+  const size_t plane = (size_t)batch_pad * n_act_pad;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= plane) return;
+  const int b = (int)(i / n_act_pad), a = (int)(i % n_act_pad);
+  const float c = (a < n_act && b < batch) ? coefs[(size_t)a * batch + b] : 0.f;
+  const float h = to_tf32(c);
+  out[i] = h;
+  out[plane + i] = c - h;
+}
+
+template <int BN>
+int launch_tc3(const float* modes2, const float* coefs2, int n_pix, int n_act_pad, int batch, int batch_pad,
+               float scale, const float* base, float* out, int* err, cudaStream_t st) {
+  CUtensorMap tah, tal, tb;
+  const size_t plane = (size_t)n_pix * n_act_pad;
+  int s = encode_2d(&tah, modes2, (uint64_t)n_act_pad, (uint64_t)n_pix, kBK3, kBM, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4);
+  if (s) return s;
+  s = encode_2d(&tal, modes2 + plane, (uint64_t)n_act_pad, (uint64_t)n_pix, kBK3, kBM, CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                4);
+  if (s) return s;
+  s = encode_2d(&tb, coefs2, (uint64_t)n_act_pad, (uint64_t)(2 * batch_pad), kBK3, BN, CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                4);
+  if (s) return s;
+  const size_t smem = tc3_smem_bytes<BN>();
+  OOPAO_CUDA_TRY(cudaFuncSetAttribute(dm_tc3_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int tiles_n = batch_pad / BN, tiles = tiles_n * ceil_div(n_pix, kBM);
+  int dev = 0, sms = 0;
+  OOPAO_CUDA_TRY(cudaGetDevice(&dev));
+  OOPAO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  TcParams p{n_pix, batch, n_act_pad / kBK3, batch_pad, tiles_n, tiles, scale, base, out, err};
+  dm_tc3_kernel<BN><<<std::min(tiles, sms), kThreads, smem, st>>>(tah, tal, tb, p);
   return OOPAO_OK;
 }
 
@@ -487,6 +717,50 @@ extern "C" int oopao_dm_opd_bf16_tiled(const void* modes, int n_act_pad, const f
   dm_coefs_to_bf16<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(coefs, n_act, batch, n_act_pad, batch_pad, ct);
   const int s = bn == 64 ? launch_tc<64>(modes, ct, n_pix, n_act_pad, batch, batch_pad, scale, base, opd, err, st)
                          : launch_tc<128>(modes, ct, n_pix, n_act_pad, batch, batch_pad, scale, base, opd, err, st);
+  if (s) return s;
+  oopao_count_launches(2);
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_dm_modes_tf32x2(const float* modes_t, int n_act, int n_pix, int n_act_pad, float* out,
+                                     void* stream) {
+  OOPAO_CHECK_ARG(modes_t && out, "NULL argument");
+  OOPAO_CHECK_ARG(n_act > 0 && n_pix > 0 && n_act_pad >= n_act && n_act_pad % kBK3 == 0,
+                  "n_act_pad must be a multiple of 32 and >= n_act");
+  const size_t total = (size_t)n_pix * n_act_pad;
+  dm_modes_to_tf32x2<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(modes_t, n_act, n_pix,
+                                                                                           n_act_pad, out);
+  oopao_count_launches(1);
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}
+
+extern "C" size_t oopao_dm_tf32_workspace_bytes(int n_act_pad, int batch) {
+  if (n_act_pad <= 0 || batch <= 0) return 0;
+  const size_t batch_pad = (size_t)ceil_div(batch, 128) * 128;
+  return 256 + 2 * batch_pad * n_act_pad * 4;
+}
+
+extern "C" int oopao_dm_opd_tf32x3(const float* modes2, int n_act_pad, const float* coefs, int n_act, int n_pix,
+                                   int batch, float scale, const float* base, float* opd, void* workspace,
+                                   size_t workspace_bytes, void* stream) {
+  OOPAO_CHECK_ARG(modes2 && coefs && opd && workspace, "NULL argument");
+  OOPAO_CHECK_ARG(n_act > 0 && n_pix > 0 && batch > 0, "sizes must be positive");
+  OOPAO_CHECK_ARG(n_act_pad >= n_act && n_act_pad % kBK3 == 0, "n_act_pad must be a multiple of 32 and >= n_act");
+  OOPAO_CHECK_ARG(((uintptr_t)modes2 & 15) == 0 && ((uintptr_t)workspace & 255) == 0,
+                  "modes must be 16-byte and the workspace 256-byte aligned");
+  OOPAO_CHECK_ARG(workspace_bytes >= oopao_dm_tf32_workspace_bytes(n_act_pad, batch), "workspace too small");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int bn = batch <= 64 ? 64 : 128;
+  const int batch_pad = ceil_div(batch, bn) * bn;
+  int* err = reinterpret_cast<int*>(workspace);
+  float* ct = reinterpret_cast<float*>((char*)workspace + 256);
+  OOPAO_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
+  const size_t total = (size_t)batch_pad * n_act_pad;
+  dm_coefs_to_tf32x2<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(coefs, n_act, batch, n_act_pad, batch_pad, ct);
+  const int s = bn == 64 ? launch_tc3<64>(modes2, ct, n_pix, n_act_pad, batch, batch_pad, scale, base, opd, err, st)
+                         : launch_tc3<128>(modes2, ct, n_pix, n_act_pad, batch, batch_pad, scale, base, opd, err, st);
   if (s) return s;
   oopao_count_launches(2);
   OOPAO_CUDA_TRY(cudaGetLastError());

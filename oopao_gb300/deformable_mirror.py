@@ -134,6 +134,7 @@ class DeformableMirror:
         # and the GEMM's batch tile per batch size: [(max batch, 64 or 128)],
         # empty for the library's rule; both set by autotune.tune_dm
         self.separable_max_batch = self.SEPARABLE_MAX_BATCH_VS_TC
+        self.tf32_min_batch = self.TF32_MIN_BATCH
         self.tc_tile_rule = []
         self._sep = None
         self._sep_ws = None
@@ -281,6 +282,8 @@ class DeformableMirror:
 
     def _upload_modes(self):
         self._modes_bf16 = None
+        self._modes_tf32 = None
+        self._tc_ws = None
         if self.if_dtype == 'bf16':
             self._n_act_pad = (self.nValidAct + 63) // 64 * 64
             npix = self.resolution ** 2
@@ -312,14 +315,23 @@ class DeformableMirror:
     # 40x40 0.097 against 0.128 ms; autotune.tune_dm measures the cut-over
     # per mirror.
     SEPARABLE_MAX_BATCH_VS_TC = 1 << 30
+    # FP32 IFs that do not factorise: from this many columns on the projection
+    # runs on the tensor cores at FP32 accuracy (three TF32 products); below
+    # it the FP32 GEMV/SGEMM on the CUDA cores.  None: never.
+    TF32_MIN_BATCH = 16
 
     def projection_path(self, B=1):
         """Path of a projection of B coefficient vectors: 'separable', 'bf16'
-        (tensor cores) or 'fp32' (dense CUDA cores)."""
+        (BF16 IFs on the tensor cores), 'tf32' (FP32 IFs on the tensor cores,
+        three TF32 products) or 'fp32' (dense CUDA cores)."""
         if self._sep is not None and self.separable_projection and (
                 self._modes_bf16 is None or B <= self.separable_max_batch):
             return 'separable'
-        return 'bf16' if self._modes_bf16 is not None else 'fp32'
+        if self._modes_bf16 is not None:
+            return 'bf16'
+        if self.tf32_min_batch is not None and B >= self.tf32_min_batch:
+            return 'tf32'
+        return 'fp32'
 
     def projection_workspace_bytes(self, B):
         """Device workspace bytes the projection of B coefficient vectors needs."""
@@ -328,7 +340,22 @@ class DeformableMirror:
             return N.load().oopao_dm_sep_workspace_bytes(self._sep[4], self.resolution, B)
         if path == 'bf16':
             return N.load().oopao_dm_bf16_workspace_bytes(self._n_act_pad, B)
+        if path == 'tf32':
+            return N.load().oopao_dm_tf32_workspace_bytes(self._tf32_pad(), B)
         return 0
+
+    def _tf32_pad(self):
+        return (self.nValidAct + 31) // 32 * 32
+
+    def _tf32_modes(self, stream):
+        """The IFs as TF32 values and FP32 remainders [2][n_pix][n_act_pad],
+        built on the first tensor-core projection of FP32 IFs."""
+        if self._modes_tf32 is None:
+            npix, pad = self.resolution ** 2, self._tf32_pad()
+            m = torch.empty((2, npix, pad), dtype=torch.float32, device=self._dev)
+            N.call('oopao_dm_modes_tf32x2', self._modes_t, self.nValidAct, npix, pad, m, stream)
+            self._modes_tf32 = m
+        return self._modes_tf32
 
     def _projection_workspace(self, B):
         """The DM's own projection workspace, grown on demand (a captured
@@ -363,13 +390,17 @@ class DeformableMirror:
             tile = next((t for bound, t in self.tc_tile_rule if B <= bound), 0)
             N.call('oopao_dm_opd_bf16_tiled', self._modes_bf16, self._n_act_pad, c, self.nValidAct, res * res, B,
                    float(scale), base, out, ws, ws.numel(), tile, stream)
+        elif path == 'tf32':
+            N.call('oopao_dm_opd_tf32x3', self._tf32_modes(stream), self._tf32_pad(), c, self.nValidAct, res * res, B,
+                   float(scale), base, out, ws, ws.numel(), stream)
         else:
             N.call('oopao_dm_opd_acc_f32', self._modes_t, c, self.nValidAct, res * res, B, float(scale), base, out,
                    stream)
 
     def tensor_core_status(self):
-        """0, or the code of a timed-out pipeline wait of the last BF16 projection."""
-        if self._modes_bf16 is None or self._tc_ws is None:
+        """0, or the code of a timed-out pipeline wait of the last tensor-core
+        projection (BF16 or TF32)."""
+        if self._tc_ws is None:
             return 0
         return int(self._tc_ws[:4].view(torch.int32).item())
 

@@ -69,3 +69,26 @@ def test_tune_dm(cache):
         got = dm.opd_device(torch.as_tensor(c, dtype=torch.float32, device='cuda')).double().cpu().numpy()
         ref = (modes @ c).T.reshape(B, 120, 120)
         assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 2e-3, (B, dm.projection_path(B))
+
+
+def test_tune_dm_tf32_cut_over(cache):
+    """FP32 IFs that do not factorise (a rotated grid): the tuner times the
+    CUDA-core FP32 GEMM against the FP32-accuracy tensor-core GEMM and sets
+    the batch from which the latter runs; every batch stays at FP32 accuracy."""
+    import torch
+    import oopao_gb300 as og
+    from oopao_gb300 import autotune
+    with _quiet():
+        tel = og.Telescope(resolution=120, diameter=8.0, samplingTime=1e-3)
+        mr = og.MisRegistration({'rotationAngle': 2.0, 'shiftX': 0.0, 'shiftY': 0.0, 'anamorphosisAngle': 0,
+                                 'tangentialScaling': 0, 'radialScaling': 0})
+        dm = og.DeformableMirror(tel, nSubap=20, misReg=mr)
+    ms = autotune.tune_dm(dm, batches=(1, 16, 64, 300))
+    assert all({'fp32', 'tf32'} <= set(r) for r in ms.values())
+    assert dm.tf32_min_batch is None or dm.tf32_min_batch in (1, 16, 64, 300)
+    modes = np.asarray(dm.modes)
+    for B in (1, 16, 300):
+        c = np.random.default_rng(B).standard_normal((dm.nValidAct, B)) * 1e-8
+        got = dm.opd_device(torch.as_tensor(c, dtype=torch.float32, device='cuda')).double().cpu().numpy()
+        ref = (modes @ c).T.reshape(B, 120, 120)
+        assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 2e-6, (B, dm.projection_path(B))
