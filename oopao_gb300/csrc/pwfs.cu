@@ -1680,9 +1680,9 @@ namespace {
 // Tangent through the two passes: the operating point's filtered rows, then
 // its fields G_k stored once ([K][N][N], the storing column pass), then per
 // chunk of tangents the filtered rows of i dphi W and the tangent column
-// pass, which sums 2 w_k Re(conj(G_k) dG_k) against the stored G_k.  The
-// items of one (column block, slot) run side by side, so they share the G_k
-// columns through L2.  OOPAO_ERR_WORKSPACE (nothing launched) when one item
+// pass, which sums 2 w_k Re(conj(G_k) dG_k) against the stored G_k.  Its
+// grid puts the items fastest: the items of one (column block, slot) run side
+// by side and share the G_k columns through L2.  OOPAO_ERR_WORKSPACE (nothing launched) when one item
 // does not fit.
 int jvp_sep(const oopao_pwfs_plan* p, const float* opd0, int opd0_batch, const float* dopd, double phase_scale,
             int batch, float* dframe, char* base, size_t usable, cudaStream_t st) {
@@ -1727,7 +1727,7 @@ int jvp_sep(const oopao_pwfs_plan* p, const float* opd0, int opd0_batch, const f
     s->rows<<<dim3(ceil_div(res, s->l_rows), ng, nb), s->t * s->l_rows, s->smem_rows, st>>>(ra);
     SepColsArgs ca{p->d_tw, p->d_mcol, y, p->d_group, p->d_colfac, weights_of(p), g, nullptr, nullptr, part,
                    res, 0 /* support at row/column 0 */, ng, k / ks, ks, p->bin, cam};
-    s->cols[kSepTangent]<<<dim3(n / s->l_cols, ks, nb), s->t * s->l_cols, s->smem_cols(res), st>>>(ca);
+    s->cols[kSepTangent]<<<dim3(nb, ks, n / s->l_cols), s->t * s->l_cols, s->smem_cols(res), st>>>(ca);
     pwfs_reduce_binned<<<dim3(ceil_div(cam * cam, 256), nb), 256, 0, st>>>(part, dframe + (size_t)b0 * cam * cam,
                                                                            cam * cam, ks);
     launches += 4;

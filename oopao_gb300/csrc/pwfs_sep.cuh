@@ -241,7 +241,12 @@ __global__ void __launch_bounds__(T* L) __maxnreg__(MAXREG) pwfs_scols(SepColsAr
     twi[i] = make_float2(w.x, -w.y);
     mf[i] = a.mcol[i];
   }
-  const int b = blockIdx.z, slot = blockIdx.y, c0 = blockIdx.x * L, c = c0 + l;
+  // grid (column blocks, slots, items); the tangent form takes (items,
+  // slots, column blocks) instead, so the CTAs of one (column block, slot)
+  // for every item of the launch run together and read each G_k tile from
+  // HBM once, the others from L2
+  const int b = (MODE == kSepTangent) ? blockIdx.x : blockIdx.z;
+  const int slot = blockIdx.y, c0 = ((MODE == kSepTangent) ? blockIdx.z : blockIdx.x) * L, c = c0 + l;
   const int kbeg = slot * a.slot_pts, kend = kbeg + a.slot_pts;
   // copies of point kk's Y' tile (res rows x L columns) and colfac row,
   // issued once the previous point's stage A has read the buffer
