@@ -1303,6 +1303,27 @@ def run_case(args):
         torch.cuda.nvtx.range_pop()
         out = {'case': args.case, 'batch': args.batch, 'reps': args.reps, 'tc_status': dm.tensor_core_status(),
                'tf32_status': int(wst[:4].view(torch.int32).item())}
+    elif args.case == 'jvp40':
+        # tangent passes of the 40x40 sensor: --batch modal tangents at the
+        # flat operating point through oopao_pwfs_jvp (the storing column
+        # pass of G_k, then the tangent row and column passes of the batch)
+        from oopao_gb300 import autodiff as AD
+        res, nsub, mod, nth = CASES['pwfs40']
+        tel, ngs, dm, wfs = build_system(0, res, nsub, mod, nth, max_batch=args.batch)
+        ngs ** tel
+        wfs.plan.set_amplitude(ngs.intensity, wfs._amplitude_key())
+        c = torch.randn((dm.nValidAct, args.batch), device='cuda', generator=g) * 1e-8
+        dopd = dm.opd_device(c)
+        opd0 = torch.zeros((1, res, res), device='cuda')
+        AD.frame_jvp(wfs, opd0, dopd)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push('case')
+        for _ in range(args.reps):
+            df = AD.frame_jvp(wfs, opd0, dopd)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        out = {'case': args.case, 'batch': args.batch, 'reps': args.reps,
+               'dframe_norm': float(df.double().norm().item())}
     elif args.case == 'clgsc':
         out = {'case': args.case, 'cl_gsc_20x20': cl_gsc()}
     elif args.case == 'cl':
@@ -1337,7 +1358,7 @@ def main():
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline and accuracy legs')
     ap.add_argument('--no-extra', action='store_true',
                     help='skip the interaction-matrix comparisons and the closed-loop rate')
-    ap.add_argument('--case', default=None, help='run a small profiling workload (%s, dm40, gsc, next, clgsc, cl, c4, c5, dmproj) instead'
+    ap.add_argument('--case', default=None, help='run a small profiling workload (%s, dm40, jvp40, gsc, next, clgsc, cl, c4, c5, dmproj) instead'
                     % ', '.join(CASES))
     ap.add_argument('--batch', type=int, default=16)
     ap.add_argument('--reps', type=int, default=3)

@@ -93,3 +93,23 @@ def test_gradient_descent_lowers_the_loss(problem):
     assert hist[-1] < 0.5 * hist[0]
     loss = AD.modal_loss(wfs, dm, m2c, x, targets).cpu().numpy()
     assert np.isfinite(loss).all()
+
+
+def test_lift_gauss_newton_recovers_kl_modes(problem):
+    """LiFT's Gauss-Newton modal estimation (OOPAO/LiFT.py:297-330 pattern,
+    the pyramid signal as the measurement) on this configuration: 40 KL
+    coefficients ~N(0, 5 nm) (wavefronts of ~30 nm RMS, 0.4 rad at 500 nm,
+    where the sensor is already non-linear) are recovered from their signal to
+    1e-3 relative in six iterations, the Jacobian re-formed from batched
+    tangents at each estimate."""
+    import torch
+    from oopao_gb300 import autodiff as AD
+    tel, ngs, dm, wfs, m2c, truth, targets = problem
+    small = np.random.default_rng(8).standard_normal((N_MODES, 2)) * 5e-9
+    m = torch.as_tensor(m2c, dtype=torch.float32, device='cuda')
+    with torch.no_grad():
+        t = AD.dm_signal(wfs, dm, m @ torch.as_tensor(small, dtype=torch.float32, device='cuda'))
+    for b in range(2):
+        x = AD.lift_estimate(wfs, dm, m2c, t[b], n_iter=6)
+        err = np.linalg.norm(x.double().cpu().numpy() - small[:, b]) / np.linalg.norm(small[:, b])
+        assert err < 1e-3, (b, err)
