@@ -136,6 +136,7 @@ static const float* weights_of(const oopao_pwfs_plan* p) { return p->weights_on 
 // (shared by every modulation point).
 __global__ void pwfs_field(const float* __restrict__ opd, float scale, const float* __restrict__ amp,
                            float2* __restrict__ field, int npix) {
+  pdl_wait();
   const int b = blockIdx.y;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= npix) return;
@@ -466,6 +467,7 @@ constexpr int kSigCells = 8;
 
 __global__ void pwfs_signal(SignalArgs a) {
   __shared__ float red[33];
+  pdl_wait();
   const int b = blockIdx.x;
   const float* fr = a.frame + (size_t)b * a.cam * a.cam;
   float* s2 = a.signal_2d + (size_t)b * a.n2d;
@@ -1047,6 +1049,7 @@ extern "C" size_t oopao_pwfs_workspace_bytes(const oopao_pwfs_plan* p, int batch
 
 __global__ void pwfs_reduce_binned(const float* __restrict__ binned, float* __restrict__ frame, int cam2,
                                    int ksplit) {
+  pdl_wait();
   const int b = blockIdx.y;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= cam2) return;
@@ -1147,22 +1150,25 @@ int measure_sep(const oopao_pwfs_plan* p, const float* opd, double phase_scale, 
   for (int b0 = 0; b0 < batch; b0 += bc) {
     const int nb = std::min(bc, batch - b0);
     mark(0);
-    pwfs_field<<<dim3(ceil_div(res * res, 256), nb), 256, 0, st>>>(opd + (size_t)b0 * res * res, (float)phase_scale,
-                                                                   p->d_amp, field, res * res);
+    OOPAO_CUDA_TRY(launch_pdl(pwfs_field, dim3(ceil_div(res * res, 256), nb), dim3(256), 0, st,
+                              opd + (size_t)b0 * res * res, (float)phase_scale, (const float*)p->d_amp, field,
+                              res * res));
     mark(0);
     SepRowsArgs ra{p->d_tw, field, p->d_growfac, p->d_mrow, y, res, ng, 0 /* support at row/column 0 */};
     mark(0);
-    s->rows<<<dim3(ceil_div(res, s->l_rows), ng, nb), s->t * s->l_rows, s->smem_rows, st>>>(ra);
+    OOPAO_CUDA_TRY(launch_pdl(s->rows, dim3(ceil_div(res, s->l_rows), ng, nb), dim3(s->t * s->l_rows), s->smem_rows,
+                              st, ra));
     mark(0);
     SepColsArgs ca{p->d_tw, p->d_mcol, y, p->d_group, p->d_colfac, weights_of(p), nullptr, nullptr,
                    fused ? nullptr : part, fused ? part : nullptr, res, 0 /* support at row/column 0 */, ng, k / ks, ks, p->bin, cam};
     mark(1);
-    s->cols[kSepIntensity]<<<dim3(n / s->l_cols, ks, nb), s->t * s->l_cols, s->smem_cols(res), st>>>(ca);
+    OOPAO_CUDA_TRY(launch_pdl(s->cols[kSepIntensity], dim3(n / s->l_cols, ks, nb), dim3(s->t * s->l_cols),
+                              s->smem_cols(res), st, ca));
     mark(1);
     mark(3);
     if (fused) {
-      pwfs_reduce_binned<<<dim3(ceil_div(cam * cam, 256), nb), 256, 0, st>>>(part, frame + (size_t)b0 * cam * cam,
-                                                                             cam * cam, ks);
+      OOPAO_CUDA_TRY(launch_pdl(pwfs_reduce_binned, dim3(ceil_div(cam * cam, 256), nb), dim3(256), 0, st,
+                                (const float*)part, frame + (size_t)b0 * cam * cam, cam * cam, ks));
     } else {
       pwfs_bin<<<dim3(cam, nb), 128, 0, st>>>(part, frame + (size_t)b0 * cam * cam,
                                               raw + (size_t)b0 * n * n, n, cam, p->bin, ks);
@@ -1536,7 +1542,7 @@ extern "C" int oopao_pwfs_signal(const oopao_pwfs_plan* p, const float* frame, i
   a.n_valid = p->cam2;
   for (int q = 0; q < 4; q++) { a.q_r0[q] = p->q_r0[q]; a.q_c0[q] = p->q_c0[q]; }
   a.units = p->slopes_units; a.norma_const = p->norma_const;
-  pwfs_signal<<<batch, 512, 0, (cudaStream_t)stream>>>(a);
+  OOPAO_CUDA_TRY(launch_pdl(pwfs_signal, dim3(batch), dim3(512), 0, (cudaStream_t)stream, a));
   oopao_count_launches(1);
   OOPAO_CUDA_TRY(cudaGetLastError());
   return OOPAO_OK;

@@ -147,6 +147,7 @@ __global__ void __launch_bounds__(T* L) pwfs_srows(SepRowsArgs a) {
     twi[i] = make_float2(w.x, -w.y);
     mf[i] = a.mrow[i];
   }
+  pdl_wait();  // the field comes from the previous kernel
   __syncthreads();
   const int b = blockIdx.z, g = blockIdx.y, row = blockIdx.x * L + l;
   const bool active = row < a.res;
@@ -260,6 +261,7 @@ __global__ void __launch_bounds__(T* L) __maxnreg__(MAXREG) pwfs_scols(SepColsAr
     for (int i = tid; i < res / 2; i += T * L) cp_async16(tile + res * L + 2 * i, cfs + 2 * i);
     cp_async_commit();
   };
+  pdl_wait();  // the filtered rows come from the previous kernel
   issue(kbeg);
   float acc[PBA][R1];
 #pragma unroll
