@@ -117,7 +117,11 @@ int oopao_pwfs_variant_info(const oopao_pwfs_plan* plan, int variant, int* info)
  * with 1 <= i <= num_separable selects compile-time two-pass plan i (radix
  * order, columns per CTA) and uses the two passes whenever they apply (a new
  * plan starts on plan 1).  separable() returns 1 when a measure call without
- * a focal-plane frame takes the two-pass path, else 0. */
+ * a focal-plane frame takes the two-pass path, 2 when every mask of the plan
+ * varies along one focal-plane axis only (the Bi-O Edge knife edges without
+ * tip/tilt shifts, OOPAO/BioEdge.py:331-392) and a call takes the one-axis
+ * path (filtered lines of that axis only, no column transform), else 0;
+ * set_separable(plan, 0) turns both off. */
 int oopao_pwfs_set_separable(oopao_pwfs_plan* plan, int enable);
 int oopao_pwfs_separable(const oopao_pwfs_plan* plan);
 int oopao_pwfs_num_separable(const oopao_pwfs_plan* plan);

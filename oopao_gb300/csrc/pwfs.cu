@@ -116,6 +116,21 @@ struct oopao_pwfs_plan {
   // differ), and its resident column-pass CTAs
   const struct SepPasses* sep_ad;
   int sep_ad_ctas;
+  // Masks that each vary along one focal-plane axis only (the Bi-O Edge knife
+  // edges, OOPAO/BioEdge.py:331-392, without their tip/tilt shifts).  The
+  // filter then acts on the lines of that axis alone, and |G_k|^2 no longer
+  // depends on the point's phasor along the other axis: the frame of such a
+  // mask is sum over the groups of points sharing that axis' phasor of
+  // (their weight) |filtered line|^2 (measure_edge).
+  bool edge_1d;
+  int edge_axis[8];               // 0: the mask varies along x (a row), 1: along y (a column)
+  float2* d_edge_filt;            // [n_masks][n] the 1-D factors, pupil offset folded in
+  int nygroups;                   // points with equal y_k
+  float2* d_ygrowfac;             // [nygroups*res] their column phasor, with the 1/n^2 of ifft2
+  float* d_gsum;                  // [2][k] points per x-group, per y-group (unweighted)
+  float* d_gsum_w;                // [2][k] weights summed per x-group, per y-group
+  int* h_group;                   // [k] x-group of each point (host)
+  int* h_ygroup;                  // [k] y-group of each point (host)
   // signal processing
   int sp_mode, nq, n2d, n_signal, cam2;
   int q_r0[4], q_c0[4];
@@ -629,6 +644,12 @@ void free_plan(oopao_pwfs_plan* p) {
   cudaFree(p->d_masks);
   cudaFree(p->d_mrow);
   cudaFree(p->d_mcol);
+  cudaFree(p->d_edge_filt);
+  cudaFree(p->d_ygrowfac);
+  cudaFree(p->d_gsum);
+  cudaFree(p->d_gsum_w);
+  free(p->h_group);
+  free(p->h_ygroup);
   free(p);
 }
 
@@ -735,6 +756,57 @@ cudaError_t sep_setup(oopao_pwfs_plan* p, const float* mask_host) {
   return e;
 }
 
+// Masks that each vary along one axis only: mask m is f_m[c] on every row
+// (axis 0) or g_m[r] on every column (axis 1), within 1e-6 of max|M| (the
+// tolerance of factor_mask).  Such a mask filters the lines of one axis and
+// leaves the other untouched, so measure_edge needs the filtered lines of
+// each axis only.  The factors carry the pupil-offset phase of sep_setup.
+// Leaves edge_1d false when a mask is two-dimensional or no two-pass plan
+// serves n.
+cudaError_t edge_setup(oopao_pwfs_plan* p, int n_masks, const float* masks_host) {
+  p->edge_1d = false;
+  if (!p->sep || !sep_fits(p->sep, p->res) || n_masks < 1 || n_masks > 8) return cudaSuccess;
+  const int n = p->n;
+  const size_t nn = (size_t)n * n;
+  const float2* all = reinterpret_cast<const float2*>(masks_host);
+  std::vector<float2> filt((size_t)n_masks * n);
+  int axis[8];
+  for (int m = 0; m < n_masks; m++) {
+    const float2* M = all + (size_t)m * nn;
+    double mx = 0.0;
+    for (size_t i = 0; i < nn; i++) mx = std::max(mx, (double)M[i].x * M[i].x + (double)M[i].y * M[i].y);
+    const double tol2 = 1e-12 * mx;
+    auto same = [&](const float2& a, const float2& b) {
+      const double dr = (double)a.x - b.x, di = (double)a.y - b.y;
+      return dr * dr + di * di <= tol2;
+    };
+    bool along_x = true, along_y = true;
+    for (int r = 0; r < n && (along_x || along_y); r++)
+      for (int c = 0; c < n && (along_x || along_y); c++) {
+        if (along_x && !same(M[(size_t)r * n + c], M[c])) along_x = false;
+        if (along_y && !same(M[(size_t)r * n + c], M[(size_t)r * n])) along_y = false;
+      }
+    if (!along_x && !along_y) return cudaSuccess;
+    axis[m] = along_x ? 0 : 1;
+    for (int u = 0; u < n; u++) {
+      const float2 f = along_x ? M[u] : M[(size_t)u * n];
+      const long long q = ((long long)u * p->off) % n;
+      const double a = -2.0 * M_PI * (double)q / n, cr = cos(a), ci = sin(a);
+      filt[(size_t)m * n + u] = make_float2((float)(f.x * cr - f.y * ci), (float)(f.x * ci + f.y * cr));
+    }
+  }
+  cudaError_t e = cudaSuccess;
+  if (!p->d_edge_filt) e = cudaMalloc((void**)&p->d_edge_filt, sizeof(float2) * 8 * n);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(p->d_edge_filt, filt.data(), sizeof(float2) * filt.size(), cudaMemcpyHostToDevice);
+  int ctas = 0;
+  if (e == cudaSuccess) e = sep_attrs_for(p->sep, p->res, &ctas);
+  if (e != cudaSuccess) return e;
+  for (int m = 0; m < n_masks; m++) p->edge_axis[m] = axis[m];
+  p->edge_1d = true;
+  return cudaSuccess;
+}
+
 // numpy.linspace(-pi, pi, res)[j]
 double tt_grid(int j, int res) {
   if (res == 1) return -M_PI;
@@ -824,6 +896,41 @@ extern "C" int oopao_pwfs_plan_create(oopao_pwfs_plan** out, int res, int n, int
     group[kk] = g;
   }
   p->ngroups = (int)gx.size();
+  // the same for y_k: the column phasors of the points with equal y_k, for
+  // masks that vary along y only (with the 1/n^2 the row phasors carry)
+  std::vector<double> gy;
+  std::vector<int> ygroup(k);
+  std::vector<float2> ygrowfac;
+  for (int kk = 0; kk < k; kk++) {
+    const double yk = path_host ? path_host[2 * kk + 1] : 0.0;
+    int g = -1;
+    for (size_t q = 0; q < gy.size(); q++)
+      if (fabs(gy[q] - yk) <= 1e-12 * std::max(1.0, fabs(yk))) { g = (int)q; break; }
+    if (g < 0) {
+      g = (int)gy.size();
+      gy.push_back(yk);
+      for (int j = 0; j < res; j++) {
+        const float2 c = colfac[(size_t)kk * res + j];
+        ygrowfac.push_back(make_float2((float)(c.x * inv_n2), (float)(c.y * inv_n2)));
+      }
+    }
+    ygroup[kk] = g;
+  }
+  p->nygroups = (int)gy.size();
+  p->h_group = (int*)malloc(sizeof(int) * k);
+  p->h_ygroup = (int*)malloc(sizeof(int) * k);
+  if (!p->h_group || !p->h_ygroup) {
+    free_plan(p);
+    oopao_set_last_error("host allocation failed", __FILE__, __LINE__);
+    return OOPAO_ERR_CUDA;
+  }
+  std::vector<float> gsum(2 * (size_t)k, 0.f);
+  for (int kk = 0; kk < k; kk++) {
+    p->h_group[kk] = group[kk];
+    p->h_ygroup[kk] = ygroup[kk];
+    gsum[group[kk]] += 1.f;
+    gsum[k + ygroup[kk]] += 1.f;
+  }
   std::vector<float> ones((size_t)res * res, 0.f);
 #define ALLOC_COPY(dst, src, bytes)                                   \
   do {                                                                \
@@ -842,6 +949,9 @@ extern "C" int oopao_pwfs_plan_create(oopao_pwfs_plan** out, int res, int n, int
   ALLOC_COPY(p->d_colfac, colfac.data(), sizeof(float2) * colfac.size());
   ALLOC_COPY(p->d_growfac, growfac.data(), sizeof(float2) * growfac.size());
   ALLOC_COPY(p->d_group, group.data(), sizeof(int) * group.size());
+  ALLOC_COPY(p->d_ygrowfac, ygrowfac.data(), sizeof(float2) * ygrowfac.size());
+  ALLOC_COPY(p->d_gsum, gsum.data(), sizeof(float) * gsum.size());
+  ALLOC_COPY(p->d_gsum_w, gsum.data(), sizeof(float) * gsum.size());
   {
     std::vector<float2> mc((size_t)n * n), ones((size_t)k * n, make_float2(1.f, 0.f));
     const float2* m = reinterpret_cast<const float2*>(mask_host);
@@ -868,6 +978,7 @@ extern "C" int oopao_pwfs_plan_create(oopao_pwfs_plan** out, int res, int n, int
     p->sep_on = true;
   }
   if (e == cudaSuccess) e = sep_setup(p, mask_host);
+  if (e == cudaSuccess) e = edge_setup(p, 1, mask_host);
   if (e != cudaSuccess) {
     oopao_set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
     free_plan(p);
@@ -923,6 +1034,7 @@ extern "C" int oopao_pwfs_set_masks(oopao_pwfs_plan* p, int n_masks, const float
   p->d_masks = nullptr;
   p->mask_sep = false;
   if (n_masks == 1) OOPAO_CUDA_TRY(sep_setup(p, masks_host));
+  OOPAO_CUDA_TRY(edge_setup(p, n_masks, masks_host));
   if (n_masks > 1) {
     OOPAO_CUDA_TRY(cudaMalloc((void**)&p->d_masks, sizeof(float2) * nn * n_masks));
     OOPAO_CUDA_TRY(cudaMemcpy(p->d_masks, masks_host, sizeof(float2) * nn * n_masks, cudaMemcpyHostToDevice));
@@ -943,6 +1055,14 @@ extern "C" int oopao_pwfs_set_weights(oopao_pwfs_plan* p, const float* w) {
   }
   if (!p->d_weights) OOPAO_CUDA_TRY(cudaMalloc((void**)&p->d_weights, sizeof(float) * p->k));
   OOPAO_CUDA_TRY(cudaMemcpy(p->d_weights, w, sizeof(float) * p->k, cudaMemcpyHostToDevice));
+  // the weights summed over the groups of points that share a phasor
+  // (masks that vary along one axis only)
+  std::vector<float> gs(2 * (size_t)p->k, 0.f);
+  for (int kk = 0; kk < p->k; kk++) {
+    gs[p->h_group[kk]] += w[kk];
+    gs[p->k + p->h_ygroup[kk]] += w[kk];
+  }
+  OOPAO_CUDA_TRY(cudaMemcpy(p->d_gsum_w, gs.data(), sizeof(float) * gs.size(), cudaMemcpyHostToDevice));
   p->weights_on = true;
   return OOPAO_OK;
 }
@@ -1059,6 +1179,77 @@ __global__ void pwfs_reduce_binned(const float* __restrict__ binned, float* __re
   frame[(size_t)b * cam2 + i] = s;
 }
 
+// ---- masks that vary along one axis only (measure_edge) ----
+
+// out[b][x][y] = in[b][y][x] for res x res complex maps, through a 32 x 32 tile.
+__global__ void __launch_bounds__(256) edge_transpose(const float2* __restrict__ in, float2* __restrict__ out,
+                                                      int res) {
+  __shared__ float2 tile[32][33];
+  const size_t plane = (size_t)res * res;
+  const float2* src = in + (size_t)blockIdx.z * plane;
+  float2* dst = out + (size_t)blockIdx.z * plane;
+  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+  for (int dy = threadIdx.y; dy < 32; dy += 8) {
+    const int y = y0 + dy, x = x0 + threadIdx.x;
+    if (y < res && x < res) tile[dy][threadIdx.x] = src[(size_t)y * res + x];
+  }
+  __syncthreads();
+  for (int dx = threadIdx.y; dx < 32; dx += 8) {
+    const int x = x0 + dx, y = y0 + threadIdx.x;
+    if (x < res && y < res) dst[(size_t)x * res + y] = tile[threadIdx.x][dx];
+  }
+}
+
+struct EdgeBinArgs {
+  const float2* lines;  // mask m at lines + m * mask_stride: [items][ng[m]][res][n] filtered lines
+  size_t mask_stride;
+  int ng[8], axis[8];
+  const float* gsum;    // [2][k]: weight of each x-group, then of each y-group
+  int k, res, n, off, cam, bin, n_masks;
+  float* frame;         // [items][n_masks][cam][cam]
+  float* raw;           // [items][n_masks][n][n] un-binned intensity, or null
+  float nsq;            // n * n
+};
+
+// Camera frames of masks that vary along one axis only.  |G_k|^2 is then the
+// squared filtered line of point k's group (the phasor along the other axis
+// has unit modulus and is not transformed), so a frame is sum over groups of
+// (group weight) |line|^2: lines along x hold the pupil rows [off, off+res) of
+// the grid, lines along y its pupil columns.  One CTA per (camera row, mask,
+// item): each thread sums a grid column over the camera row's bin rows and
+// the groups (writing each grid pixel to raw when asked), then the columns
+// are summed in bins.
+__global__ void __launch_bounds__(256) edge_bin(EdgeBinArgs a) {
+  extern __shared__ float colsum[];  // [n]
+  const int cy = blockIdx.x, m = blockIdx.y, b = blockIdx.z;
+  const int ng = a.ng[m], ax = a.axis[m], res = a.res, n = a.n;
+  const float* w = a.gsum + (ax ? a.k : 0);
+  const float2* L = a.lines + m * a.mask_stride + (size_t)b * ng * res * n;
+  for (int X = threadIdx.x; X < n; X += blockDim.x) {
+    float s = 0.f;
+    for (int dy = 0; dy < a.bin; dy++) {
+      const int Y = cy * a.bin + dy;
+      const int line = ax == 0 ? Y - a.off : X - a.off, pos = ax == 0 ? X : Y;
+      float v = 0.f;
+      if (line >= 0 && line < res)
+        for (int g = 0; g < ng; g++) v = fmaf(w[g], cabs2(L[((size_t)g * res + line) * n + pos]), v);
+      // the line phasors carry the 1/n^2 of the 2-D inverse transform, but
+      // only one axis went through the unnormalised transform pair (a gain
+      // of n): n^2 back in intensity
+      v *= a.nsq;
+      if (a.raw) a.raw[(((size_t)b * a.n_masks + m) * n + Y) * n + X] = v;
+      s += v;
+    }
+    colsum[X] = s;
+  }
+  __syncthreads();
+  for (int cx = threadIdx.x; cx < a.cam; cx += blockDim.x) {
+    float t = 0.f;
+    for (int dx = 0; dx < a.bin; dx++) t += colsum[cx * a.bin + dx];
+    a.frame[(((size_t)b * a.n_masks + m) * a.cam + cy) * a.cam + cx] = t;
+  }
+}
+
 namespace {
 int measure_impl(const oopao_pwfs_plan* p, const float* opd, double phase_scale, int batch, float* frame,
                  float* raw, float* focal, void* ws, size_t ws_bytes, void* stream);
@@ -1119,6 +1310,70 @@ size_t sep_chunk_bytes(const oopao_pwfs_plan* p, int bc, int ks, bool fused) {
   const size_t f = (size_t)p->res * p->res * sizeof(float2);
   const size_t part = (size_t)ks * (fused ? (size_t)p->cam * p->cam : (size_t)p->n * p->n) * sizeof(float);
   return (size_t)bc * (y + f + part) + 1024;
+}
+
+// The frames of masks that each vary along one axis only (edge_setup): per
+// chunk of items the field and, for masks along y, its transpose; one
+// two-pass row launch per mask over the groups of points that share the
+// phasor of its axis (with the mask's 1-D factor as the filter); then
+// edge_bin.  No column transform is needed.  OOPAO_ERR_WORKSPACE (nothing
+// launched) when one item does not fit.
+bool edge_applies(const oopao_pwfs_plan* p, bool focal) {
+  return p->edge_1d && p->sep && p->sep_on && p->variant >= 1 && !focal;
+}
+
+int measure_edge(const oopao_pwfs_plan* p, const float* opd, double phase_scale, int batch, float* frame,
+                 float* raw, char* base, size_t usable, cudaStream_t st) {
+  const SepPasses* s = p->sep;
+  const int n = p->n, res = p->res, cam = p->cam, nm = p->n_masks;
+  const int gmax = std::max(p->ngroups, p->nygroups);
+  bool any_y = false;
+  for (int m = 0; m < nm; m++) any_y |= p->edge_axis[m] == 1;
+  // per item: the field (and its transpose), then each mask's filtered lines
+  const size_t lines_mask = (size_t)gmax * res * n;  // float2 per item and mask (room for either axis)
+  const size_t item = sizeof(float2) * ((size_t)res * res * (any_y ? 2 : 1) + (size_t)nm * lines_mask);
+  if (item + 1024 > usable) return OOPAO_ERR_WORKSPACE;
+  const int bc = (int)std::min<size_t>((size_t)batch, (usable - 1024) / item);
+  float2* field = (float2*)base;
+  float2* field_t = field + (size_t)bc * res * res;
+  float2* lines = field_t + (any_y ? (size_t)bc * res * res : 0);
+  EdgeBinArgs ea{};
+  ea.lines = lines;
+  ea.mask_stride = (size_t)bc * lines_mask;
+  for (int m = 0; m < nm; m++) {
+    ea.axis[m] = p->edge_axis[m];
+    ea.ng[m] = p->edge_axis[m] ? p->nygroups : p->ngroups;
+  }
+  ea.gsum = p->weights_on ? p->d_gsum_w : p->d_gsum;
+  ea.k = p->k; ea.res = res; ea.n = n; ea.off = p->off; ea.cam = cam; ea.bin = p->bin; ea.n_masks = nm;
+  ea.nsq = (float)n * (float)n;
+  int launches = 0;
+  for (int b0 = 0; b0 < batch; b0 += bc) {
+    const int nb = std::min(bc, batch - b0);
+    OOPAO_CUDA_TRY(launch_pdl(pwfs_field, dim3(ceil_div(res * res, 256), nb), dim3(256), 0, st,
+                              opd + (size_t)b0 * res * res, (float)phase_scale, (const float*)p->d_amp, field,
+                              res * res));
+    launches++;
+    if (any_y) {
+      edge_transpose<<<dim3(ceil_div(res, 32), ceil_div(res, 32), nb), dim3(32, 8), 0, st>>>(field, field_t, res);
+      launches++;
+    }
+    for (int m = 0; m < nm; m++) {
+      const bool ya = p->edge_axis[m] == 1;
+      SepRowsArgs ra{p->d_tw, ya ? field_t : field, ya ? p->d_ygrowfac : p->d_growfac, p->d_edge_filt + (size_t)m * n,
+                     lines + (size_t)m * ea.mask_stride, res, ea.ng[m], 0 /* support at line position 0 */};
+      OOPAO_CUDA_TRY(launch_pdl(s->rows, dim3(ceil_div(res, s->l_rows), ea.ng[m], nb), dim3(s->t * s->l_rows),
+                                s->smem_rows, st, ra));
+      launches++;
+    }
+    ea.frame = frame + (size_t)b0 * nm * cam * cam;
+    ea.raw = raw ? raw + (size_t)b0 * nm * n * n : nullptr;
+    edge_bin<<<dim3(cam, nm, nb), 256, sizeof(float) * n, st>>>(ea);
+    launches++;
+  }
+  oopao_count_launches(launches);
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
 }
 
 // Two-pass measurement (pwfs_sep.cuh): field, filtered rows of every
@@ -1188,6 +1443,10 @@ int measure_impl(const oopao_pwfs_plan* p, const float* opd, double phase_scale,
   cudaStream_t st = (cudaStream_t)stream;
   uintptr_t base = ((uintptr_t)ws + 255) & ~(uintptr_t)255;
   const size_t usable = ws_bytes > (base - (uintptr_t)ws) ? ws_bytes - (base - (uintptr_t)ws) : 0;
+  if (edge_applies(p, focal != nullptr)) {
+    const int r = measure_edge(p, opd, phase_scale, batch, frame, raw, (char*)base, usable, st);
+    if (r != OOPAO_ERR_WORKSPACE) return r;
+  }
   if (sep_applies(p, focal != nullptr, raw != nullptr)) {
     const int r = measure_sep(p, opd, phase_scale, batch, frame, raw, (char*)base, usable, st);
     if (r != OOPAO_ERR_WORKSPACE) return r;  // else the three-pass path below, in smaller passes
@@ -2052,6 +2311,7 @@ extern "C" int oopao_pwfs_num_separable(const oopao_pwfs_plan* p) {
 
 extern "C" int oopao_pwfs_separable(const oopao_pwfs_plan* p) {
   if (!p) return -1;
+  if (edge_applies(p, false)) return 2;
   return sep_applies(p, false, false) ? 1 : 0;
 }
 

@@ -109,3 +109,38 @@ def test_shared_forward_matches_per_mask_plans(system):
         rr = raw[:, i * n:(i + 1) * n, j * n:(j + 1) * n].double().cpu().numpy()
         assert O.rel_l2(ft, tile.double().cpu().numpy()) < 1e-6, q
         assert O.rel_l2(rr, rt.double().cpu().numpy()) < 1e-6, q
+
+
+def test_one_axis_path_matches_three_passes(system):
+    """The Bi-O Edge masks vary along one focal-plane axis each, so their plans
+    take the one-axis path (filtered lines of that axis, |line|^2 summed over
+    the points that share the other axis' phasor, no column transform):
+    frames and raw data equal those of the three-pass path to float32
+    round-off, for a batch with and without per-point weights."""
+    import torch
+    from oopao_gb300 import _native as N
+    d, tel, ngs, dm, wfs = system
+    plans = wfs.plans
+    assert all(N.call('oopao_pwfs_separable', p.h) == 2 for p in plans)
+    rng = np.random.default_rng(12)
+    opd = torch.as_tensor(rng.standard_normal((3, tel.resolution, tel.resolution)) * 50e-9, dtype=torch.float32,
+                          device='cuda')
+    scale = 2 * np.pi / ngs.wavelength
+    ngs ** tel
+    for weights in (None, rng.uniform(0.5, 1.5, wfs.nTheta)):
+        # weights apply to a single wavefront (a 2-D OPD), as in the reference
+        wfs._weight_vector = weights
+        o = opd[0] if weights is not None else opd
+        f1, r1 = wfs._measure_frames(o, scale, want_raw=True)
+        f1b, _ = wfs._measure_frames(o, scale, want_raw=False)
+        for p in plans:
+            N.call('oopao_pwfs_set_separable', p.h, 0)
+        try:
+            f3, r3 = wfs._measure_frames(o, scale, want_raw=True)
+        finally:
+            for p in plans:
+                N.call('oopao_pwfs_set_separable', p.h, 1)
+        assert O.rel_l2(f1.double().cpu().numpy(), f3.double().cpu().numpy()) < 2e-6
+        assert O.rel_l2(f1b.double().cpu().numpy(), f3.double().cpu().numpy()) < 2e-6
+        assert O.rel_l2(r1.double().cpu().numpy(), r3.double().cpu().numpy()) < 2e-6
+    wfs._weight_vector = None
