@@ -34,9 +34,7 @@
 namespace {
 
 constexpr int kBM = 128;     // pixels per tile = TMEM lanes
-constexpr int kBK = 64;      // actuators per stage: one 128-byte swizzle row of BF16
-constexpr int kUK = 16;      // K of one tcgen05.mma kind::f16
-constexpr int kStages = 4;
+constexpr int kBK = 64;      // BF16 actuators per stage (n_act_pad granularity of the BF16 IFs)
 constexpr int kEpiWarps = 4;                 // one per quarter of the TMEM lanes
 constexpr int kThreads = 64 + 32 * kEpiWarps;  // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 
@@ -93,20 +91,43 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
   return d;
 }
 
-// Instruction descriptor, kind::f16: F32 accumulator, BF16 A and B, both
-// K-major, N >> 3 at bit 17, M >> 4 at bit 24.
-__host__ __device__ constexpr uint32_t make_idesc(int m, int n) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
-}
+// The two operand forms of the GEMM.  BF16: the IFs in BF16, the
+// coefficients as hi + lo BF16 terms, one product (kind::f16).  TF32: the IFs
+// and the coefficients each as a TF32 value plus its FP32 remainder, three
+// products (kind::tf32), FP32 accuracy.  Both stage 128-byte swizzled rows.
+template <bool TF32>
+struct TcKind {
+  static constexpr int kElem = TF32 ? 4 : 2;     // bytes per operand element
+  static constexpr int kBK = 128 / kElem;       // K per stage: one 128-byte swizzle row
+  static constexpr int kUK = TF32 ? 8 : 16;      // K of one MMA
+  static constexpr int kStages = TF32 ? 3 : 4;
+  static constexpr int kAPlanes = TF32 ? 2 : 1;  // A: values (then remainders)
+  // instruction descriptor: F32 accumulator, A and B of format BF16 (1) or
+  // TF32 (2), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+  static __host__ __device__ constexpr uint32_t idesc(int m, int n) {
+    return (1u << 4) | ((TF32 ? 2u : 1u) << 7) | ((TF32 ? 2u : 1u) << 10) | ((uint32_t)(n >> 3) << 17) |
+           ((uint32_t)(m >> 4) << 24);
+  }
+};
 
-__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                         uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-      ::"r"(tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
+template <bool TF32>
+__device__ __forceinline__ void mma(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                    uint32_t accumulate) {
+  if constexpr (TF32) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+  } else {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+  }
 }
 
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
@@ -125,25 +146,31 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r) {
 
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-template <int BN>
+template <int BN, bool TF32>
 constexpr size_t tc_smem_bytes() {
-  return 1024 + (size_t)kStages * (kBM + 2 * BN) * kBK * 2 + 256;
+  using K = TcKind<TF32>;
+  return 1024 + (size_t)K::kStages * (K::kAPlanes * kBM + 2 * BN) * K::kBK * K::kElem + 256;
 }
 
-template <int BN>
+// Persistent GEMM over the 128 x BN output tiles; tma_a_lo is read by the
+// TF32 form only (the BF16 form is given tma_a twice).
+template <int BN, bool TF32>
 __global__ void __launch_bounds__(kThreads, 1)
-    dm_tc_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_b, TcParams p) {
+    dm_tc_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_a_lo,
+                 const __grid_constant__ CUtensorMap tma_b, TcParams p) {
+  using K = TcKind<TF32>;
   constexpr int NC = 2 * BN;                     // accumulator columns of a tile: hi products, then lo products
   constexpr uint32_t kTmemCols = 2 * NC;         // two accumulators (a power of two, <= 512)
-  constexpr int A_BYTES = kBM * kBK * 2;
-  constexpr int B_BYTES = 2 * BN * kBK * 2;      // hi rows, then lo rows: one 2*BN-row operand
-  constexpr int B_HALF = BN * kBK * 2;
+  constexpr int A_BYTES = kBM * K::kBK * K::kElem;
+  constexpr int B_BYTES = 2 * BN * K::kBK * K::kElem;  // hi rows, then lo rows: one 2*BN-row operand
+  constexpr int B_HALF = BN * K::kBK * K::kElem;
+  constexpr int S_BYTES = K::kAPlanes * A_BYTES + B_BYTES;
+  constexpr int kStages = K::kStages;
   static_assert(NC <= 256 && kTmemCols <= 512, "tile too wide for one MMA or for TMEM");
+  static_assert(S_BYTES % 1024 == 0, "stages must keep the 1024-byte swizzle alignment");
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  unsigned char* sa = smem;
-  unsigned char* sb = smem + kStages * A_BYTES;
-  uint64_t* full = reinterpret_cast<uint64_t*>(sb + kStages * B_BYTES);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * S_BYTES);
   uint64_t* empty = full + kStages;
   uint64_t* tfull = empty + kStages;   // [2] accumulator ready for the epilogue
   uint64_t* tempty = tfull + 2;        // [2] accumulator read back, free for the next tile
@@ -189,16 +216,21 @@ __global__ void __launch_bounds__(kThreads, 1)
           break;
         }
         issued = it + 1;
-        mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
-        tma_load_2d(sa + s * A_BYTES, &tma_a, &full[s], kb * kBK, m0);
-        tma_load_2d(sb + s * B_BYTES, &tma_b, &full[s], kb * kBK, n0);
-        tma_load_2d(sb + s * B_BYTES + B_HALF, &tma_b, &full[s], kb * kBK, p.batch_pad + n0);
+        unsigned char* st = smem + s * S_BYTES;
+        mbar_expect_tx(&full[s], S_BYTES);
+        tma_load_2d(st, &tma_a, &full[s], kb * K::kBK, m0);
+        if constexpr (TF32) tma_load_2d(st + A_BYTES, &tma_a_lo, &full[s], kb * K::kBK, m0);
+        unsigned char* sb = st + K::kAPlanes * A_BYTES;
+        tma_load_2d(sb, &tma_b, &full[s], kb * K::kBK, n0);
+        tma_load_2d(sb + B_HALF, &tma_b, &full[s], kb * K::kBK, p.batch_pad + n0);
       }
       if (!ok) break;
     }
   } else if (warp == 1 && lane == 0) {
-    // MMA issuer
-    constexpr uint32_t idesc = make_idesc(kBM, NC);
+    // MMA issuer: per K step one MMA of N = 2*BN (A times the hi and the lo
+    // coefficient rows); the TF32 form adds the remainder of A times the hi
+    // rows (N = BN) into the first half
+    constexpr uint32_t idesc2 = K::idesc(kBM, NC), idesc1 = K::idesc(kBM, BN);
     int it = 0, local = 0;
     for (int t = blockIdx.x; t < p.tiles; t += gridDim.x, local++) {
       const int acc = local & 1;
@@ -213,10 +245,13 @@ __global__ void __launch_bounds__(kThreads, 1)
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t a0 = smem_u32(sa + s * A_BYTES), b0 = smem_u32(sb + s * B_BYTES);
+        const uint32_t a0 = smem_u32(smem + s * S_BYTES), b0 = a0 + K::kAPlanes * A_BYTES;
 #pragma unroll
-        for (int k = 0; k < kBK / kUK; k++)
-          mma_bf16(d, sw128_desc(a0 + k * kUK * 2), sw128_desc(b0 + k * kUK * 2), idesc, (kb | k) ? 1u : 0u);
+        for (int k = 0; k < K::kBK / K::kUK; k++) {
+          const uint64_t bd = sw128_desc(b0 + k * K::kUK * K::kElem);
+          mma<TF32>(d, sw128_desc(a0 + k * K::kUK * K::kElem), bd, idesc2, (kb | k) ? 1u : 0u);
+          if constexpr (TF32) mma<TF32>(d, sw128_desc(a0 + A_BYTES + k * K::kUK * K::kElem), bd, idesc1, 1u);
+        }
         mma_commit(&empty[s]);
       }
       if (!ok) break;
@@ -409,14 +444,15 @@ int launch_tc(const void* modes, const void* coefs_t, int n_pix, int n_act_pad, 
   if (s) return s;
   s = encode_2d(&tb, coefs_t, (uint64_t)n_act_pad, (uint64_t)(2 * batch_pad), kBK, BN);
   if (s) return s;
-  const size_t smem = tc_smem_bytes<BN>();
-  OOPAO_CUDA_TRY(cudaFuncSetAttribute(dm_tc_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const size_t smem = tc_smem_bytes<BN, false>();
+  OOPAO_CUDA_TRY(cudaFuncSetAttribute(dm_tc_kernel<BN, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
   const int tiles_n = batch_pad / BN, tiles = tiles_n * ceil_div(n_pix, kBM);
   int dev = 0, sms = 0;
   OOPAO_CUDA_TRY(cudaGetDevice(&dev));
   OOPAO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   TcParams p{n_pix, batch, n_act_pad / kBK, batch_pad, tiles_n, tiles, scale, base, out, err};
-  dm_tc_kernel<BN><<<std::min(tiles, sms), kThreads, smem, st>>>(ta, tb, p);
+  dm_tc_kernel<BN, false><<<std::min(tiles, sms), kThreads, smem, st>>>(ta, ta, tb, p);
   return OOPAO_OK;
 }
 
@@ -430,169 +466,7 @@ int launch_tc(const void* modes, const void* coefs_t, int n_pix, int n_act_pad, 
 // one MMA of N = 2*BN multiplies Ahi by [Bhi; Blo] into both halves of the
 // accumulator and a second of N = BN adds Alo*Bhi to the hi half; the rest is
 // the persistent pipeline of dm_tc_kernel with FP32 tiles (32 per 128-byte row).
-constexpr int kBK3 = 32;     // FP32 actuators per stage: one 128-byte swizzle row
-constexpr int kUK3 = 8;      // K of one tcgen05.mma kind::tf32
-constexpr int kStages3 = 3;
-
-// Instruction descriptor, kind::tf32: F32 accumulator, TF32 A and B (format
-// code 2), both K-major.
-__host__ __device__ constexpr uint32_t make_idesc_tf32(int m, int n) {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                         uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
-      ::"r"(tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-
-template <int BN>
-constexpr size_t tc3_smem_bytes() {
-  return 1024 + (size_t)kStages3 * (2 * kBM + 2 * BN) * kBK3 * 4 + 256;
-}
-
-template <int BN>
-__global__ void __launch_bounds__(kThreads, 1)
-    dm_tc3_kernel(const __grid_constant__ CUtensorMap tma_ahi, const __grid_constant__ CUtensorMap tma_alo,
-                  const __grid_constant__ CUtensorMap tma_b, TcParams p) {
-  constexpr int NC = 2 * BN;
-  constexpr uint32_t kTmemCols = 2 * NC;
-  constexpr int A_BYTES = kBM * kBK3 * 4;        // one of Ahi, Alo
-  constexpr int B_BYTES = 2 * BN * kBK3 * 4;     // Bhi rows, then Blo rows
-  constexpr int B_HALF = BN * kBK3 * 4;
-  constexpr int S_BYTES = 2 * A_BYTES + B_BYTES;
-  static_assert(NC <= 256 && kTmemCols <= 512, "tile too wide for one MMA or for TMEM");
-  extern __shared__ unsigned char smem_raw[];
-  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages3 * S_BYTES);
-  uint64_t* empty = full + kStages3;
-  uint64_t* tfull = empty + kStages3;
-  uint64_t* tempty = tfull + 2;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 2);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages3; s++) {
-      mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
-    }
-    for (int a = 0; a < 2; a++) {
-      mbar_init(&tfull[a], 1);
-      mbar_init(&tempty[a], kEpiWarps);
-    }
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(kTmemCols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const uint32_t tmem = *tmem_slot;
-
-  int issued = 0;
-  if (warp == 0 && lane == 0) {
-    int it = 0;
-    for (int t = blockIdx.x; t < p.tiles; t += gridDim.x) {
-      const int m0 = (t / p.tiles_n) * kBM, n0 = (t % p.tiles_n) * BN;
-      bool ok = true;
-      for (int kb = 0; kb < p.nk; kb++, it++) {
-        const int s = it % kStages3;
-        if (!wait_or_abort(&empty[s], ((it / kStages3) & 1) ^ 1, p.err, 1)) {
-          ok = false;
-          break;
-        }
-        issued = it + 1;
-        unsigned char* st = smem + s * S_BYTES;
-        mbar_expect_tx(&full[s], S_BYTES);
-        tma_load_2d(st, &tma_ahi, &full[s], kb * kBK3, m0);
-        tma_load_2d(st + A_BYTES, &tma_alo, &full[s], kb * kBK3, m0);
-        tma_load_2d(st + 2 * A_BYTES, &tma_b, &full[s], kb * kBK3, n0);
-        tma_load_2d(st + 2 * A_BYTES + B_HALF, &tma_b, &full[s], kb * kBK3, p.batch_pad + n0);
-      }
-      if (!ok) break;
-    }
-  } else if (warp == 1 && lane == 0) {
-    constexpr uint32_t idesc2 = make_idesc_tf32(kBM, NC), idesc1 = make_idesc_tf32(kBM, BN);
-    int it = 0, local = 0;
-    for (int t = blockIdx.x; t < p.tiles; t += gridDim.x, local++) {
-      const int acc = local & 1;
-      if (!wait_or_abort(&tempty[acc], ((local >> 1) & 1) ^ 1, p.err, 2)) break;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t d = tmem + (uint32_t)(acc * NC);
-      bool ok = true;
-      for (int kb = 0; kb < p.nk; kb++, it++) {
-        const int s = it % kStages3;
-        if (!wait_or_abort(&full[s], (it / kStages3) & 1, p.err, 3)) {
-          ok = false;
-          break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t ahi = smem_u32(smem + s * S_BYTES), alo = ahi + A_BYTES, b0 = ahi + 2 * A_BYTES;
-#pragma unroll
-        for (int k = 0; k < kBK3 / kUK3; k++) {
-          const uint64_t bd = sw128_desc(b0 + k * kUK3 * 4);
-          mma_tf32(d, sw128_desc(ahi + k * kUK3 * 4), bd, idesc2, (kb | k) ? 1u : 0u);
-          mma_tf32(d, sw128_desc(alo + k * kUK3 * 4), bd, idesc1, 1u);
-        }
-        mma_commit(&empty[s]);
-      }
-      if (!ok) break;
-      mma_commit(&tfull[acc]);
-    }
-  } else if (warp >= 2) {
-    const int q = warp & 3;
-    int local = 0;
-    for (int t = blockIdx.x; t < p.tiles; t += gridDim.x, local++) {
-      const int acc = local & 1;
-      const bool ok = wait_or_abort(&tfull[acc], (local >> 1) & 1, p.err, 4);
-      if (!__all_sync(0xffffffffu, ok)) break;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const int m0 = (t / p.tiles_n) * kBM, n0 = (t % p.tiles_n) * BN;
-      const int pix = m0 + q * 32 + lane;
-      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * NC);
-#pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 16) {
-        uint32_t hi[16], lo[16];
-        tmem_ld16(taddr + (uint32_t)c0, hi);
-        tmem_ld16(taddr + (uint32_t)(BN + c0), lo);
-        tmem_ld_wait();
-        if (pix < p.n_pix) {
-#pragma unroll
-          for (int j = 0; j < 16; j++) {
-            const int b = n0 + c0 + j;
-            if (b < p.batch) {
-              const size_t o = (size_t)b * p.n_pix + pix;
-              const float v = __uint_as_float(hi[j]) + __uint_as_float(lo[j]);
-              p.out[o] = v * p.scale + (p.base ? p.base[o] : 0.f);
-            }
-          }
-        }
-      }
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&tempty[acc]);
-    }
-  }
-  __syncwarp();
-  if (warp == 0 && lane == 0 && *(volatile int*)p.err != 0) {
-    for (int kb = issued - 1; kb >= 0 && kb >= issued - kStages3; kb--)
-      tma::mbar_wait(&full[kb % kStages3], (kb / kStages3) & 1, nullptr, 0);
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  if (warp == 0) {
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
-  }
-}
+constexpr int kBK3 = TcKind<true>::kBK;  // FP32 actuators per stage (n_act_pad granularity)
 
 __device__ __forceinline__ float to_tf32(float x) {
   uint32_t r;
@@ -639,14 +513,15 @@ int launch_tc3(const float* modes2, const float* coefs2, int n_pix, int n_act_pa
   s = encode_2d(&tb, coefs2, (uint64_t)n_act_pad, (uint64_t)(2 * batch_pad), kBK3, BN, CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
                 4);
   if (s) return s;
-  const size_t smem = tc3_smem_bytes<BN>();
-  OOPAO_CUDA_TRY(cudaFuncSetAttribute(dm_tc3_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const size_t smem = tc_smem_bytes<BN, true>();
+  OOPAO_CUDA_TRY(cudaFuncSetAttribute(dm_tc_kernel<BN, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
   const int tiles_n = batch_pad / BN, tiles = tiles_n * ceil_div(n_pix, kBM);
   int dev = 0, sms = 0;
   OOPAO_CUDA_TRY(cudaGetDevice(&dev));
   OOPAO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   TcParams p{n_pix, batch, n_act_pad / kBK3, batch_pad, tiles_n, tiles, scale, base, out, err};
-  dm_tc3_kernel<BN><<<std::min(tiles, sms), kThreads, smem, st>>>(tah, tal, tb, p);
+  dm_tc_kernel<BN, true><<<std::min(tiles, sms), kThreads, smem, st>>>(tah, tal, tb, p);
   return OOPAO_OK;
 }
 
