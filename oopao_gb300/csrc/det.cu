@@ -58,32 +58,34 @@ __global__ void __launch_bounds__(kDetThreads) det_tail(float* frames, int npix,
     m = block_max(m, red);
     if (max_out && threadIdx.x == 0) max_out[blockIdx.x] = m;
   }
-  const float levels = exp2f((float)p.bits);
+  // the ADC levels and the integer conversion in double: 2^bits - 1 is not
+  // a float for bits > 24, and a float top level would wrap to 0 in the
+  // unsigned conversion
+  const double levels = exp2((double)p.bits);
   for (int i = threadIdx.x; i < npix; i += blockDim.x) {
-    float v = f[i] * p.gain;
+    double v = (double)(f[i] * p.gain);
     if (p.bits > 0) {
       if (p.fwc <= 0.f) {
-        v = v / m * levels;
+        v = v / (double)m * levels;
       } else {
-        v = v / p.fwc * (levels - 1.f);
-        if (p.clip_zero) v = fmaxf(v, 0.f);
-        v = fminf(v, levels - 1.f);
+        v = v / (double)p.fwc * (levels - 1.0);
+        if (p.clip_zero) v = fmax(v, 0.0);
+        v = fmin(v, levels - 1.0);
       }
     }
-    if (p.log_scale) v = log10f(v);
+    if (p.log_scale) v = log10(v);
     if (p.out_bits > 0) {
       // conversion to an unsigned integer: truncation toward zero; values
       // outside the type's range wrap modulo 2^bits
-      v = truncf(v);
+      v = trunc(v);
       if (p.out_bits < 64) {
         const double span = exp2((double)p.out_bits);
-        double d = fmod((double)v, span);
-        if (d < 0) d += span;
-        v = (float)d;
+        v = fmod(v, span);
+        if (v < 0) v += span;
       }
     }
-    if (p.bg) v -= p.bg[i];
-    f[i] = v;
+    if (p.bg) v -= (double)p.bg[i];
+    f[i] = (float)v;
   }
 }
 

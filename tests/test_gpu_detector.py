@@ -140,3 +140,20 @@ def test_pyramid_camera_integrates_two_steps():
     fsum = torch.as_tensor(frames[0] + frames[1], dtype=torch.float32, device=wfs._dev)[None]
     _, sig = wfs._signals(fsum)
     np.testing.assert_allclose(wfs.signal, sig[0].double().cpu().numpy(), rtol=1e-5, atol=1e-6)
+
+
+def test_adc_wide_words_against_oracle():
+    """32-bit ADC with a full well, and a 32-bit ADC without: the top level
+    2^32 - 1 and the unsigned conversion stay in range (no wrap to 0 of the
+    saturated pixels), against the float64 oracle."""
+    from oopao_gb300.detector import Detector
+    from oracle import detector_oracle as D
+    g = load('detector_tiny')
+    frames = g['frames'][:2]
+    for kw in (dict(bits=32, FWC=20000), dict(bits=32), dict(bits=16, FWC=20000, gain=3)):
+        with contextlib.redirect_stdout(io.StringIO()):
+            cam = Detector(12, **kw)
+            got = cam._integrate_device(torch.as_tensor(frames, dtype=torch.float32, device='cuda'), wfs=False)
+        ref = np.array([D.readout(f, **kw) for f in frames])
+        assert np.abs(got.double().cpu().numpy() - ref).max() <= 1e-6 * np.abs(ref).max() + 1.0, kw
+        assert got.min().item() >= 0
