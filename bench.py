@@ -1324,6 +1324,28 @@ def run_case(args):
         torch.cuda.nvtx.range_pop()
         out = {'case': args.case, 'batch': args.batch, 'reps': args.reps,
                'dframe_norm': float(df.double().norm().item())}
+    elif args.case == 'bioedge20':
+        # Bi-O Edge 20x20 (120 px, N=264, 48 points, four knife-edge masks):
+        # --reps measurements of --batch seeded OPDs through the one-axis path
+        import oopao_gb300 as og
+        with _quiet():
+            tel = og.Telescope(resolution=120, diameter=8.0, samplingTime=1e-3)
+            ngs = og.Source(optBand='V0', magnitude=8)
+            ngs * tel
+            wfs = og.BioEdge(nSubap=20, telescope=tel, modulation=3, lightRatio=0.5, nTheta_user_defined=48,
+                             max_batch=args.batch)
+        ngs ** tel
+        opd = torch.randn((args.batch, 120, 120), device='cuda', generator=g) * 50e-9
+        scale = 2 * np.pi / ngs.wavelength
+        frame, _ = wfs._measure_frames(opd, scale)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push('case')
+        for _ in range(args.reps):
+            frame, _ = wfs._measure_frames(opd, scale)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        out = {'case': args.case, 'batch': args.batch, 'reps': args.reps,
+               'path': N.call('oopao_pwfs_separable', wfs.plan.h), 'frame_sum': float(frame.double().sum().item())}
     elif args.case == 'clgsc':
         out = {'case': args.case, 'cl_gsc_20x20': cl_gsc()}
     elif args.case == 'cl':
@@ -1358,7 +1380,7 @@ def main():
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline and accuracy legs')
     ap.add_argument('--no-extra', action='store_true',
                     help='skip the interaction-matrix comparisons and the closed-loop rate')
-    ap.add_argument('--case', default=None, help='run a small profiling workload (%s, dm40, jvp40, gsc, next, clgsc, cl, c4, c5, dmproj) instead'
+    ap.add_argument('--case', default=None, help='run a small profiling workload (%s, dm40, jvp40, bioedge20, gsc, next, clgsc, cl, c4, c5, dmproj) instead'
                     % ', '.join(CASES))
     ap.add_argument('--batch', type=int, default=16)
     ap.add_argument('--reps', type=int, default=3)

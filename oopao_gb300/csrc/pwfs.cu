@@ -695,6 +695,8 @@ bool factor_mask(const float2* m, int n, std::vector<float2>* mrow, std::vector<
 // device.
 cudaError_t sep_attrs_for(const SepPasses* s, int res, int* ctas) {
   cudaError_t e = cudaFuncSetAttribute(s->rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_rows);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(s->rows_int, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_rows);
   for (int m = 0; m < 3 && e == cudaSuccess; m++)
     e = cudaFuncSetAttribute(s->cols[m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_cols(res));
   if (e == cudaSuccess)
@@ -1201,30 +1203,27 @@ __global__ void __launch_bounds__(256) edge_transpose(const float2* __restrict__
 }
 
 struct EdgeBinArgs {
-  const float2* lines;  // mask m at lines + m * mask_stride: [items][ng[m]][res][n] filtered lines
-  size_t mask_stride;
-  int ng[8], axis[8];
-  const float* gsum;    // [2][k]: weight of each x-group, then of each y-group
-  int k, res, n, off, cam, bin, n_masks;
+  const float* inten;   // mask m at inten + m * mask_stride: [slices][items][res][n] line intensity
+  size_t mask_stride, slice_stride;
+  int slices;           // partial sums over slices of groups (pwfs_srows_int)
+  int axis[8];
+  int res, n, off, cam, bin, n_masks;
   float* frame;         // [items][n_masks][cam][cam]
   float* raw;           // [items][n_masks][n][n] un-binned intensity, or null
-  float nsq;            // n * n
 };
 
-// Camera frames of masks that vary along one axis only.  |G_k|^2 is then the
-// squared filtered line of point k's group (the phasor along the other axis
-// has unit modulus and is not transformed), so a frame is sum over groups of
-// (group weight) |line|^2: lines along x hold the pupil rows [off, off+res) of
-// the grid, lines along y its pupil columns.  One CTA per (camera row, mask,
-// item): each thread sums a grid column over the camera row's bin rows and
-// the groups (writing each grid pixel to raw when asked), then the columns
-// are summed in bins.
+// Camera frames of masks that vary along one axis only, from the line
+// intensities of pwfs_srows_int: lines along x are the pupil rows
+// [off, off+res) of the grid, lines along y its pupil columns (the field was
+// transposed), the rest of the grid is dark.  One CTA per (camera row, mask,
+// item): each thread sums a grid column over the camera row's bin rows
+// (writing each grid pixel to raw when asked), then the columns are summed in
+// bins.
 __global__ void __launch_bounds__(256) edge_bin(EdgeBinArgs a) {
   extern __shared__ float colsum[];  // [n]
   const int cy = blockIdx.x, m = blockIdx.y, b = blockIdx.z;
-  const int ng = a.ng[m], ax = a.axis[m], res = a.res, n = a.n;
-  const float* w = a.gsum + (ax ? a.k : 0);
-  const float2* L = a.lines + m * a.mask_stride + (size_t)b * ng * res * n;
+  const int ax = a.axis[m], res = a.res, n = a.n;
+  const float* I = a.inten + m * a.mask_stride + (size_t)b * res * n;
   for (int X = threadIdx.x; X < n; X += blockDim.x) {
     float s = 0.f;
     for (int dy = 0; dy < a.bin; dy++) {
@@ -1232,11 +1231,7 @@ __global__ void __launch_bounds__(256) edge_bin(EdgeBinArgs a) {
       const int line = ax == 0 ? Y - a.off : X - a.off, pos = ax == 0 ? X : Y;
       float v = 0.f;
       if (line >= 0 && line < res)
-        for (int g = 0; g < ng; g++) v = fmaf(w[g], cabs2(L[((size_t)g * res + line) * n + pos]), v);
-      // the line phasors carry the 1/n^2 of the 2-D inverse transform, but
-      // only one axis went through the unnormalised transform pair (a gain
-      // of n): n^2 back in intensity
-      v *= a.nsq;
+        for (int sl = 0; sl < a.slices; sl++) v += I[sl * a.slice_stride + (size_t)line * n + pos];
       if (a.raw) a.raw[(((size_t)b * a.n_masks + m) * n + Y) * n + X] = v;
       s += v;
     }
@@ -1326,27 +1321,35 @@ int measure_edge(const oopao_pwfs_plan* p, const float* opd, double phase_scale,
                  float* raw, char* base, size_t usable, cudaStream_t st) {
   const SepPasses* s = p->sep;
   const int n = p->n, res = p->res, cam = p->cam, nm = p->n_masks;
-  const int gmax = std::max(p->ngroups, p->nygroups);
   bool any_y = false;
   for (int m = 0; m < nm; m++) any_y |= p->edge_axis[m] == 1;
-  // per item: the field (and its transpose), then each mask's filtered lines
-  const size_t lines_mask = (size_t)gmax * res * n;  // float2 per item and mask (room for either axis)
-  const size_t item = sizeof(float2) * ((size_t)res * res * (any_y ? 2 : 1) + (size_t)nm * lines_mask);
-  if (item + 1024 > usable) return OOPAO_ERR_WORKSPACE;
-  const int bc = (int)std::min<size_t>((size_t)batch, (usable - 1024) / item);
+  // slices of groups per row launch: enough CTAs for about two waves
+  const int ngmax = std::max(p->ngroups, p->nygroups), blocks = ceil_div(res, s->l_rows);
+  const int target = 2 * std::max(1, p->sep_cols_ctas);
+  auto slices_for = [&](int nb) { return std::max(1, std::min(ngmax, ceil_div(target, blocks * nb))); };
+  // per item: the field (and its transpose), then each mask's line intensity slices
+  const int sl1 = slices_for(1);
+  auto item_bytes = [&](int sl) {
+    return sizeof(float2) * (size_t)res * res * (any_y ? 2 : 1) + sizeof(float) * (size_t)nm * sl * res * n;
+  };
+  if (item_bytes(sl1) + 1024 > usable) return OOPAO_ERR_WORKSPACE;
+  int bc = (int)std::min<size_t>((size_t)batch, (usable - 1024) / item_bytes(sl1));
+  const int slices = slices_for(bc);
   float2* field = (float2*)base;
   float2* field_t = field + (size_t)bc * res * res;
-  float2* lines = field_t + (any_y ? (size_t)bc * res * res : 0);
+  float* inten = (float*)(field_t + (any_y ? (size_t)bc * res * res : 0));
   EdgeBinArgs ea{};
-  ea.lines = lines;
-  ea.mask_stride = (size_t)bc * lines_mask;
-  for (int m = 0; m < nm; m++) {
-    ea.axis[m] = p->edge_axis[m];
-    ea.ng[m] = p->edge_axis[m] ? p->nygroups : p->ngroups;
-  }
-  ea.gsum = p->weights_on ? p->d_gsum_w : p->d_gsum;
-  ea.k = p->k; ea.res = res; ea.n = n; ea.off = p->off; ea.cam = cam; ea.bin = p->bin; ea.n_masks = nm;
-  ea.nsq = (float)n * (float)n;
+  ea.inten = inten;
+  ea.slices = slices;
+  ea.slice_stride = (size_t)bc * res * n;
+  ea.mask_stride = (size_t)slices * bc * res * n;
+  for (int m = 0; m < nm; m++) ea.axis[m] = p->edge_axis[m];
+  ea.res = res; ea.n = n; ea.off = p->off; ea.cam = cam; ea.bin = p->bin; ea.n_masks = nm;
+  const float* gsum = p->weights_on ? p->d_gsum_w : p->d_gsum;
+  // the line phasors carry the 1/n^2 of the 2-D inverse transform, but only
+  // one axis goes through the unnormalised transform pair (a gain of n): n^2
+  // back in intensity
+  const float nsq = (float)n * (float)n;
   int launches = 0;
   for (int b0 = 0; b0 < batch; b0 += bc) {
     const int nb = std::min(bc, batch - b0);
@@ -1360,10 +1363,13 @@ int measure_edge(const oopao_pwfs_plan* p, const float* opd, double phase_scale,
     }
     for (int m = 0; m < nm; m++) {
       const bool ya = p->edge_axis[m] == 1;
-      SepRowsArgs ra{p->d_tw, ya ? field_t : field, ya ? p->d_ygrowfac : p->d_growfac, p->d_edge_filt + (size_t)m * n,
-                     lines + (size_t)m * ea.mask_stride, res, ea.ng[m], 0 /* support at line position 0 */};
-      OOPAO_CUDA_TRY(launch_pdl(s->rows, dim3(ceil_div(res, s->l_rows), ea.ng[m], nb), dim3(s->t * s->l_rows),
-                                s->smem_rows, st, ra));
+      const int ng = ya ? p->nygroups : p->ngroups, g_per = ceil_div(ng, slices);
+      SepRowsIntArgs ra{p->d_tw, ya ? field_t : field, ya ? p->d_ygrowfac : p->d_growfac,
+                        p->d_edge_filt + (size_t)m * n, gsum + (ya ? p->k : 0), inten + (size_t)m * ea.mask_stride,
+                        ea.slice_stride, res, ng, g_per, nsq};
+      // every slice writes its partial sums (a slice past the last group writes zeros)
+      OOPAO_CUDA_TRY(launch_pdl(s->rows_int, dim3(blocks, slices, nb), dim3(s->t * s->l_rows), s->smem_rows, st,
+                                ra));
       launches++;
     }
     ea.frame = frame + (size_t)b0 * nm * cam * cam;

@@ -171,6 +171,84 @@ __global__ void __launch_bounds__(T* L) pwfs_srows(SepRowsArgs a) {
       [] {}, [] {});
 }
 
+struct SepRowsIntArgs {
+  const float2* tw;
+  const float2* field;   // [B][res][res]
+  const float2* rowfac;  // [ng][res] phasor of each group along the line
+  const float2* mrow;    // [N] the 1-D mask factor (filter along the line)
+  const float* gw;       // [ng] weight of each group (its points, or their weights)
+  float* inten;          // [slices][B][res][N] sum over a slice's groups of gw |filtered line|^2, times scale
+  size_t slice_stride;   // floats between slices
+  int res, ng, g_per;    // groups, groups per slice (grid y = slices)
+  float scale;
+};
+
+// Row pass of the one-axis path (masks that vary along the line's axis
+// only): per pupil line, the filtered line of every group of the CTA's slice
+// of groups, gw |.|^2 summed in registers over them, then written once.  The
+// groups' lines never go to memory; slices keep small batches on every SM.
+template <int N, int R1, int R2, int T, int L, int NZ>
+__global__ void __launch_bounds__(T* L) pwfs_srows_int(SepRowsIntArgs a) {
+  constexpr int R1P = pad_odd(R1), R2P = pad_odd(R2);
+  constexpr int LS1 = xchg_stride(R2 * R1P, T, L, R1P, R2, R1);
+  constexpr int LS2 = xchg_stride(R1 * R2P, T, L, R2P, R1, R2);
+  constexpr bool ALIAS = (R1 + T - 1) / T == 1;
+  constexpr int PBA = (R2 + T - 1) / T;
+  extern __shared__ float2 sm[];
+  float2* tw = sm;
+  float2* twi = sm + N;
+  float2* mf = sm + 2 * N;
+  float2* b1 = sm + 3 * N;
+  float2* b2 = ALIAS ? b1 : b1 + L * LS1;
+  const int tid = threadIdx.x;
+  const int l = tid / T, t = tid - (tid / T) * T;
+  for (int i = tid; i < N; i += T * L) {
+    tw[i] = a.tw[(i % R1) * (i / R1)];
+    const float2 w = a.tw[(i % R2) * (i / R2)];
+    twi[i] = make_float2(w.x, -w.y);
+    mf[i] = a.mrow[i];
+  }
+  pdl_wait();  // the field comes from the previous kernel
+  __syncthreads();
+  const int b = blockIdx.z, row = blockIdx.x * L + l;
+  const bool active = row < a.res;
+  const int res = a.res;
+  const float2* fld = a.field + ((size_t)b * res + (active ? row : 0)) * res;
+  float acc[PBA][R1];
+#pragma unroll
+  for (int p = 0; p < PBA; p++)
+#pragma unroll
+    for (int q = 0; q < R1; q++) acc[p][q] = 0.f;
+  const int g0 = blockIdx.y * a.g_per, g1 = min(a.ng, g0 + a.g_per);
+  for (int g = g0; g < g1; g++) {
+    if (ALIAS && g > g0) __syncthreads();  // the previous group's exchange reads are done
+    const float2* rf = a.rowfac + (size_t)g * res;
+    const float w = a.gw[g];
+    sep_chain_x<N, R1, R2, T, R1P, R2P, ALIAS, NZ>(
+        t, b1 + l * LS1, b2 + l * LS2, tw, twi,
+        [&](int, int m, int j) {
+          const int jc = j + m * R2;
+          return (active && jc < res) ? cmul(fld[jc], rf[jc]) : make_float2(0.f, 0.f);
+        },
+        [&](int u) { return mf[u]; },
+        [&](int p, int, const float2* v) {
+#pragma unroll
+          for (int q = 0; q < R1; q++) acc[p][q] = fmaf(w, cabs2(v[q]), acc[p][q]);
+        },
+        [] {}, [] {});
+  }
+  if (!active) return;
+  float* out = a.inten + blockIdx.y * a.slice_stride + ((size_t)b * res + row) * N;
+#pragma unroll
+  for (int p = 0; p < PBA; p++) {
+    const int j = t + p * T;
+    if (j < R2) {
+#pragma unroll
+      for (int q = 0; q < R1; q++) out[j + q * R2] = acc[p][q] * a.scale;
+    }
+  }
+}
+
 struct SepColsArgs {
   const float2* tw;
   const float2* mcol;    // [N] mask factor along a column (row frequency)
@@ -544,6 +622,7 @@ struct SepPasses {
   int n, r1, r2, t, l_rows, l_cols;
   int nz;  // stage-A inputs read per butterfly: the pupil must satisfy res <= nz * r2
   void (*rows)(SepRowsArgs);
+  void (*rows_int)(SepRowsIntArgs);  // the one-axis path's row pass (filtered-line intensity over groups)
   void (*cols[3])(SepColsArgs);  // indexed by kSepIntensity / kSepTangent / kSepStore
   void (*cols_adj)(SepAdjArgs);
   void (*rows_adj)(SepAdjArgs);
@@ -572,6 +651,7 @@ SepPasses make_sep() {
   s.n = N; s.r1 = R1; s.r2 = R2; s.t = T; s.l_rows = LR; s.l_cols = LC;
   s.nz = NZ;
   s.rows = pwfs_srows<N, R1, R2, T, LR, NZ>;
+  s.rows_int = pwfs_srows_int<N, R1, R2, T, LR, NZ>;
   s.cols[kSepIntensity] = pwfs_scols<N, R1, R2, T, LC, kSepIntensity, MAXREG, SHARE, NZ>;
   s.cols[kSepTangent] = pwfs_scols<N, R1, R2, T, LC, kSepTangent, MAXREG, SHARE, NZ>;
   s.cols[kSepStore] = pwfs_scols<N, R1, R2, T, LC, kSepStore, MAXREG, SHARE, NZ>;
