@@ -337,6 +337,19 @@ int oopao_atm_update(double* maps, float* mirror, int n_layers, int n, int slots
                      int n_inner, int n_outer, const double* normals, double* range, const double* scale, int res,
                      float* opd, int* step, int advance, int* err, void* stream);
 
+/* Boiling of the layers (AR(1) decorrelation; replaces Atmosphere.apply_boiling,
+ * OOPAO/Atmosphere.py:387-408, called by updateLayer :457 before the frozen-flow
+ * moves): maps[layers[k]] = alpha[k] * maps[layers[k]] + beta[k] * phi[t][k]
+ * for k < n_boil, in float64 with separately rounded products.  Run it before
+ * oopao_atm_update of the same step, on the same stream.
+ * maps: device float64 [n_layers][n][n] (the first ping-pong half);
+ * phi: device float64 [n_steps][n_boil][n][n] new screens;
+ * layers, alpha, beta: HOST arrays [n_boil] (layers increasing);
+ * step: device int32 counter selecting t (as oopao_atm_update: err set to 1
+ *   and nothing changes outside [0, n_steps)), or NULL with n_steps = 1. */
+int oopao_atm_boil(double* maps, int n_layers, int n, const double* phi, int n_boil, const int* layers,
+                   const double* alpha, const double* beta, const int* step, int n_steps, int* err, void* stream);
+
 /* Adjoint of the projection (no reference counterpart; used by the
  * gradients of wfs.signal with respect to dm.coefs):
  * out[a][b] = scale * sum_p modes_t[a][p] * g[b][p];

@@ -72,6 +72,8 @@ SIGNATURES = {
     'oopao_atm_update': (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p,
                                  c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p,
                                  c_void_p, c_int, c_void_p, c_void_p]),
+    'oopao_atm_boil': (c_int, [c_void_p, c_int, c_int, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                               c_int, c_void_p, c_void_p]),
     'oopao_pwfs_ad_workspace_bytes': (c_size_t, [c_void_p, c_int]),
     'oopao_pwfs_jvp': (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_double, c_int, c_void_p, c_void_p,
                                c_size_t, c_void_p]),

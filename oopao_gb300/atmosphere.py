@@ -20,6 +20,12 @@ The moves, sub-pixel offsets and extrusion normals of each step are planned
 on the host ahead of time with the reference's arithmetic (``updateLayer``
 :450-514) and each layer's ``RandomState(seed + 1000 i)``.
 
+Boiling layers (``t_boiling``, ``apply_boiling`` :387-408) decorrelate
+before each step's moves: map = alpha map + beta phi, phi a new screen drawn
+on the host with the layer's seed counter (``oopao_atm_boil`` on the GPU).
+A captured closed loop draws the screens of its whole horizon up front
+(``boiling_horizon``).
+
 The sub-pixel shift is the reference's scikit-image ``warp(order=3)``: the
 bicubic convolution kernel (Keys, a = -0.5) with zeros outside the map and
 the output clipped to the map's range.
@@ -104,8 +110,6 @@ class Atmosphere:
                  t_boiling=None):
         if angular_spectrum_propagation or geometric_phase_backup or unwrap_diffractive_phase:
             raise OopaoError('oopao_gb300 Atmosphere propagates geometrically only')
-        if t_boiling is not None:
-            raise OopaoError('Boiling layers (t_boiling) are not supported by oopao_gb300')
         if elevation != 90.0:
             raise OopaoError('oopao_gb300 Atmosphere supports zenith pointing (elevation=90) only')
         if mode == 1:
@@ -121,6 +125,7 @@ class Atmosphere:
         self._L0 = L0
         self.fractionalR0 = list(fractionalR0)
         self.nLayer = n
+        self._t_boiling = self.get_t_boiling(t_boiling)
         self._windSpeed = list(windSpeed)
         self._windDirection = list(windDirection)
         self.altitude = list(altitude)
@@ -215,6 +220,7 @@ class Atmosphere:
             L.rs = RandomState(seed + i * 1000)
             m = maps[0, i].view(-1)
             m.view(n, n)[1:-1, 1:-1] = torch.as_tensor(scr, device=d)
+            L.boiling_seed = 100000 + seed + i * 100000
             if self.compute_covariance:
                 w = torch.as_tensor(L.rs.normal(size=self._B.shape[1]), device=d)
                 m[outer_idx] = self._A @ m[inner_idx] + self._B @ w
@@ -342,9 +348,13 @@ class Atmosphere:
         return torch.as_tensor([self.wavelength / 2 / np.pi * np.sqrt(f) for f in self.fractionalR0],
                                dtype=torch.float64, device=self._dev)
 
-    def _launch(self, advance=True, moved=True, stream=None):
+    def _launch(self, advance=True, moved=True, stream=None, boil=None):
         st = N.stream_handle(stream)
         res = self.telescope.resolution
+        if boil is not None and moved:
+            N.call('oopao_atm_boil', self._maps, self.nLayer, self._n, boil['phi'], len(boil['layers']),
+                   boil['layers'], boil['alpha'], boil['beta'], self._step_dev if boil['by_step'] else None,
+                   boil['steps'], self._err, st)
         if not moved:
             N.call('oopao_atm_update', self._maps, self._mirror, self.nLayer, self._n, 0, None, None, 0, None, None,
                    None, None, 0, 0, None, self._range, self._scale_dev, res, self._opd_dev, self._step_dev, 0,
@@ -359,9 +369,88 @@ class Atmosphere:
                len(self._inner_idx), len(self._outer_idx), self._normals_dev, self._range, self._scale_dev, res,
                self._opd_dev, self._step_dev, 1 if advance else 0, self._err, st)
 
+    # ------------------------------------------------------------------ boiling
+    def get_t_boiling(self, val):
+        """One boiling time per layer, None for frozen flow (OOPAO/Atmosphere.py:376-385)."""
+        if val is None:
+            return [None] * self.nLayer
+        if np.isscalar(val):
+            return [val] * self.nLayer
+        val = list(val)
+        if len(val) != self.nLayer:
+            raise OopaoError('Wrong value for t_boiling! Provide either a scalar '
+                             '(applied to each layer) or a list with a value per layer.')
+        return val
+
+    def _boil_coefs(self):
+        """(layer, alpha, beta) of the layers that boil at this sampling time:
+        alpha = exp(-dt / t_boiling), beta = sqrt(1 - alpha^2); layers with
+        no, a non-finite or a non-positive t_boiling, or with alpha >= 1 - 1e-6,
+        stay frozen (``apply_boiling`` :387-398)."""
+        out = []
+        dt = self.telescope.samplingTime
+        for i, t_b in enumerate(self._t_boiling):
+            if t_b is None or not np.isfinite(t_b) or t_b <= 0:
+                continue
+            alpha = float(np.exp(-dt / t_b))
+            if alpha >= 1.0 - 1e-6:
+                continue
+            out.append((i, alpha, float(np.sqrt(max(0.0, 1.0 - alpha ** 2)))))
+        return out
+
+    def _boil_screen(self, i, seed):
+        gen = ft_sh_phase_screen if self.mode == 2 else ft_phase_screen
+        L = self.layers[i]
+        return gen(self._r0, self._L0, self._n, L.D / L.resolution, seed=seed)
+
+    def _boil_table(self, coefs, phi, by_step):
+        """by_step: phi holds the screens of the steps [0, n) picked by the
+        device step counter; otherwise the one step of an eager update."""
+        return dict(phi=phi, steps=phi.shape[0], by_step=by_step, layers=N.host([c[0] for c in coefs], np.int32),
+                    alpha=N.host([c[1] for c in coefs], np.float64), beta=N.host([c[2] for c in coefs], np.float64))
+
+    def _boil_now(self):
+        """The boiling of one eager update: each boiling layer's seed counter
+        moves on and a new screen of the map's size is drawn with it on the
+        host, as the reference does, then blended on the GPU."""
+        coefs = self._boil_coefs()
+        if not coefs:
+            return None
+        phi = np.empty((1, len(coefs), self._n, self._n))
+        for k, (i, _, _) in enumerate(coefs):
+            self.layers[i].boiling_seed += 1
+            phi[0, k] = self._boil_screen(i, self.layers[i].boiling_seed)
+        return self._boil_table(coefs, torch.as_tensor(phi, device=self._dev), False)
+
+    def boiling_horizon(self, n_steps):
+        """The boiling screens of the steps [0, n_steps) after the last
+        generateNewPhaseScreen, on the GPU ([n_steps][boiling layers][n][n]
+        float64), for a captured closed loop whose device step counter picks
+        the step's screens: step t of layer i uses the seed
+        100000 + seed + 100000 i + t + 1, as t + 1 eager updates would.  None
+        when no layer boils."""
+        coefs = self._boil_coefs()
+        if not coefs:
+            return None
+        nbytes = n_steps * len(coefs) * self._n * self._n * 8
+        free = torch.cuda.mem_get_info(self._dev)[0]
+        if nbytes > 0.5 * free:
+            raise OopaoError('the boiling screens of %d steps need %.1f GB on the GPU (%.1f GB free); plan fewer '
+                             'steps' % (n_steps, nbytes / 1e9, free / 1e9))
+        phi = torch.empty((n_steps, len(coefs), self._n, self._n), dtype=torch.float64, device=self._dev)
+        for k, (i, _, _) in enumerate(coefs):
+            base = 100000 + self._seed + i * 100000
+            host = np.empty((n_steps, self._n, self._n))
+            for t in range(n_steps):
+                host[t] = self._boil_screen(i, base + t + 1)
+            phi[:, k].copy_(torch.as_tensor(host))
+        return self._boil_table(coefs, phi, True)
+
     def reset_state(self):
         """Back to the screens of the last generateNewPhaseScreen (same plan)."""
         self._maps[0].copy_(self._maps0)
+        for i, L in enumerate(self.layers):
+            L.boiling_seed = 100000 + self._seed + i * 100000
         self._step_dev.zero_()
         self._step = 0
         self._err.zero_()
@@ -382,7 +471,8 @@ class Atmosphere:
         need = self._step + 1
         if self._dev_plan_len < need:
             self.prepare(max(need, 2 * max(self._dev_plan_len, 16)))
-        self._launch(advance=True)
+        boil = self._boil_now()
+        self._launch(advance=True, boil=boil)
         self._step += 1
 
     # ------------------------------------------------------------------ outputs
@@ -449,6 +539,15 @@ class Atmosphere:
         if len(val) != self.nLayer:
             raise OopaoError('Wrong value for the wind-speed! Make sure that you inpute a wind-speed for each layer')
         self._windSpeed = list(val)
+
+    @property
+    def t_boiling(self):
+        return self._t_boiling
+
+    @t_boiling.setter
+    def t_boiling(self, val):
+        """Boiling times, applied from the next update on (OOPAO/Atmosphere.py:1104-1115)."""
+        self._t_boiling = self.get_t_boiling(val)
 
     @property
     def windDirection(self):

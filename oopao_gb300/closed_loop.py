@@ -178,13 +178,17 @@ class ClosedLoop:
         self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=d)
         self.layers = layers
         self._atm = None
+        self._boil = None
         if layers is not None and hasattr(layers, 'prepare'):
             # infinite-screen Atmosphere: plan the whole horizon, then its
             # device update is one more part of the captured step
             self._atm = layers
             layers.reset_state()
             layers.prepare(max_steps + 2)
-            layers._launch(advance=True)         # the first step's turbulence (one update)
+            # boiling layers: every step's new screens drawn up front, the
+            # device step counter picks them inside the graph
+            self._boil = layers.boiling_horizon(max_steps + 2)
+            layers._launch(advance=True, boil=self._boil)   # the first step's turbulence (one update)
             self._atm_opd = layers.device_opd().view(1, res, res)
         elif layers is not None:
             self._scr = [torch.as_tensor(s, device=d) for s in layers.screens]
@@ -235,7 +239,7 @@ class ClosedLoop:
             # tutorial updates it first in every iteration); each step then
             # prepares the next step's turbulence while the sensor runs
             self._atm.reset_state()
-            self._atm._launch(advance=True)
+            self._atm._launch(advance=True, boil=self._boil)
 
     def _science(self):
         lo, res = self._sci_lo, self.res
@@ -277,7 +281,7 @@ class ClosedLoop:
         with torch.cuda.stream(side):
             ss = N.stream_handle(side)
             if self._atm is not None:
-                self._atm._launch(advance=True, stream=side)
+                self._atm._launch(advance=True, stream=side, boil=self._boil)
             N.call('oopao_cl_pupil_rms', self.opd, self.pupil_idx, self.pupil_idx.numel(), self.step_counter,
                    self.wfe, self.max_steps, ss)
             if self.science:

@@ -10,6 +10,8 @@
 // the entries of the step held in a device counter, so the same launches
 // serve eager updates and a captured CUDA graph.
 //
+//   atm_boil     boiling (apply_boiling :387-408): map = alpha map + beta phi
+//                for the layers that boil, before the step's moves
 //   atm_shift    one add_row slot: interior one-pixel move (or plain copy
 //                when the slot is idle), map[s%2] -> map[(s+1)%2]
 //   atm_extrude  the new outer ring X = A Z + B w (float64), Z = the inner
@@ -211,6 +213,31 @@ __global__ void atm_opd(const float* __restrict__ mirror, const double* __restri
   opd[p] = acc;
 }
 
+struct AtmBoil {
+  int layer[kMaxAtmLayers];  // map of boiling layer k
+  double alpha[kMaxAtmLayers], beta[kMaxAtmLayers];
+};
+
+// Boiling (AR(1) decorrelation) of the maps before the step's moves:
+// map_l = alpha_k map_l + beta_k phi[t][k] for the k-th boiling layer.  The
+// products and the sum are rounded separately (no fused multiply-add), as
+// the float64 host arithmetic of the same update.
+__global__ void atm_boil(double* __restrict__ maps, const double* __restrict__ phi, AtmBoil b, const int* step,
+                         int n_steps, int n_boil, int n, int* err) {
+  int t = 0;
+  if (step != nullptr) {
+    t = atm_step(step, n_steps, err);
+    if (t < 0) return;
+  }
+  const int k = blockIdx.y;
+  const size_t nn = (size_t)n * n;
+  double* m = maps + (size_t)b.layer[k] * nn;
+  const double* f = phi + ((size_t)t * n_boil + k) * nn;
+  const double a = b.alpha[k], c = b.beta[k];
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += (size_t)gridDim.x * blockDim.x)
+    m[i] = __dadd_rn(__dmul_rn(a, m[i]), __dmul_rn(c, f[i]));
+}
+
 __global__ void atm_advance(int* step) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *step += 1;
 }
@@ -253,6 +280,30 @@ extern "C" int oopao_atm_update(double* maps, float* mirror, int n_layers, int n
     launches += 1;
   }
   oopao_count_launches(launches);
+  OOPAO_CUDA_TRY(cudaGetLastError());
+  return OOPAO_OK;
+}
+
+extern "C" int oopao_atm_boil(double* maps, int n_layers, int n, const double* phi, int n_boil, const int* layers,
+                              const double* alpha, const double* beta, const int* step, int n_steps, int* err,
+                              void* stream) {
+  OOPAO_CHECK_ARG(maps && phi && layers && alpha && beta, "NULL argument");
+  OOPAO_CHECK_ARG(n_layers > 0 && n_layers <= kMaxAtmLayers && n >= 8 && n_boil >= 1 && n_boil <= n_layers,
+                  "bad sizes (1 to 64 layers, 1 to n_layers boiling layers)");
+  OOPAO_CHECK_ARG(step != nullptr ? n_steps >= 1 : n_steps == 1,
+                  "a table of steps needs the device step counter; without it the table holds one step");
+  AtmBoil b{};
+  for (int k = 0; k < n_boil; k++) {
+    OOPAO_CHECK_ARG(layers[k] >= 0 && layers[k] < n_layers && (k == 0 || layers[k] > layers[k - 1]),
+                    "boiling layers must be distinct, increasing and below n_layers");
+    b.layer[k] = layers[k];
+    b.alpha[k] = alpha[k];
+    b.beta[k] = beta[k];
+  }
+  const size_t nn = (size_t)n * n;
+  const dim3 g((unsigned)ceil_div((int)nn, 256), n_boil);
+  atm_boil<<<g, 256, 0, (cudaStream_t)stream>>>(maps, phi, b, step, n_steps, n_boil, n, err);
+  oopao_count_launches(1);
   OOPAO_CUDA_TRY(cudaGetLastError());
   return OOPAO_OK;
 }

@@ -120,8 +120,10 @@ class OracleAtmosphere:
     """Reference atmosphere for an on-axis source (telescope fov 0)."""
 
     def __init__(self, res, diameter, sampling_time, r0, L0, fractional_r0, wind_speed, wind_direction,
-                 altitude, wavelength=500e-9):
+                 altitude, wavelength=500e-9, t_boiling=None):
         self.res, self.D, self.dt = res, diameter, sampling_time
+        n_layers = len(fractional_r0)
+        self.t_boiling = list(t_boiling) if t_boiling is not None else [None] * n_layers
         self.r0, self.L0 = r0, L0
         self.fractional_r0 = list(fractional_r0)
         self.wavelength = wavelength
@@ -168,6 +170,23 @@ class OracleAtmosphere:
             L.map[L.outer != 0] = L.A @ z + L.B @ L.rs.normal(size=L.B.shape[1])
             L.map[L.outer == 0] = L.opd.reshape(-1)
             L.not_done_once = True
+            L.boiling_seed = 100000 + seed + i * 100000
+
+    def _boil(self, i, L):
+        """``apply_boiling`` (:387-408): AR(1) decorrelation of the map,
+        map = alpha map + beta phi with alpha = exp(-dt / t_boiling) and phi a
+        fresh screen of the map's size; returns whether the layer boiled."""
+        t_b = self.t_boiling[i]
+        if t_b is None or not np.isfinite(t_b) or t_b <= 0:
+            return False
+        alpha = float(np.exp(-self.dt / t_b))
+        if alpha >= 1.0 - 1e-6:
+            return False
+        beta = float(np.sqrt(max(0.0, 1.0 - alpha ** 2)))
+        L.boiling_seed += 1
+        phi = ft_sh_phase_screen(self.r0, self.L0, L.map.shape[0], L.D / L.resolution, seed=L.boiling_seed)
+        L.map = alpha * L.map + beta * phi
+        return True
 
     def _add_row(self, L, step):
         """``add_row`` (:410-419): one-pixel shift, ring extrusion."""
@@ -179,9 +198,13 @@ class OracleAtmosphere:
         return shifted
 
     def update(self):
-        """``updateLayer`` for every layer (:450-514)."""
-        for L in self.layers:
+        """``updateLayer`` for every layer (:447-514): boiling first, then the
+        frozen-flow moves; a still layer that boiled shows its map's interior."""
+        for i, L in enumerate(self.layers):
+            boiled = self._boil(i, L)
             if L.vX == 0 and L.vY == 0:
+                if boiled:
+                    L.opd = L.map[L.outer == 0].reshape(L.resolution, L.resolution)
                 continue
             if L.not_done_once:
                 L.not_done_once = False

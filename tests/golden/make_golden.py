@@ -167,6 +167,12 @@ ATM_CASE = dict(res=32, diameter=8.0, r0=0.15, L0=25.0, fractionalR0=[0.5, 0.3, 
                 altitude=[0.0, 5000.0, 10000.0], steps=40)
 
 
+# boiling (AR(1) decorrelation): a still layer that boils, a fast diagonal
+# layer that boils, a slow layer that does not
+ATM_BOIL_CASE = dict(name='atm_boil', windSpeed=[0.0, 370.0, 10.0], windDirection=[0.0, 135.0, 30.0],
+                     t_boiling=[0.01, 0.005, None], steps=20)
+
+
 def case_atmosphere(OOPAO, name='atm_small', **p):
     """Infinite-screen atmosphere: OPD seen by an on-axis NGS after each of
     `steps` updates (the wind speeds are large so that every branch of the
@@ -181,8 +187,10 @@ def case_atmosphere(OOPAO, name='atm_small', **p):
         tel = Telescope(resolution=p['res'], diameter=p['diameter'], samplingTime=1e-3)
         ngs = Source(optBand='V0', magnitude=8)
         ngs * tel
+        extra = {'t_boiling': p['t_boiling']} if p.get('t_boiling') is not None else {}
         atm = Atmosphere(telescope=tel, r0=p['r0'], L0=p['L0'], fractionalR0=p['fractionalR0'],
-                         windSpeed=p['windSpeed'], windDirection=p['windDirection'], altitude=p['altitude'])
+                         windSpeed=p['windSpeed'], windDirection=p['windDirection'], altitude=p['altitude'],
+                         **extra)
         atm.initializeAtmosphere(tel)
         opds = []
         ngs ** atm * tel
@@ -683,6 +691,8 @@ def main():
             case_small(OOPAO, name, *args, **kw)
     if not only or 'atm_small' in only:
         case_atmosphere(OOPAO)
+    if not only or 'atm_boil' in only:
+        case_atmosphere(OOPAO, **ATM_BOIL_CASE)
     if not only or 'c5_screen' in only:
         case_large(OOPAO)
     if not only or 'c3' in only:

@@ -30,6 +30,20 @@ def test_oracle_matches_reference_atmosphere():
         assert np.linalg.norm(atm.opd - ref[t + 1]) < 1e-9 * np.linalg.norm(ref[t + 1]), t
 
 
+def test_oracle_matches_reference_boiling():
+    z = np.load(os.path.join(os.path.dirname(GOLDEN), 'atm_boil.npz'))
+    p = json.loads(str(z['params']))
+    atm = A.OracleAtmosphere(p['res'], p['diameter'], 1e-3, p['r0'], p['L0'], p['fractionalR0'], p['windSpeed'],
+                             p['windDirection'], p['altitude'], t_boiling=p['t_boiling'])
+    ref = z['opd']
+    assert np.linalg.norm(atm.opd - ref[0]) < 1e-12 * np.linalg.norm(ref[0])
+    for t in range(p['steps']):
+        atm.update()
+        assert np.linalg.norm(atm.opd - ref[t + 1]) < 1e-9 * np.linalg.norm(ref[t + 1]), t
+    # the still layer changes only through boiling
+    assert np.linalg.norm(ref[1] - ref[0]) > 0.05 * np.linalg.norm(ref[0])
+
+
 def test_package_screens_equal_oracle():
     from oopao_gb300 import atmosphere as P
     for seed in (0, 3):
@@ -51,3 +65,31 @@ def test_cubic_shift_properties():
     np.testing.assert_array_equal(A.cubic_shift(img, 0.0, 0.0), img)
     s = A.cubic_shift(img, 0.3, 0.7)
     assert s.min() >= img.min() and s.max() <= img.max()
+
+
+def test_boiling_arguments():
+    """t_boiling: a scalar for every layer, a list per layer, anything else an
+    error; which layers boil and their AR(1) coefficients (host only)."""
+    import contextlib
+    import io
+    import pytest
+    import oopao_gb300 as og
+    with contextlib.redirect_stdout(io.StringIO()):
+        tel = og.Telescope(resolution=32, diameter=8.0, samplingTime=1e-3)
+        ngs = og.Source(optBand='V0', magnitude=8)
+        ngs * tel
+    kw = dict(telescope=tel, r0=0.15, L0=25.0, fractionalR0=[0.5, 0.5], windSpeed=[1.0, 2.0],
+              windDirection=[0.0, 0.0], altitude=[0.0, 1000.0])
+    atm = og.Atmosphere(t_boiling=0.01, **kw)
+    assert atm.t_boiling == [0.01, 0.01]
+    with pytest.raises(og.OopaoError, match='t_boiling'):
+        og.Atmosphere(t_boiling=[0.01], **kw)
+    assert og.Atmosphere(**kw).t_boiling == [None, None]
+    # frozen: None, non-positive, non-finite, or alpha within 1e-6 of 1
+    atm.t_boiling = [None, 1e9]
+    assert atm._boil_coefs() == []
+    atm.t_boiling = [-1.0, float('inf')]
+    assert atm._boil_coefs() == []
+    atm.t_boiling = [None, 0.005]
+    (i, a, b), = atm._boil_coefs()
+    assert i == 1 and a == np.exp(-0.2) and abs(a * a + b * b - 1) < 1e-15
