@@ -61,3 +61,15 @@ def test_argument_validation_without_gpu(lib):
     st = N._lib.oopao_pwfs_plan_create(ctypes.byref(h), 30, 34, 17, 4, mask.ctypes.data, path.ctypes.data, 1.0, 1)
     assert st == 2
     assert b'prime factor' in N._lib.oopao_last_error()
+    # boiling: a one-step table without the step counter, layers out of order
+    dummy = np.zeros(8)
+    lay = np.array([1, 0], np.int32)
+    ab = np.array([0.9, 0.4])
+    f = N._lib.oopao_atm_boil
+    f.argtypes = N.SIGNATURES['oopao_atm_boil'][1]
+    st = f(dummy.ctypes.data, 2, 16, dummy.ctypes.data, 2, lay.ctypes.data, ab.ctypes.data, ab.ctypes.data, None, 2,
+           None, None)
+    assert st == 1 and b'step counter' in N._lib.oopao_last_error()
+    st = f(dummy.ctypes.data, 2, 16, dummy.ctypes.data, 2, lay.ctypes.data, ab.ctypes.data, ab.ctypes.data, None, 1,
+           None, None)
+    assert st == 1 and b'increasing' in N._lib.oopao_last_error()
