@@ -106,6 +106,7 @@ class BioEdge:
         self.cam._frame_host = np.zeros([2 * self._cam_eff, 2 * self._cam_eff])
         self.focal_plane_camera = Detector(int((modulation * 4 + 12) * self.zeroPaddingFactor))
         self.focal_plane_camera.is_focal_plane_camera = True
+        self.fov_l_d = self.resolution / self.zeroPaddingFactor
         self._lightRatio = lightRatio
         self.calibModulation = res / 2 - 1 if calibModulation >= res / 2 else calibModulation
         self.isInitialized = False
@@ -332,6 +333,62 @@ class BioEdge:
                 raw[:, i * n:(i + 1) * n, j * n:(j + 1) * n] = rtile
         return frame, raw
 
+    # ------------------------------------------------------------------ focal-plane camera
+    def _focal_plan(self):
+        """One-mask plan for the focal-plane intensity: the field before the
+        masks is the same for the four of them.  Rebuilt with the masks'
+        plans (mask, modulation or geometry changes)."""
+        plans = self.plans
+        if getattr(self, '_focal_for', None) is not plans:
+            tel = self.telescope
+            self._focal = _Plan(tel.resolution, self.resolution, self._cam_eff, self.mask[0], self.modulation_path,
+                                tel.resolution / tel.initial_resolution, True)
+            self._focal_for = plans
+        return self._focal
+
+    def _focal_device(self):
+        """Focal-plane intensity of the last measured wavefront, float32 device
+        tensor [N,N] (or [B,N,N]).  The reference keeps each modulation point's
+        focal field fft2(sqrt(0.5) A exp(i phi) phasor) once per mask
+        (OOPAO/BioEdge.py:435-443) and sums |.|^2 over that list, unweighted
+        (:1036-1038): 4 N^2 times the sum over points of |F_k/N|^2 of the
+        sqrt(0.5) field, which the plan's focal output gives."""
+        last = getattr(self, '_last_measure', None)
+        if last is None:
+            raise OopaoError('No wavefront measured yet')
+        opd, scale = last
+        plan = self._focal_plan()
+        plan.set_weights(None)
+        plan.set_amplitude(0.5 * np.asarray(self.src.intensity, dtype=np.float64), self._amplitude_key())
+        x = (opd if opd.ndim == 3 else opd[None]).contiguous()
+        B, n = x.shape[0], self.resolution
+        frame = torch.empty((B, self._cam_eff, self._cam_eff), dtype=torch.float32, device=self._dev)
+        focal = torch.empty((B, n, n), dtype=torch.float32, device=self._dev)
+        nb = plan.workspace_bytes(min(B, self.max_batch))
+        ws = self._ws.get(nb)
+        N.call('oopao_pwfs_measure_focal', plan.h, N.ptr(x), float(scale), B, N.ptr(frame), None, N.ptr(focal),
+               N.ptr(ws), nb, N.stream_handle())
+        focal *= 4.0 * n * n
+        return focal[0] if opd.ndim == 2 else focal
+
+    def get_modulation_frame(self, radius=6, norma=True):
+        """Zoom of the focal-plane camera frame on +-radius lambda/D
+        (OOPAO/BioEdge.py:822-838)."""
+        if radius <= 0:
+            warning('radius for the field of view must be a strictly positive number. Ignoring the input value.')
+            radius = self.telescope.resolution // 2
+        self.modulation_camera_frame = np.asarray(self.focal_plane_camera.frame, dtype=float)
+        n_trunc = int(self.resolution / 2 - radius * self.zeroPaddingFactor)
+        if n_trunc <= 0:
+            warning('radius Value is too high as the field of view is limited to ' + str(int(self.fov_l_d / 2)) +
+                    ' lambda/D -- ignoring')
+            zoom = self.modulation_camera_frame.copy()
+        else:
+            zoom = self.modulation_camera_frame[n_trunc:-n_trunc, n_trunc:-n_trunc]
+        if norma:
+            zoom = zoom / zoom.max()
+        return zoom
+
     # ------------------------------------------------------------------ signals
     def _quadrant_origins(self):
         cp = int(np.round((self._cam_eff / self.binning) / 2))
@@ -428,6 +485,7 @@ class BioEdge:
         single = opd.ndim == 2
         want_raw = self.keep_raw_data and (single or opd.shape[0] == 1)
         frame, raw = self._measure_frames(opd, scale, want_raw=want_raw)
+        self._last_measure = (opd, scale)
         frame = self.cam._integrate_device(frame, dt=self.telescope.samplingTime)
         self.cam._set_device_frame(frame)
         self._raw_dev = raw
@@ -475,7 +533,22 @@ class BioEdge:
     def __mul__(self, obj):
         if obj.tag == 'detector':
             if obj.is_focal_plane_camera:
-                raise OopaoError('The BioEdge focal-plane camera is not provided by oopao_gb300')
+                # OOPAO/BioEdge.py:1036-1044: centred crop of the focal-plane
+                # intensity to the camera size, then the camera's integration
+                intensity = self._focal_device()
+                if intensity.ndim == 3:
+                    intensity = intensity.sum(dim=0)
+                n = intensity.shape[0]
+                if obj.resolution > self.resolution:
+                    frame = intensity
+                    warning('Maximum resolution for focal plane camera is %i, cropping field to this dimension'
+                            % self.resolution)
+                else:
+                    h = obj.resolution // 2
+                    frame = intensity[n // 2 - h:n // 2 + h, n // 2 - h:n // 2 + h]
+                obj._integrated_time = getattr(obj, '_integrated_time', 0) + self.telescope.samplingTime
+                obj.integrate(frame)
+                return
             if obj is not self.cam:
                 raise OopaoError('Only the sensor camera wfs.cam is supported')
             return

@@ -84,6 +84,22 @@ class OracleBioEdge:
                 out[i * N:(i + 1) * N, j * N:(j + 1) * N] += np.abs(np.fft.ifft2(F * self.masks[q])) ** 2
         return out
 
+    def focal(self, phase):
+        """What the focal-plane camera sums: each point's focal field
+        fft2(sqrt(0.5) A exp(i(phi + TT_k)) phasor), kept once per mask
+        (``convolution`` :435-443), |.|^2 summed over that list
+        (``__mul__`` :1036-1038)."""
+        g = self.geom
+        N, res, c = g.N, g.res, g.center
+        lo = c - res // 2
+        amp = np.sqrt(self.intensity / self.tt.shape[0])
+        out = np.zeros((N, N))
+        for k in range(self.tt.shape[0]):
+            sup = np.zeros((N, N), dtype=np.complex128)
+            sup[lo:lo + res, lo:lo + res] = np.sqrt(0.5) * amp * np.exp(1j * (phase + self.tt[k].astype(np.float64)))
+            out += len(self.masks) * np.abs(np.fft.fft2(sup * g.phasor)) ** 2
+        return out
+
     def frame(self, phase):
         return P.set_binning(self.raw(phase), self.geom.N / self.geom.cam)
 

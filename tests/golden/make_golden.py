@@ -262,6 +262,12 @@ def case_bioedge(OOPAO, name, res, n_subap, modulation, light_ratio, seeds=(3, 4
         ngs ** tel * dm * wfs
     rec.update(dm_coefs=coefs, dm_phase=np.array(ngs.phase), dm_raw=np.array(wfs.raw_data),
                dm_frame=np.array(wfs.cam.frame), dm_signal=np.array(wfs.signal), dm_signal_2D=np.array(wfs.signal_2D))
+    # focal-plane (modulation) camera of the same measurement: the reference
+    # keeps each point's field once per mask (BioEdge.py:435-443, :1036-1044)
+    with _quiet():
+        wfs * wfs.focal_plane_camera
+    rec.update(dm_focal=np.sum(np.abs(np.asarray(wfs.modulation_camera_em)) ** 2, axis=0),
+               dm_focal_cam=np.array(wfs.focal_plane_camera.frame), n_focal_fields=len(wfs.modulation_camera_em))
     ph = screen(res, seeds[1], 2.0) * tel.pupil
     with _quiet():
         dm.coefs = 0

@@ -1,7 +1,8 @@
 """Bi-O Edge drop-in against golden vectors made by the unmodified reference:
 geometry, valid pixels, reference slopes, a DM measurement through
 ``ngs**tel*dm*wfs``, a screen through ``wfs_measure`` and push-pull IM
-columns.  FP32 path bounds: 1e-5 (frames, signals), 1e-4 (IM columns)."""
+columns, the focal-plane camera.  FP32 path bounds: 1e-5 (frames, signals,
+focal-plane frames), 1e-4 (IM columns)."""
 import contextlib
 import io
 import json
@@ -57,6 +58,23 @@ def test_dm_measurement(system):
     assert O.rel_l2(wfs.cam.frame, d['dm_frame']) < 1e-5
     assert O.rel_l2(wfs.signal_2D, d['dm_signal_2D']) < 1e-5
     assert O.rel_l2(wfs.signal, d['dm_signal']) < 1e-5
+
+
+def test_focal_plane_camera(system):
+    """wfs * wfs.focal_plane_camera after the DM measurement: the reference's
+    sum over its list of four fields per modulation point, cropped to the
+    camera; the zoom of get_modulation_frame follows it."""
+    d, tel, ngs, dm, wfs = system
+    dm.coefs = d['dm_coefs']
+    ngs ** tel * dm * wfs
+    with _quiet():
+        wfs * wfs.focal_plane_camera
+    assert O.rel_l2(wfs.focal_plane_camera.frame, d['dm_focal_cam']) < 1e-5
+    # radius 8 lambda/D: a crop inside both cases' camera frames (72 of N=72, 80 of N=128)
+    n_trunc = int(wfs.resolution / 2 - 8 * wfs.zeroPaddingFactor)
+    ref = d['dm_focal_cam'][n_trunc:-n_trunc, n_trunc:-n_trunc]
+    assert ref.size > 0
+    assert O.rel_l2(wfs.get_modulation_frame(radius=8), ref / ref.max()) < 1e-5
 
 
 def test_screen_measurement(system):

@@ -56,6 +56,16 @@ def test_dm_and_screen_measurements(case):
     assert O.rel_l2(s, d['screen_signal']) < TOL
 
 
+def test_focal_plane_camera(case):
+    d, b = case
+    f = b.focal(d['dm_phase'])
+    assert int(d['n_focal_fields']) == 4 * b.tt.shape[0]
+    assert O.rel_l2(f, d['dm_focal']) < TOL
+    n, m = f.shape[0], d['dm_focal_cam'].shape[0]
+    crop = f[n // 2 - m // 2:n // 2 + m // 2, n // 2 - m // 2:n // 2 + m // 2]
+    assert O.rel_l2(crop, d['dm_focal_cam']) < TOL
+
+
 @pytest.mark.parametrize('kw', [dict(), dict(grey_width=1.0, quadrants_numbering=(2, 3, 0, 1)),
                                 dict(grey_width=0.5, grey_length=2, sx=[1, 0, -1, 0.5], sy=[0, 1, 0.5, -1]),
                                 dict(sx=0.5, sy=-0.25)],
