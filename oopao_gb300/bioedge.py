@@ -401,6 +401,33 @@ class BioEdge:
         r, c = org[2 * (n - 1)], org[2 * (n - 1) + 1]
         return f[r:r + cp, c:c + cp]
 
+    def grabFullQuadrant(self, n, cameraFrame=None):
+        """Half-frame block n of a camera frame (OOPAO/BioEdge.py:855-868), the
+        half size from the frame itself, the negative starts as -n_tot // 2."""
+        f = np.array(self.cam.frame) if cameraFrame is None else cameraFrame
+        n_tot = f.shape[0]
+        if n == 4:
+            return f[:n_tot // 2, :n_tot // 2]
+        if n == 3:
+            return f[:n_tot // 2, -n_tot // 2:]
+        if n == 1:
+            return f[-n_tot // 2:, -n_tot // 2:]
+        if n == 2:
+            return f[-n_tot // 2:, :n_tot // 2]
+        raise OopaoError('quadrant number must be 1, 2, 3 or 4')
+
+    def signalProcessing(self, cameraFrame=None):
+        """(signal_2D, signal) through the signal kernel, float64 host arrays
+        (OOPAO/BioEdge.py:729-767).  Both supported modes read their quadrants
+        from the camera's own frame whatever the argument, as the reference
+        does."""
+        own = self.cam.frame
+        if own is None:
+            raise OopaoError('The camera has no frame yet')
+        x = torch.as_tensor(np.ascontiguousarray(own, dtype=np.float32), device=self._dev)[None]
+        s2d, sig = self._signals(x)
+        return s2d[0].to('cpu', torch.float64).numpy(), sig[0].to('cpu', torch.float64).numpy()
+
     def _norma_const(self):
         return self.src.nPhoton * self.telescope.samplingTime * (self.telescope.D / self.nSubap) ** 2
 

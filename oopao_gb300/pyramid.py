@@ -473,6 +473,51 @@ class Pyramid:
         r, c = org[2 * (n - 1)], org[2 * (n - 1) + 1]
         return f[r:r + npx, c:c + npx]
 
+    def grabFullQuadrant(self, n, cameraFrame=None):
+        """Half-frame block n of a camera frame (OOPAO/Pyramid.py:963-976); the
+        half size is taken from the camera's resolution, the negative starts
+        as -n_tot // 2 (one more pixel for an odd size), as in the reference."""
+        n_tot = self.cam.resolution
+        f = np.array(self.cam.frame) if cameraFrame is None else cameraFrame
+        if n == 3:
+            return f[:n_tot // 2, :n_tot // 2]
+        if n == 4:
+            return f[:n_tot // 2, -n_tot // 2:]
+        if n == 1:
+            return f[-n_tot // 2:, -n_tot // 2:]
+        if n == 2:
+            return f[-n_tot // 2:, :n_tot // 2]
+        raise OopaoError('quadrant number must be 1, 2, 3 or 4')
+
+    def signalProcessing(self, cameraFrame=None):
+        """(signal_2D, signal) of a camera frame through the signal kernel,
+        float64 host arrays (OOPAO/Pyramid.py:835-926).  As in the reference,
+        the slopes-maps modes read their quadrants (and the camera_flux
+        normalisation) from the camera's own frame whatever the argument; the
+        full-frame modes map the argument, fullFrame_camera_flux and
+        fullFrame_sum_flux normalised by the camera frame's mean or sum."""
+        own = self.cam.frame
+        if own is None:
+            raise OopaoError('The camera has no frame yet')
+        full = self.postProcessing.startswith('fullFrame')
+        use_arg = full and cameraFrame is not None
+        f = np.asarray(cameraFrame if use_arg else own, dtype=np.float64)
+        if f.shape != np.shape(own):
+            raise OopaoError('cameraFrame must have the camera frame shape %s' % (np.shape(own),))
+        x = torch.as_tensor(np.ascontiguousarray(f, dtype=np.float32), device=self._dev)[None]
+        s2d, sig = self._signals(x)
+        s2d = s2d[0].to('cpu', torch.float64).numpy()
+        if use_arg and self.postProcessing in ('fullFrame_camera_flux', 'fullFrame_sum_flux'):
+            own = np.asarray(own, dtype=np.float64)
+            if self.postProcessing == 'fullFrame_camera_flux':
+                ratio = f.mean() / own.mean()
+            else:
+                ratio = f.sum() / own.sum()
+            ref = self.referenceSignal_2D
+            s2d = (s2d + ref) * ratio - ref
+            return s2d, s2d[np.where(self.validSignal == 1)]
+        return s2d, sig[0].to('cpu', torch.float64).numpy()
+
     # ------------------------------------------------------------------ device measurement
     def _amplitude_key(self):
         return (id(self.src), self.src._intensity_version)

@@ -1,0 +1,21 @@
+"""Host-side quadrant blocks of the drop-in sensors (no GPU: the methods only
+slice a given frame)."""
+import numpy as np
+
+
+def test_full_quadrant_blocks():
+    """grabFullQuadrant of both sensors on even and odd frames: the half size
+    n_tot // 2 and the negative starts -n_tot // 2 of the reference
+    (OOPAO/Pyramid.py:963-976, OOPAO/BioEdge.py:855-868)."""
+    import types
+    from oopao_gb300.bioedge import BioEdge
+    from oopao_gb300.pyramid import Pyramid
+    for n_tot, h in ((44, 22), (45, 22)):
+        f = np.arange(n_tot * n_tot, dtype=float).reshape(n_tot, n_tot)
+        o = types.SimpleNamespace(cam=types.SimpleNamespace(resolution=n_tot, frame=f))
+        lo, hi = slice(None, h), slice(n_tot - (n_tot + 1) // 2, None)
+        want_pyr = {3: f[lo, lo], 4: f[lo, hi], 1: f[hi, hi], 2: f[hi, lo]}
+        want_be = {4: f[lo, lo], 3: f[lo, hi], 1: f[hi, hi], 2: f[hi, lo]}
+        for q in (1, 2, 3, 4):
+            np.testing.assert_array_equal(Pyramid.grabFullQuadrant(o, q), want_pyr[q])
+            np.testing.assert_array_equal(BioEdge.grabFullQuadrant(o, q), want_be[q])
