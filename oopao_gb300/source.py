@@ -97,6 +97,12 @@ class Source:
                 obj.relay(self)
         return self
 
+    def print_optical_path(self):
+        """The objects the light went through, ' ~~> '-separated
+        (OOPAO/Source.py:197-204)."""
+        if self.optical_path is not None:
+            print(' ~~> '.join(str(o[0]) for o in self.optical_path))
+
     def reset(self):
         self.mask = 1
         self._opd = None

@@ -31,6 +31,7 @@ class Telescope:
         self.isPaired = False
         self.spatialFilter = None
         self.display_optical_path = display_optical_path
+        self.optical_path = None
         self.isInitialized = True
         self.initial_pupil = self.pupil.copy()
 
@@ -60,6 +61,14 @@ class Telescope:
         self.pixelArea = np.sum(self._pupil)
         self.pupilLogical = np.where(np.reshape(self._pupil, self.resolution ** 2) > 0)
         self.pupilReflectivity = self._pupil.astype(np.float64)
+
+    def print_optical_path(self):
+        """OOPAO/Telescope.py:575-585: the telescope's own optical path (which
+        the light's relays do not fill), else a notice."""
+        if self.optical_path is not None:
+            print(' ~~> '.join(str(o[0]) for o in self.optical_path))
+        else:
+            print('No light propagated through the telescope')
 
     def relay(self, src):
         if src.tag != 'source':

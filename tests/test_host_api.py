@@ -1,5 +1,5 @@
-"""Host-side quadrant blocks of the drop-in sensors (no GPU: the methods only
-slice a given frame)."""
+"""Host-only parts of the drop-in API (no GPU): the sensors' full-quadrant
+blocks of a given frame, the optical-path printers."""
 import numpy as np
 
 
@@ -19,3 +19,17 @@ def test_full_quadrant_blocks():
         for q in (1, 2, 3, 4):
             np.testing.assert_array_equal(Pyramid.grabFullQuadrant(o, q), want_pyr[q])
             np.testing.assert_array_equal(BioEdge.grabFullQuadrant(o, q), want_be[q])
+
+
+def test_print_optical_path(capsys):
+    """Source and Telescope print_optical_path (OOPAO/Source.py:197-204,
+    OOPAO/Telescope.py:575-585) after a host-only relay through the telescope."""
+    import oopao_gb300 as og
+    tel = og.Telescope(resolution=16, diameter=8.0, samplingTime=1e-3)
+    ngs = og.Source(optBand='V0', magnitude=8)
+    ngs * tel
+    capsys.readouterr()
+    ngs.print_optical_path()
+    tel.print_optical_path()
+    out = capsys.readouterr().out.splitlines()
+    assert out == ['NGS(V0) ~~> telescope', 'No light propagated through the telescope']
