@@ -26,7 +26,7 @@ import numpy as np
 import torch
 
 from . import _native as N
-from .tools import OopaoError, warning
+from .tools import OopaoError, set_binning, warning
 
 _UNSIGNED_BITS = {np.dtype(np.uint8): 8, np.dtype(np.uint16): 16, np.dtype(np.uint32): 32,
                   np.dtype(np.uint64): 64}
@@ -317,6 +317,17 @@ class Detector:
         self._frame_dev = None
 
     # ------------------------------------------------------------------ reports
+    def rebin(self, arr, new_shape):
+        """Sum-rebin of a host 2-D array to new_shape, as the mean of each
+        block times its size (OOPAO/Detector.py:174-179)."""
+        arr = np.asarray(arr)
+        fy, fx = arr.shape[0] // new_shape[0], arr.shape[1] // new_shape[1]
+        return arr.reshape(new_shape[0], fy, new_shape[1], fx).mean(-1).mean(1) * fy * fx
+
+    def set_binning(self, array, binning_factor, mode='sum'):
+        """Sum (or mean) binning of a host 2-D array (OOPAO/Detector.py:181-183)."""
+        return set_binning(np.asarray(array), binning_factor, mode)
+
     def computeSNR(self):
         """computeSNR (OOPAO/Detector.py:356-365)."""
         self.SNR_max = self.FWC / np.sqrt(self.FWC) if self.FWC is not None else np.nan

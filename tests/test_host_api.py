@@ -1,5 +1,6 @@
 """Host-only parts of the drop-in API (no GPU): the sensors' full-quadrant
-blocks of a given frame, the optical-path printers."""
+blocks of a given frame, the optical-path printers, the detector's host
+binning helpers."""
 import numpy as np
 
 
@@ -33,3 +34,15 @@ def test_print_optical_path(capsys):
     tel.print_optical_path()
     out = capsys.readouterr().out.splitlines()
     assert out == ['NGS(V0) ~~> telescope', 'No light propagated through the telescope']
+
+
+def test_detector_binning_helpers():
+    """Detector.rebin and Detector.set_binning on host arrays
+    (OOPAO/Detector.py:174-183): block sums."""
+    import oopao_gb300 as og
+    cam = og.Detector(8)
+    a = np.arange(64, dtype=float).reshape(8, 8)
+    want = a.reshape(4, 2, 4, 2).sum(axis=(1, 3))
+    np.testing.assert_allclose(cam.rebin(a, (4, 4)), want, rtol=1e-15)
+    np.testing.assert_array_equal(cam.set_binning(a, 2), want)
+    np.testing.assert_array_equal(cam.set_binning(a, 2, mode='mean'), want / 4)
