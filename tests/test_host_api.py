@@ -1,6 +1,6 @@
 """Host-only parts of the drop-in API (no GPU): the sensors' full-quadrant
 blocks of a given frame, the optical-path printers, the detector's host
-binning helpers."""
+binning helpers, the calibration vault's truncation setter."""
 import numpy as np
 
 
@@ -46,3 +46,27 @@ def test_detector_binning_helpers():
     np.testing.assert_allclose(cam.rebin(a, (4, 4)), want, rtol=1e-15)
     np.testing.assert_array_equal(cam.set_binning(a, 2), want)
     np.testing.assert_array_equal(cam.set_binning(a, 2, mode='mean'), want / 4)
+
+
+def test_vault_truncation_setter():
+    """CalibrationVault.nTrunc setter (OOPAO/calibration/CalibrationVault.py):
+    the truncated inverse and reconstruction from the stored U, s, V on the
+    host, against the reference's Mtrunc (nTrunc=1) of the im_offset_tiny
+    golden.  The thin SVD is taken in numpy here; the vault's own SVD runs on
+    the GPU."""
+    import os
+    from oopao_gb300.calibration import CalibrationVault
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden', 'im_offset_tiny.npz'))
+    for tag in ('pp', 'sp'):
+        D = z[tag + '_D_offset']
+        U, s, Vh = np.linalg.svd(D, full_matrices=False)
+        v = CalibrationVault.__new__(CalibrationVault)
+        v.s = v.eigenValues = s
+        v.U, v.V = U.T, Vh
+        v.nTrunc = 1
+        np.testing.assert_allclose(v.Mtrunc, z[tag + '_Mtrunc'], rtol=1e-9, atol=1e-9 * np.abs(v.Mtrunc).max())
+        assert v.Dtrunc.shape == D.shape and v.Vtrunc.shape == (len(s) - 1, D.shape[1])
+        assert v.cond == s[0] / s[-2]
+        # no truncation: the plain pseudo-inverse
+        v.nTrunc = 0
+        np.testing.assert_allclose(v.Mtrunc, np.linalg.pinv(D), rtol=1e-9, atol=1e-9 * np.abs(v.Mtrunc).max())
